@@ -1,0 +1,345 @@
+/*
+ * suzerain_gb300 -- GB300-native batched BSMBSM implicit solve.
+ *
+ * Two layers, both plain C ABI (pointers, sizes, no torch types):
+ *
+ *  1. Drop-in replacements for the reference's entry points on the
+ *     per-wavenumber implicit-solve path, with the reference's names,
+ *     signatures, argument meaning and error conventions.  Each is cited
+ *     beside its declaration.  Pointers may be host or device memory; host
+ *     data is staged through device memory and every computation runs on the
+ *     GPU (there is no CPU fallback: without a usable device the calls return
+ *     an error).
+ *
+ *  2. The batched device API (prefix sgb_) that one call per substep drives
+ *     thousands of (kx, kz) systems through: explicit operator apply, complex
+ *     band LU (complex128, or complex64 with FP64 refinement and complex128
+ *     fallback), solve, permutation.  Device pointers, a cudaStream_t
+ *     (passed as void*), caller-owned memory.
+ *
+ * Complex scalars are C99 double _Complex / float _Complex in C and
+ * std::complex<double> / std::complex<float> in C++ (layout compatible, as
+ * suzerain/complex.h:28-45 arranges for the reference).
+ */
+#ifndef SUZERAIN_GB300_H
+#define SUZERAIN_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+#include <complex>
+typedef std::complex<double> sgb_complex_double;
+typedef std::complex<float>  sgb_complex_float;
+extern "C" {
+#else
+#include <complex.h>
+typedef double _Complex sgb_complex_double;
+typedef float _Complex  sgb_complex_float;
+#endif
+
+/* ======================================================================== */
+/* 1. Drop-in replacements                                                  */
+/* ======================================================================== */
+
+/** BSMBSM geometry; same fields and meaning as suzerain/bsmbsm.h:104-116. */
+typedef struct suzerain_bsmbsm {
+    int S, n, kl, ku, ld, N, KL, KU, LD;
+} suzerain_bsmbsm;
+
+/** suzerain/bsmbsm.h:130-149 (static inline there; exported here). */
+suzerain_bsmbsm suzerain_bsmbsm_construct(int S, int n, int kl, int ku);
+/** q(i) = (i mod S) n + floor(i / S); suzerain/bsmbsm.h:162-169. */
+int suzerain_bsmbsm_q(int S, int n, int i);
+/** q^{-1}(i) = q with S and n exchanged; suzerain/bsmbsm.h:182-186. */
+int suzerain_bsmbsm_qinv(int S, int n, int i);
+
+/** y <- alpha P x + beta y ('N') or alpha P^T x + beta y ('T');
+ *  suzerain/bsmbsm.h:208-257, suzerain/bsmbsm_aPxpby_complex.def:36-329.
+ *  Returns 0, or the positive BLAS argument position of a bad argument
+ *  (1 trans, 2 S, 3 n, 58 x aliases y). */
+int suzerain_bsmbsm_saPxpby(char trans, int S, int n, const float alpha,
+                            const float *x, int incx, const float beta,
+                            float *y, int incy);
+int suzerain_bsmbsm_daPxpby(char trans, int S, int n, const double alpha,
+                            const double *x, int incx, const double beta,
+                            double *y, int incy);
+int suzerain_bsmbsm_caPxpby(char trans, int S, int n,
+                            const sgb_complex_float alpha,
+                            const sgb_complex_float *x, int incx,
+                            const sgb_complex_float beta,
+                            sgb_complex_float *y, int incy);
+int suzerain_bsmbsm_zaPxpby(char trans, int S, int n,
+                            const sgb_complex_double alpha,
+                            const sgb_complex_double *x, int incx,
+                            const sgb_complex_double beta,
+                            sgb_complex_double *y, int incy);
+
+/** Pack alpha B^{ihat,jhat} into band storage of P A P^T, zeroing the
+ *  block's positions outside B's band; suzerain/bsmbsm.h:338-381,
+ *  suzerain/bsmbsm_pack.def:36-122.  Returns 0 or the positive argument
+ *  position (511 when b aliases papt). */
+int suzerain_bsmbsm_dpack(int S, int n, int ihat, int jhat, int kl, int ku,
+                          const double alpha, const double *b, int ldb,
+                          int KL, int KU, double *papt, int ldpapt);
+int suzerain_bsmbsm_zpack(int S, int n, int ihat, int jhat, int kl, int ku,
+                          const sgb_complex_double alpha,
+                          const sgb_complex_double *b, int ldb, int KL, int KU,
+                          sgb_complex_double *papt, int ldpapt);
+int suzerain_bsmbsm_zdpack(int S, int n, int ihat, int jhat, int kl, int ku,
+                           const sgb_complex_double alpha, const double *b,
+                           int ldb, int KL, int KU, sgb_complex_double *papt,
+                           int ldpapt);
+/** packc / packf conveniences; suzerain/bsmbsm.h:407-468, :543-610. */
+int suzerain_bsmbsm_zpackc(const suzerain_bsmbsm *A, int ihat, int jhat,
+                           const sgb_complex_double alpha,
+                           const sgb_complex_double *b,
+                           sgb_complex_double *papt);
+int suzerain_bsmbsm_zpackf(const suzerain_bsmbsm *A, int ihat, int jhat,
+                           const sgb_complex_double alpha,
+                           const sgb_complex_double *b,
+                           sgb_complex_double *papt);
+int suzerain_bsmbsm_zdpackc(const suzerain_bsmbsm *A, int ihat, int jhat,
+                            const sgb_complex_double alpha, const double *b,
+                            sgb_complex_double *papt);
+int suzerain_bsmbsm_zdpackf(const suzerain_bsmbsm *A, int ihat, int jhat,
+                            const sgb_complex_double alpha, const double *b,
+                            sgb_complex_double *papt);
+
+/** Partial-pivot band LU, LAPACK zgbtrf/cgbtrf semantics and storage
+ *  ((2kl+ku+1) x n, 1-based ipiv, info > 0 at the first zero pivot);
+ *  wraps of suzerain/blas_et_al/lapack.c:185-198. */
+int suzerain_lapack_zgbtrf(const int m, const int n, const int kl,
+                           const int ku, sgb_complex_double *ab,
+                           const int ldab, int *ipiv);
+int suzerain_lapack_cgbtrf(const int m, const int n, const int kl,
+                           const int ku, sgb_complex_float *ab,
+                           const int ldab, int *ipiv);
+/** Band solve with a zgbtrf/cgbtrf factor, trans 'N', 'T' or 'C';
+ *  suzerain/blas_et_al/lapack.c:261-279. */
+int suzerain_lapack_zgbtrs(const char trans, const int n, const int kl,
+                           const int ku, const int nrhs,
+                           const sgb_complex_double *ab, const int ldab,
+                           const int *ipiv, sgb_complex_double *b,
+                           const int ldb);
+int suzerain_lapack_cgbtrs(const char trans, const int n, const int kl,
+                           const int ku, const int nrhs,
+                           const sgb_complex_float *ab, const int ldab,
+                           const int *ipiv, sgb_complex_float *b,
+                           const int ldb);
+
+/** Factor when *fact == 'N' (then *fact = 'F'), solve;
+ *  suzerain/blas_et_al/lapackext.c:127-147. */
+int suzerain_lapackext_zgbsv(char *const fact, const char trans, const int n,
+                             const int kl, const int ku, const int nrhs,
+                             sgb_complex_double *ab, const int ldab, int *ipiv,
+                             sgb_complex_double *b, const int ldb);
+int suzerain_lapackext_cgbsv(char *const fact, const char trans, const int n,
+                             const int kl, const int ku, const int nrhs,
+                             sgb_complex_float *ab, const int ldab, int *ipiv,
+                             sgb_complex_float *b, const int ldb);
+
+/** Complex64 LU with FP64 iterative refinement and complex128 fallback;
+ *  suzerain/blas_et_al/lapackext.h:258-299,
+ *  suzerain/blas_et_al/dsgbsvx.def:70-313.  Same 18 arguments.  ab must be
+ *  contiguous (ldab = kl+ku+1); afb returns the factor in LAPACK storage
+ *  (ldafb = 2kl+ku+1), complex64 packed at its start when *fact == 'S'.
+ *  The residual uses the reference gbmv's convention for trans 'C'
+ *  (suzerain/blas_et_al/gbmv.def:161-196 treats 'C' as 'T'). */
+int suzerain_lapackext_zcgbsvx(char *const fact, int *const apprx,
+                               const int aiter, char trans, const int n,
+                               const int kl, const int ku,
+                               sgb_complex_double *const ab,
+                               double *const afrob,
+                               sgb_complex_double *const afb, int *const ipiv,
+                               sgb_complex_double *const b,
+                               sgb_complex_double *const x, int *const siter,
+                               int *const diter, double *const tolsc,
+                               sgb_complex_double *const r, double *const res);
+
+/** y <- alpha op(A) x + beta y for a band A; suzerain/blas_et_al/blas.c:1035-1054
+ *  over suzerain/blas_et_al/gbmv.def ('C' takes the 'T' branch unconjugated). */
+int suzerain_blas_zgbmv(const char trans, const int m, const int n,
+                        const int kl, const int ku,
+                        const sgb_complex_double alpha,
+                        const sgb_complex_double *a, const int lda,
+                        const sgb_complex_double *x, const int incx,
+                        const sgb_complex_double beta, sgb_complex_double *y,
+                        const int incy);
+
+/** B-spline collocation operators; workspace layout of
+ *  suzerain/bsplineop.h:125-180 (transposed bands D_T). */
+enum suzerain_bsplineop_method {
+    SUZERAIN_BSPLINEOP_COLLOCATION_GREVILLE = 1,
+    SUZERAIN_BSPLINEOP_GALERKIN_L2
+};
+typedef struct suzerain_bsplineop_workspace {
+    enum suzerain_bsplineop_method method;
+    int k, n, nderiv;
+    int *kl, *ku;
+    int max_kl, max_ku, ld;
+    double **D_T;
+} suzerain_bsplineop_workspace;
+/** Replaces suzerain_bsplineop_alloc(gsl_bspline_workspace*, nderiv,
+ *  COLLOCATION_GREVILLE) (suzerain/bsplineop.c:102-202): the GSL workspace
+ *  argument becomes its defining data (order k and the breakpoints). */
+suzerain_bsplineop_workspace *
+sgb_bsplineop_alloc_breakpoints(int k, int nbreak, const double *breakpts,
+                                int nderiv);
+/** suzerain/bsplineop.c:205-219. */
+void suzerain_bsplineop_free(suzerain_bsplineop_workspace *w);
+/** y <- alpha D^nderiv x + beta y per right-hand side;
+ *  suzerain/bsplineop.c:261-298. */
+int suzerain_bsplineop_accumulate_complex(int nderiv, int nrhs,
+                                          const sgb_complex_double alpha,
+                                          const sgb_complex_double *x,
+                                          int incx, int ldx,
+                                          const sgb_complex_double beta,
+                                          sgb_complex_double *y, int incy,
+                                          int ldy,
+                                          const suzerain_bsplineop_workspace *w);
+
+/** Non-transposed collocation matrices d^m B_j(xi_i), m = 0..nderiv, as
+ *  LAPACK bands with the common trimmed kl/ku; bands may be NULL to query
+ *  n/kl/ku.  bands[(m*n + j)*ld + ku + i - j], ld = kl+1+ku. */
+int sgb_bspline_collocation_bands(int k, int nbreak, const double *breakpts,
+                                  int nderiv, int *n, int *kl, int *ku,
+                                  double *bands, double *abscissae);
+
+/** 0.5 (1 + tanh(delta (x/L - 1/2)) / tanh(delta/2)); suzerain/htstretch.c:112-125. */
+double suzerain_htstretch2(const double delta, const double L, const double x);
+/** Signed wavenumber of in-order index i; suzerain/inorder.h:92-96. */
+int suzerain_inorder_wavenumber(const int N, const int i);
+
+/** Scale complex wave-space field x (Ny x Nx x Nz, column-major, Y fastest)
+ *  by alpha (i kx)^dxcnt (i kz)^dzcnt, zeroing dealiased and Nyquist modes;
+ *  suzerain/diffwave.h:90-97, suzerain/diffwave.c:66-131. */
+int suzerain_diffwave_apply(const int dxcnt, const int dzcnt,
+                            const sgb_complex_double alpha,
+                            sgb_complex_double *x, const double Lx,
+                            const double Lz, const int Ny, const int Nx,
+                            const int dNx, const int dkbx, const int dkex,
+                            const int Nz, const int dNz, const int dkbz,
+                            const int dkez);
+
+/* ======================================================================== */
+/* 2. Batched device API                                                    */
+/* ======================================================================== */
+
+/** Last error message of this thread (static storage). */
+const char *sgb_last_error(void);
+/** 0 when a CUDA device of compute capability 10.3 is usable. */
+int sgb_device_ok(void);
+
+/** Complex elements of one system's row-panel LU factor:
+ *  N rows of U (KL+KU+1 each) then N columns of L (KL each). */
+long long sgb_factor_elems(int N, int KL, int KU);
+
+/** Batched partial-pivot LU of nsys packed bands (complex128, LAPACK packc
+ *  layout, ldab >= KL+KU+1 rows, system s at ab + s*ab_stride).  prec 'Z'
+ *  factors in complex128, 'C' in complex64 (the band is demoted on load).
+ *  fac: nsys * sgb_factor_elems complex of prec; ipiv nsys*N (1-based);
+ *  info nsys (zgbtrf semantics). */
+int sgb_gbtrf_batched(char prec, int nsys, int N, int KL, int KU,
+                      const void *ab, int ldab, long long ab_stride,
+                      void *fac, int *ipiv, int *info, void *stream);
+
+/** Batched solve op(A) x = b with row-panel factors; b, x complex128
+ *  (nsys x N, stride N).  x may equal b. */
+int sgb_gbtrs_batched(char prec, char trans, int nsys, int N, int KL, int KU,
+                      const void *fac, const int *ipiv, const void *b,
+                      void *x, void *stream);
+
+/** Row-panel factor -> LAPACK gbtrf storage ((2KL+KU+1) x N per system). */
+int sgb_factor_to_lapack(char prec, int nsys, int N, int KL, int KU,
+                         const void *fac, void *ab, void *stream);
+
+/** Refinement controls, the parameters of the zcgbsvx spec string. */
+typedef struct sgb_refine_spec {
+    int aiter, siter, diter;
+    double tolsc;
+} sgb_refine_spec;
+
+/** Per-system outputs of the mixed-precision driver (device pointers, any
+ *  may be NULL). fact: 'S' or 'D' per system. */
+typedef struct sgb_refine_report {
+    int *info, *siter, *diter;
+    double *res, *tolsc;
+    char *fact;
+} sgb_refine_report;
+
+/** Batched zcgbsvx over packed complex128 bands: b, x permuted complex128
+ *  (nsys x N).  Allocates its workspace internally on first use. */
+int sgb_zcgbsvx_batched(int nsys, int N, int KL, int KU, char trans,
+                        const void *ab, int ldab, long long ab_stride,
+                        const void *b, void *x, const sgb_refine_spec *spec,
+                        const sgb_refine_report *report, void *stream);
+
+/** One synthetic case (see sgb_case in the model header): bands and
+ *  coefficients.  For sgb_plan_create the pointers are HOST pointers. */
+typedef struct sgb_case {
+    int S, n, kl, ku, ld;
+    const double *M, *D1, *D2;
+    const double *a, *b, *c, *g;
+    unsigned dirichlet_mask;
+    int pad_;
+} sgb_case;
+
+/** A resident batch: one case, nsys wavenumber pairs, device workspace. */
+typedef struct sgb_plan sgb_plan;
+
+sgb_plan *sgb_plan_create(const sgb_case *host_case, int nsys,
+                          const double *kx, const double *kz,
+                          int max_double_slots);
+int sgb_plan_destroy(sgb_plan *p);
+/** Device bytes the plan holds. */
+size_t sgb_plan_device_bytes(const sgb_plan *p);
+
+/** One implicit substep for every system of the plan:
+ *    y = P (M + phi_exp L) u          (explicit operator, Dirichlet rows 0)
+ *    (M + phi_imp L) x = y            method 'Z': complex128 LU (zgbsv)
+ *                                     method 'M': complex64 LU + FP64 refine
+ *    u_out = P^T x
+ *  u_in/u_out: device, nsys x N complex128, natural (unpermuted) order.
+ *  phi_exp == 0 skips the explicit apply and uses u_in as y (P applied). */
+int sgb_plan_substep(sgb_plan *p, char method, double phi_exp, double phi_imp,
+                     const void *u_in, void *u_out,
+                     const sgb_refine_spec *spec, void *stream);
+
+/** Same, from and to host memory (copies inside the call). */
+int sgb_plan_substep_host(sgb_plan *p, char method, double phi_exp,
+                          double phi_imp, const void *u_in_host,
+                          void *u_out_host, const sgb_refine_spec *spec,
+                          void *stream);
+
+/** Copy the last substep's per-system statistics to host arrays (any may be
+ *  NULL): info, siter, diter, res (||r||_2), tolsc, fact ('S'/'D'). */
+int sgb_plan_report(const sgb_plan *p, int *info, int *siter, int *diter,
+                    double *res, double *tolsc, char *fact);
+
+/** Normwise backward error ||b - A x||_inf / (||A||_inf ||x||_inf + ||b||_inf)
+ *  of the last substep for every system, computed in FP64 on the device. */
+int sgb_plan_backward_error(sgb_plan *p, double *berr_host, void *stream);
+
+/** Record CUDA events around each phase of later substeps (on the stream
+ *  they run in); sgb_plan_timings returns "name total_ms calls" lines. */
+int sgb_plan_set_timing(sgb_plan *p, int on);
+int sgb_plan_timings(sgb_plan *p, char *buf, int buflen);
+/** Kernels this library has launched since load (all entry points). */
+long long sgb_launch_count(void);
+
+/** Synthetic inputs (host): seeded B-spline case and right-hand sides. */
+int sgb_synth_case(int S, int Ny, int k, double htdelta, double left,
+                   double right, double offscale, int complex_coupling,
+                   uint64_t seed, unsigned dirichlet_mask, int *kl, int *ku,
+                   double *M, double *D1, double *D2, double *a, double *b,
+                   double *c, double *g);
+int sgb_synth_wavenumbers(int Nx, int Nz, double Lx, double Lz, double *kx,
+                          double *kz);
+int sgb_synth_rhs(uint64_t seed, long long nsys, int N, double *u);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SUZERAIN_GB300_H */

@@ -1,0 +1,344 @@
+"""ORACLE — test infrastructure, not product code.
+
+ctypes access to
+  * oracle/_lib/liboracle.so   the C restatement of the reference's banded
+                               solve path (oracle/oracle.c), and
+  * oracle/_ref/libsuzref.so   the reference's own C sources of that path
+                               compiled against SciPy's OpenBLAS
+                               (oracle/ref/Makefile), present only where the
+                               reference checkout was available at build time.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
+this module, always as the checker.  Nothing in suzerain_gb300/ uses it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import glob
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "liboracle.so")
+REF_PATH = os.path.join(HERE, "_ref", "libsuzref.so")
+
+_i = C.c_int
+_d = C.c_double
+_p = C.c_void_p
+_cp = C.c_char_p
+
+
+class _Z(C.Structure):
+    """C99 double complex passed by value."""
+    _fields_ = [("re", C.c_double), ("im", C.c_double)]
+
+
+def _z(v) -> _Z:
+    v = complex(v)
+    return _Z(v.real, v.imag)
+
+
+def build(quiet: bool = True) -> None:
+    """Compile oracle.c (always) and the reference build (when possible)."""
+    out = subprocess.DEVNULL if quiet else None
+    subprocess.run(["make", "-C", HERE], check=True, stdout=out, stderr=out)
+    if os.path.isdir("/root/reference/suzerain"):
+        subprocess.run(["make", "-C", HERE, "ref"], check=True, stdout=out,
+                       stderr=out)
+
+
+def openblas_path() -> str | None:
+    """SciPy's bundled OpenBLAS, located by glob (x86 here, aarch64 on Grace)."""
+    try:
+        import scipy
+    except ImportError:  # pragma: no cover
+        return None
+    pats = [os.path.join(os.path.dirname(scipy.__file__) + ".libs",
+                         "libscipy_openblas*.so"),
+            os.path.join(os.path.dirname(scipy.__file__), ".dylibs",
+                         "libscipy_openblas*")]
+    for pat in pats:
+        hits = sorted(glob.glob(pat))
+        if hits:
+            return hits[0]
+    return None
+
+
+_lib = None
+_ref = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = C.CDLL(LIB_PATH)
+        L.orc_q.argtypes = [_i, _i, _i]
+        L.orc_qinv.argtypes = [_i, _i, _i]
+        L.orc_zaPxpby.argtypes = [C.c_char, _i, _i, _Z, _p, _i, _Z, _p, _i]
+        L.orc_zpack.argtypes = [_i] * 6 + [_Z, _p, _i, _i, _i, _p, _i]
+        L.orc_zdpack.argtypes = [_i] * 6 + [_Z, _p, _i, _i, _i, _p, _i]
+        for f in ("orc_builtin_zgbtrf", "orc_builtin_cgbtrf", "orc_zgbtrf",
+                  "orc_cgbtrf"):
+            getattr(L, f).argtypes = [_i, _i, _i, _p, _i, _p]
+        for f in ("orc_builtin_zgbtrs", "orc_builtin_cgbtrs", "orc_zgbtrs",
+                  "orc_cgbtrs"):
+            getattr(L, f).argtypes = [C.c_char, _i, _i, _i, _i, _p, _i, _p,
+                                      _p, _i]
+        L.orc_zgbmv.argtypes = [C.c_char, _i, _i, _i, _i, _Z, _p, _i, _p, _i,
+                                _Z, _p, _i]
+        L.orc_dznrm2.argtypes = [_i, _p]
+        L.orc_dznrm2.restype = _d
+        L.orc_zlangb_fro.argtypes = [_i, _i, _i, _p, _i]
+        L.orc_zlangb_fro.restype = _d
+        L.orc_zcgbsvx.argtypes = [_p, _p, _i, C.c_char, _i, _i, _i, _p, _p,
+                                  _p, _p, _p, _p, _p, _p, _p, _p, _p]
+        L.orc_use_openblas.argtypes = [_cp]
+        L.orc_assemble_packed.argtypes = [_i, _i, _i, _i, _p, _p, _p, _i, _p,
+                                          _p, _p, _p, _p, _i, _i]
+        L.orc_block_coefs.argtypes = [_i, _p, _p, _p, _p, _d, _d, _d, _p, _p,
+                                      _p]
+        L.orc_batch_solve.argtypes = (
+            [_i, _i, _i, _i, _i, C.c_char, _p, _p, _p, _i, _p, _p, _p, _p, _p,
+             _p, _p, _d, _d, _p, _p, _p, _i, _i, _i, _i, _d, _p, _p, _p, _p,
+             _p, _p, _i])
+        L.orc_batch_solve.restype = _d
+        _lib = L
+    return _lib
+
+
+def ref():
+    """The reference's own compiled C, or None when it was not built here."""
+    global _ref
+    if _ref is None:
+        if not os.path.exists(REF_PATH):
+            return None
+        L = C.CDLL(REF_PATH)
+        L.suzerain_bsmbsm_zaPxpby.argtypes = [C.c_char, _i, _i, _Z, _p, _i,
+                                              _Z, _p, _i]
+        L.suzerain_bsmbsm_zpack.argtypes = [_i] * 6 + [_Z, _p, _i, _i, _i, _p,
+                                                       _i]
+        L.suzerain_bsmbsm_zdpack.argtypes = [_i] * 6 + [_Z, _p, _i, _i, _i,
+                                                        _p, _i]
+        L.suzerain_bsmbsm_dpack.argtypes = [_i] * 6 + [_d, _p, _i, _i, _i, _p,
+                                                       _i]
+        L.suzerain_lapack_zgbtrf.argtypes = [_i, _i, _i, _i, _p, _i, _p]
+        L.suzerain_lapack_cgbtrf.argtypes = [_i, _i, _i, _i, _p, _i, _p]
+        L.suzerain_lapack_zgbtrs.argtypes = [C.c_char, _i, _i, _i, _i, _p, _i,
+                                             _p, _p, _i]
+        L.suzerain_lapackext_zgbsv.argtypes = [_p, C.c_char, _i, _i, _i, _i,
+                                               _p, _i, _p, _p, _i]
+        L.suzerain_lapackext_zcgbsvx.argtypes = [_p, _p, _i, C.c_char, _i, _i,
+                                                 _i, _p, _p, _p, _p, _p, _p,
+                                                 _p, _p, _p, _p, _p]
+        L.suzerain_blas_zgbmv.argtypes = [C.c_char, _i, _i, _i, _i, _Z, _p,
+                                          _i, _p, _i, _Z, _p, _i]
+        L.oracle_ref_single_thread()
+        _ref = L
+    return _ref
+
+
+def _ptr(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+# --------------------------------------------------------------------------
+# Pythonic helpers over the restatement
+# --------------------------------------------------------------------------
+def bsmbsm(S: int, n: int, kl: int, ku: int) -> dict:
+    """Geometry of suzerain_bsmbsm_construct (suzerain/bsmbsm.h:130-149)."""
+    KL = S * (kl + 1) - 1
+    KU = S * (ku + 1) - 1
+    return dict(S=S, n=n, kl=kl, ku=ku, ld=kl + 1 + ku, N=S * n, KL=KL, KU=KU,
+                LD=KL + 1 + KU)
+
+
+def q(S, n, i):
+    return lib().orc_q(S, n, i)
+
+
+def qinv(S, n, i):
+    return lib().orc_qinv(S, n, i)
+
+
+def zaPxpby(trans, S, n, alpha, x, incx, beta, y, incy) -> int:
+    return lib().orc_zaPxpby(trans.encode(), S, n, _z(alpha), _ptr(x), incx,
+                             _z(beta), _ptr(y), incy)
+
+
+def zgbtrf(ab: np.ndarray, n, kl, ku, ldab, builtin=True):
+    """In-place band LU; returns (info, ipiv 1-based)."""
+    ipiv = np.zeros(n, dtype=np.int32)
+    f = lib().orc_builtin_zgbtrf if builtin else lib().orc_zgbtrf
+    info = f(n, kl, ku, _ptr(ab), ldab, _ptr(ipiv))
+    return info, ipiv
+
+
+def cgbtrf(ab: np.ndarray, n, kl, ku, ldab, builtin=True):
+    ipiv = np.zeros(n, dtype=np.int32)
+    f = lib().orc_builtin_cgbtrf if builtin else lib().orc_cgbtrf
+    info = f(n, kl, ku, _ptr(ab), ldab, _ptr(ipiv))
+    return info, ipiv
+
+
+def zgbtrs(trans, ab, n, kl, ku, ldab, ipiv, b, builtin=True) -> int:
+    nrhs = 1 if b.ndim == 1 else b.shape[1]
+    f = lib().orc_builtin_zgbtrs if builtin else lib().orc_zgbtrs
+    bb = np.asfortranarray(b)
+    info = f(trans.encode(), n, kl, ku, nrhs, _ptr(ab), ldab, _ptr(ipiv),
+             _ptr(bb), n)
+    b[...] = bb
+    return info
+
+
+def cgbtrs(trans, ab, n, kl, ku, ldab, ipiv, b, builtin=True) -> int:
+    nrhs = 1 if b.ndim == 1 else b.shape[1]
+    f = lib().orc_builtin_cgbtrs if builtin else lib().orc_cgbtrs
+    bb = np.asfortranarray(b)
+    info = f(trans.encode(), n, kl, ku, nrhs, _ptr(ab), ldab, _ptr(ipiv),
+             _ptr(bb), n)
+    b[...] = bb
+    return info
+
+
+def zgbmv(trans, m, n, kl, ku, alpha, a, lda, x, beta, y) -> int:
+    return lib().orc_zgbmv(trans.encode(), m, n, kl, ku, _z(alpha), _ptr(a),
+                           lda, _ptr(x), 1, _z(beta), _ptr(y), 1)
+
+
+def zcgbsvx(ab, n, kl, ku, b, trans="N", aiter=5, siter=25, diter=5,
+            tolsc=1.0):
+    """Restated suzerain_lapackext_zcgbsvx with fact='N'.  Returns dict."""
+    ldafb = 2 * kl + ku + 1
+    fact = C.create_string_buffer(b"N", 1)
+    apprx = C.c_int(0)
+    afrob = C.c_double(-1)
+    afb = np.zeros(ldafb * n, dtype=np.complex128)
+    ipiv = np.zeros(n, dtype=np.int32)
+    x = np.zeros(n, dtype=np.complex128)
+    r = np.zeros(n, dtype=np.complex128)
+    si, di = C.c_int(siter), C.c_int(diter)
+    ts, res = C.c_double(tolsc), C.c_double(0)
+    bb = np.ascontiguousarray(b, dtype=np.complex128)
+    info = lib().orc_zcgbsvx(C.addressof(fact), C.addressof(apprx), aiter,
+                             trans.encode(), n, kl, ku, _ptr(ab),
+                             C.addressof(afrob), _ptr(afb), _ptr(ipiv),
+                             _ptr(bb), _ptr(x), C.addressof(si),
+                             C.addressof(di), C.addressof(ts), _ptr(r),
+                             C.addressof(res))
+    return dict(info=info, fact=fact.raw.decode(), x=x, r=r, siter=si.value,
+                diter=di.value, tolsc=ts.value, res=res.value,
+                afrob=afrob.value)
+
+
+def assemble_packed(S, n, kl, ku, M, D1, D2, ld, cM, cD1, cD2, dirichlet,
+                    layout="packc"):
+    """Packed P A P^T (complex128, column-major band) of one synthetic system.
+
+    layout 'packc': LD rows; 'packf': LD + KL rows with A at row offset KL.
+    """
+    g = bsmbsm(S, n, kl, ku)
+    rows = g["LD"] if layout == "packc" else g["LD"] + g["KL"]
+    off = 0 if layout == "packc" else g["KL"]
+    papt = np.full(rows * g["N"], np.nan, dtype=np.complex128)
+    dm = np.ascontiguousarray(dirichlet, dtype=np.int32)
+    lib().orc_assemble_packed(S, n, kl, ku, _ptr(M), _ptr(D1), _ptr(D2), ld,
+                              _ptr(np.ascontiguousarray(cM, np.complex128)),
+                              _ptr(np.ascontiguousarray(cD1, np.complex128)),
+                              _ptr(np.ascontiguousarray(cD2, np.complex128)),
+                              _ptr(dm), _ptr(papt), rows, off)
+    return papt
+
+
+def block_coefs(case, phi, kx, kz):
+    """(cM, cD1, cD2), each (S, S) complex128, of one wavenumber pair."""
+    S = case.S
+    out = np.zeros((3, S, S), dtype=np.complex128)
+    lib().orc_block_coefs(S, _ptr(case.a), _ptr(case.b), _ptr(case.c),
+                          _ptr(case.g), float(phi), float(kx), float(kz),
+                          _ptr(out[0]), _ptr(out[1]), _ptr(out[2]))
+    return out[0], out[1], out[2]
+
+
+def dirichlet_flags(case) -> np.ndarray:
+    return np.array([(case.dirichlet_mask >> e) & 1 for e in range(case.S)],
+                    dtype=np.int32)
+
+
+def batch_solve(case, kx, kz, u, phi_exp=0.0, phi_imp=1e-3, trans="N",
+                mixed=False, aiter=5, siter=25, diter=5, tolsc=1.0,
+                nthreads=1, openblas=False):
+    """One synthetic substep for every system on host threads.
+
+    case: a suzerain_gb300.synth.SynthCase (bands + coefficients).  u: (nsys,
+    N) complex128 natural-order input; with phi_exp != 0 the right-hand side
+    is the explicit operator applied to u (wall rows zeroed), else u itself.
+    Returns dict with x (natural order), info, wall seconds and, for the mixed
+    path, per-system siter/diter/res/tolsc/fact and latencies.
+    """
+    L = lib()
+    if openblas:
+        path = openblas_path()
+        if path is None or L.orc_use_openblas(path.encode()) != 0:
+            raise RuntimeError("SciPy OpenBLAS not loadable for the oracle")
+    else:
+        L.orc_use_openblas(None)
+    u = np.ascontiguousarray(u, dtype=np.complex128)
+    nsys, N = u.shape
+    kx = np.ascontiguousarray(kx, dtype=np.float64)
+    kz = np.ascontiguousarray(kz, dtype=np.float64)
+    x = np.zeros_like(u)
+    info = np.zeros(nsys, dtype=np.int32)
+    so = np.zeros(nsys, dtype=np.int32)
+    do = np.zeros(nsys, dtype=np.int32)
+    ro = np.zeros(nsys)
+    to = np.zeros(nsys)
+    fo = np.zeros(nsys, dtype=np.uint8)
+    lat = np.zeros(nsys)
+    dm = dirichlet_flags(case)
+    wall = L.orc_batch_solve(nsys, case.S, case.n, case.kl, case.ku,
+                             trans.encode(), _ptr(case.M), _ptr(case.D1),
+                             _ptr(case.D2), case.ld, _ptr(case.a),
+                             _ptr(case.b), _ptr(case.c), _ptr(case.g),
+                             _ptr(dm), _ptr(kx), _ptr(kz), float(phi_exp),
+                             float(phi_imp), _ptr(u), _ptr(x), _ptr(info),
+                             int(mixed), aiter, siter, diter, float(tolsc),
+                             _ptr(so), _ptr(do), _ptr(ro), _ptr(to), _ptr(fo),
+                             _ptr(lat), int(nthreads))
+    if openblas:
+        L.orc_use_openblas(None)
+    return dict(x=x, info=info, wall=wall, siter=so, diter=do, res=ro,
+                tolsc=to, fact=fo.tobytes().decode(errors="replace"),
+                latency=lat)
+
+
+def assemble_case(case, phi, kx, kz, layout="packc"):
+    """Packed P A P^T of one system of a synthetic case."""
+    cM, cD1, cD2 = block_coefs(case, phi, kx, kz)
+    return assemble_packed(case.S, case.n, case.kl, case.ku, case.M, case.D1,
+                           case.D2, case.ld, cM, cD1, cD2,
+                           dirichlet_flags(case), layout=layout)
+
+
+# --------------------------------------------------------------------------
+# Dense helpers for checks (small sizes only)
+# --------------------------------------------------------------------------
+def band_to_dense(ab, n, kl, ku, ldab, off=0):
+    """Dense A from column-major band storage with A(i,j) at
+    ab[off + ku + i - j + j*ldab]."""
+    A = np.zeros((n, n), dtype=ab.dtype)
+    for j in range(n):
+        for i in range(max(0, j - ku), min(n, j + kl + 1)):
+            A[i, j] = ab[off + ku + i - j + j * ldab]
+    return A
+
+
+def rel_resid(A_apply, x, b):
+    """Normwise backward error ||b-Ax||inf / (||A||inf ||x||inf + ||b||inf)
+    where A_apply = (callable y=A@x, ||A||inf)."""
+    apply, anorm = A_apply
+    r = b - apply(x)
+    return np.max(np.abs(r)) / (anorm * np.max(np.abs(x)) + np.max(np.abs(b)))

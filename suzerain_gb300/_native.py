@@ -1,0 +1,176 @@
+"""ctypes binding of libsuzerain_gb300.so (the C-ABI in include/suzerain_gb300.h).
+
+The library is built in-tree by suzerain_gb300.build.  Loading fails loudly
+when it is missing: there is no CPU implementation behind this package.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import build as _build
+
+_i, _d, _p, _ll, _sz = C.c_int, C.c_double, C.c_void_p, C.c_longlong, C.c_size_t
+_u64 = C.c_uint64
+
+
+class ZC(C.Structure):
+    """double _Complex / std::complex<double> by value."""
+    _fields_ = [("re", C.c_double), ("im", C.c_double)]
+
+
+class CC(C.Structure):
+    """float _Complex / std::complex<float> by value."""
+    _fields_ = [("re", C.c_float), ("im", C.c_float)]
+
+
+class Bsmbsm(C.Structure):
+    _fields_ = [(k, C.c_int) for k in ("S", "n", "kl", "ku", "ld", "N", "KL",
+                                       "KU", "LD")]
+
+
+class Case(C.Structure):
+    _fields_ = [("S", _i), ("n", _i), ("kl", _i), ("ku", _i), ("ld", _i),
+                ("M", _p), ("D1", _p), ("D2", _p), ("a", _p), ("b", _p),
+                ("c", _p), ("g", _p), ("dirichlet_mask", C.c_uint),
+                ("pad_", _i)]
+
+
+class RefineSpec(C.Structure):
+    _fields_ = [("aiter", _i), ("siter", _i), ("diter", _i), ("tolsc", _d)]
+
+
+class RefineReport(C.Structure):
+    _fields_ = [("info", _p), ("siter", _p), ("diter", _p), ("res", _p),
+                ("tolsc", _p), ("fact", _p)]
+
+
+class BsplineopWorkspace(C.Structure):
+    _fields_ = [("method", _i), ("k", _i), ("n", _i), ("nderiv", _i),
+                ("kl", C.POINTER(_i)), ("ku", C.POINTER(_i)), ("max_kl", _i),
+                ("max_ku", _i), ("ld", _i),
+                ("D_T", C.POINTER(C.POINTER(_d)))]
+
+
+_SIGS = {
+    # drop-ins
+    "suzerain_bsmbsm_construct": (Bsmbsm, [_i, _i, _i, _i]),
+    "suzerain_bsmbsm_q": (_i, [_i, _i, _i]),
+    "suzerain_bsmbsm_qinv": (_i, [_i, _i, _i]),
+    "suzerain_bsmbsm_saPxpby": (_i, [C.c_char, _i, _i, C.c_float, _p, _i,
+                                     C.c_float, _p, _i]),
+    "suzerain_bsmbsm_daPxpby": (_i, [C.c_char, _i, _i, _d, _p, _i, _d, _p,
+                                     _i]),
+    "suzerain_bsmbsm_caPxpby": (_i, [C.c_char, _i, _i, CC, _p, _i, CC, _p,
+                                     _i]),
+    "suzerain_bsmbsm_zaPxpby": (_i, [C.c_char, _i, _i, ZC, _p, _i, ZC, _p,
+                                     _i]),
+    "suzerain_bsmbsm_dpack": (_i, [_i] * 6 + [_d, _p, _i, _i, _i, _p, _i]),
+    "suzerain_bsmbsm_zpack": (_i, [_i] * 6 + [ZC, _p, _i, _i, _i, _p, _i]),
+    "suzerain_bsmbsm_zdpack": (_i, [_i] * 6 + [ZC, _p, _i, _i, _i, _p, _i]),
+    "suzerain_bsmbsm_zpackc": (_i, [_p, _i, _i, ZC, _p, _p]),
+    "suzerain_bsmbsm_zpackf": (_i, [_p, _i, _i, ZC, _p, _p]),
+    "suzerain_bsmbsm_zdpackc": (_i, [_p, _i, _i, ZC, _p, _p]),
+    "suzerain_bsmbsm_zdpackf": (_i, [_p, _i, _i, ZC, _p, _p]),
+    "suzerain_lapack_zgbtrf": (_i, [_i, _i, _i, _i, _p, _i, _p]),
+    "suzerain_lapack_cgbtrf": (_i, [_i, _i, _i, _i, _p, _i, _p]),
+    "suzerain_lapack_zgbtrs": (_i, [C.c_char, _i, _i, _i, _i, _p, _i, _p,
+                                    _p, _i]),
+    "suzerain_lapack_cgbtrs": (_i, [C.c_char, _i, _i, _i, _i, _p, _i, _p,
+                                    _p, _i]),
+    "suzerain_lapackext_zgbsv": (_i, [_p, C.c_char, _i, _i, _i, _i, _p, _i,
+                                      _p, _p, _i]),
+    "suzerain_lapackext_cgbsv": (_i, [_p, C.c_char, _i, _i, _i, _i, _p, _i,
+                                      _p, _p, _i]),
+    "suzerain_lapackext_zcgbsvx": (_i, [_p, _p, _i, C.c_char, _i, _i, _i, _p,
+                                        _p, _p, _p, _p, _p, _p, _p, _p, _p,
+                                        _p]),
+    "suzerain_blas_zgbmv": (_i, [C.c_char, _i, _i, _i, _i, ZC, _p, _i, _p, _i,
+                                 ZC, _p, _i]),
+    "sgb_bsplineop_alloc_breakpoints": (C.POINTER(BsplineopWorkspace),
+                                        [_i, _i, _p, _i]),
+    "suzerain_bsplineop_free": (None, [C.POINTER(BsplineopWorkspace)]),
+    "suzerain_bsplineop_accumulate_complex": (
+        _i, [_i, _i, ZC, _p, _i, _i, ZC, _p, _i, _i,
+             C.POINTER(BsplineopWorkspace)]),
+    "sgb_bspline_collocation_bands": (_i, [_i, _i, _p, _i, _p, _p, _p, _p,
+                                           _p]),
+    "suzerain_htstretch2": (_d, [_d, _d, _d]),
+    "suzerain_inorder_wavenumber": (_i, [_i, _i]),
+    "suzerain_diffwave_apply": (_i, [_i, _i, ZC, _p, _d, _d, _i, _i, _i, _i,
+                                     _i, _i, _i, _i, _i]),
+    # batched device API
+    "sgb_last_error": (C.c_char_p, []),
+    "sgb_device_ok": (_i, []),
+    "sgb_factor_elems": (_ll, [_i, _i, _i]),
+    "sgb_gbtrf_batched": (_i, [C.c_char, _i, _i, _i, _i, _p, _i, _ll, _p, _p,
+                               _p, _p]),
+    "sgb_gbtrs_batched": (_i, [C.c_char, C.c_char, _i, _i, _i, _i, _p, _p, _p,
+                               _p, _p]),
+    "sgb_factor_to_lapack": (_i, [C.c_char, _i, _i, _i, _i, _p, _p, _p]),
+    "sgb_zcgbsvx_batched": (_i, [_i, _i, _i, _i, C.c_char, _p, _i, _ll, _p,
+                                 _p, C.POINTER(RefineSpec),
+                                 C.POINTER(RefineReport), _p]),
+    "sgb_plan_create": (_p, [C.POINTER(Case), _i, _p, _p, _i]),
+    "sgb_plan_destroy": (_i, [_p]),
+    "sgb_plan_device_bytes": (_sz, [_p]),
+    "sgb_plan_substep": (_i, [_p, C.c_char, _d, _d, _p, _p,
+                              C.POINTER(RefineSpec), _p]),
+    "sgb_plan_substep_host": (_i, [_p, C.c_char, _d, _d, _p, _p,
+                                   C.POINTER(RefineSpec), _p]),
+    "sgb_plan_report": (_i, [_p, _p, _p, _p, _p, _p, _p]),
+    "sgb_plan_backward_error": (_i, [_p, _p, _p]),
+    "sgb_plan_set_timing": (_i, [_p, _i]),
+    "sgb_plan_timings": (_i, [_p, C.c_char_p, _i]),
+    "sgb_launch_count": (_ll, []),
+    "sgb_synth_case": (_i, [_i, _i, _i, _d, _d, _d, _d, _i, _u64, C.c_uint,
+                            _p, _p, _p, _p, _p, _p, _p, _p, _p]),
+    "sgb_synth_wavenumbers": (_i, [_i, _i, _d, _d, _p, _p]),
+    "sgb_synth_rhs": (_i, [_u64, _ll, _i, _p]),
+}
+
+_lib = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = False):
+    """Load the native library; raise if it is absent (no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(_build.LIB):
+        if build_if_missing:
+            _build.build()
+        else:
+            raise ImportError(
+                "suzerain_gb300 native library is not built "
+                f"({_build.LIB}); run suzerain_gb300.build.build()")
+    L = C.CDLL(_build.LIB)
+    for name, (res, args) in _SIGS.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def last_error() -> str:
+    return load().sgb_last_error().decode()
+
+
+def check(rc: int, what: str) -> None:
+    if rc != 0:
+        raise RuntimeError(f"{what} failed ({rc}): {last_error()}")
+
+
+def zc(v) -> ZC:
+    v = complex(v)
+    return ZC(v.real, v.imag)
+
+
+def cc(v) -> CC:
+    v = complex(v)
+    return CC(v.real, v.imag)

@@ -1,0 +1,572 @@
+// C-ABI of the batched device API: error reporting, batched gbtrf/gbtrs,
+// batched zcgbsvx, and the resident-batch plan driving whole substeps.
+#include "suzerain_gb300.h"
+#include "sgb_internal.h"
+#include "sgb_refine.h"
+#include "sgb_timer.h"
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+using namespace sgb;
+
+namespace sgb { std::atomic<long long> g_launches{0}; }
+
+namespace {
+thread_local std::string g_err;
+}
+
+extern "C" long long sgb_launch_count(void) { return g_launches.load(); }
+
+int sgb_set_error(cudaError_t e, const char *what, const char *file, int line)
+{
+    char buf[512];
+    std::snprintf(buf, sizeof buf, "%s: %s (%s:%d)", what, cudaGetErrorString(e), file, line);
+    g_err = buf;
+    return (int) e;
+}
+
+static int fail(const char *msg, int code = -1)
+{
+    g_err = msg;
+    return code;
+}
+
+extern "C" const char *sgb_last_error(void) { return g_err.c_str(); }
+
+extern "C" int sgb_device_ok(void)
+{
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return sgb_set_error(e, "cudaGetDevice", __FILE__, __LINE__);
+    int major = 0, minor = 0;
+    cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
+    cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
+    if (major != 10 || minor != 3) return fail("device is not compute capability 10.3 (GB300)", -2);
+    return 0;
+}
+
+extern "C" long long sgb_factor_elems(int N, int KL, int KU)
+{
+    return FactorGeom{N, KL, KU}.fac_elems();
+}
+
+static bool geom_ok(int N, int KL, int KU)
+{
+    return N >= 1 && KL >= 0 && KU >= 0 && KL + 1 <= 64 && KL + KU + 1 <= 192;
+}
+
+extern "C" int sgb_gbtrf_batched(char prec, int nsys, int N, int KL, int KU, const void *ab,
+                                 int ldab, long long ab_stride, void *fac, int *ipiv,
+                                 int *info, void *stream)
+{
+    if (prec != 'Z' && prec != 'C') return fail("sgb_gbtrf_batched: prec must be 'Z' or 'C'");
+    if (!geom_ok(N, KL, KU) || ldab < KL + KU + 1 || nsys < 0)
+        return fail("sgb_gbtrf_batched: bad geometry");
+    GbtrfArgs a;
+    a.prec = prec; a.g = {N, KL, KU}; a.nsys = nsys;
+    a.src = {reinterpret_cast<const double2 *>(ab), ab_stride, ldab, 0};
+    a.fac = fac; a.fac_stride = a.g.fac_elems(); a.ipiv = ipiv; a.info = info;
+    SGB_CUDA_TRY(launch_gbtrf(a, (cudaStream_t) stream));
+    return 0;
+}
+
+extern "C" int sgb_gbtrs_batched(char prec, char trans, int nsys, int N, int KL, int KU,
+                                 const void *fac, const int *ipiv, const void *b, void *x,
+                                 void *stream)
+{
+    trans = (char) toupper(trans);
+    if (prec != 'Z' && prec != 'C') return fail("sgb_gbtrs_batched: prec must be 'Z' or 'C'");
+    if (trans != 'N' && trans != 'T' && trans != 'C') return fail("sgb_gbtrs_batched: bad trans");
+    if (!geom_ok(N, KL, KU) || nsys < 0) return fail("sgb_gbtrs_batched: bad geometry");
+    GbtrsArgs a;
+    a.prec = prec; a.trans = trans; a.g = {N, KL, KU}; a.nsys = nsys; a.fac = fac;
+    a.fac_stride = a.g.fac_elems(); a.ipiv = ipiv;
+    a.b = reinterpret_cast<const double2 *>(b); a.b_stride = N;
+    a.x = reinterpret_cast<double2 *>(x); a.x_stride = N;
+    SGB_CUDA_TRY(launch_gbtrs(a, (cudaStream_t) stream));
+    return 0;
+}
+
+template <typename T2>
+__global__ void k_factor_to_lapack(int nsys, FactorGeom g, const T2 *__restrict__ fac,
+                                   T2 *__restrict__ ab)
+{
+    const int s = blockIdx.y;
+    const int j = blockIdx.x * blockDim.y + threadIdx.y;
+    if (s >= nsys || j >= g.N) return;
+    const int KL = g.KL, UW = g.UW(), KV = UW - 1, LDAB = 2 * KL + g.KU + 1;
+    const T2 *fu = fac + s * g.fac_elems();
+    const T2 *fl = fu + (long long) g.N * UW;
+    T2 *col = ab + (long long) s * LDAB * g.N;
+    // column j of LAPACK storage: U(j-KV..j, j) rows 0..KV, L(j+1..j+KL, j) rows KV+1..
+    for (int r = threadIdx.x; r < LDAB; r += blockDim.x) {
+        T2 v; v.x = 0; v.y = 0;
+        if (r <= KV) {
+            const int i = j - KV + r;       // U(i, j) = fu[i*UW + (j - i)]
+            if (i >= 0) v = fu[(long long) i * UW + (j - i)];
+        } else {
+            const int i = r - KV;           // L(j+i, j)
+            if (j + i < g.N) v = fl[(long long) j * KL + i - 1];
+        }
+        col[(long long) j * LDAB + r] = v;
+    }
+}
+
+extern "C" int sgb_factor_to_lapack(char prec, int nsys, int N, int KL, int KU,
+                                    const void *fac, void *ab, void *stream)
+{
+    if (!geom_ok(N, KL, KU)) return fail("sgb_factor_to_lapack: bad geometry");
+    if (nsys == 0) return 0;
+    FactorGeom g{N, KL, KU};
+    dim3 blk(32, 4), grd((N + 3) / 4, nsys);
+    if (prec == 'Z')
+        k_factor_to_lapack<double2><<<grd, blk, 0, (cudaStream_t) stream>>>(
+            nsys, g, (const double2 *) fac, (double2 *) ab);
+    else if (prec == 'C')
+        k_factor_to_lapack<float2><<<grd, blk, 0, (cudaStream_t) stream>>>(
+            nsys, g, (const float2 *) fac, (float2 *) ab);
+    else return fail("sgb_factor_to_lapack: prec must be 'Z' or 'C'");
+    SGB_CUDA_TRY(cudaGetLastError());
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Small elementwise kernels
+// ---------------------------------------------------------------------------
+// dir 'N': dst[i] = src[q(i)]  (natural -> permuted); 'T': dst[i] = src[qinv(i)]
+__global__ void k_permute(long long nsys, int S, int n, const double2 *__restrict__ src,
+                          double2 *__restrict__ dst, int to_natural)
+{
+    const long long N = (long long) S * n;
+    const long long t = (long long) blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nsys * N) return;
+    const long long s = t / N;
+    const int i = (int) (t - s * N);
+    const int o = to_natural ? (i % n) * S + i / n : (i % S) * n + i / S;
+    dst[t] = src[s * N + o];
+}
+
+// ---------------------------------------------------------------------------
+// Batched zcgbsvx over packed bands
+// ---------------------------------------------------------------------------
+namespace {
+struct Scratch {
+    void *p = nullptr; size_t bytes = 0;
+    int *hcount = nullptr;
+    std::mutex mu;
+    int ensure(size_t b)
+    {
+        if (!hcount) {
+            cudaError_t e = cudaMallocHost(&hcount, sizeof(int));
+            if (e != cudaSuccess) return sgb_set_error(e, "cudaMallocHost", __FILE__, __LINE__);
+        }
+        if (b <= bytes) return 0;
+        if (p) cudaFree(p);
+        p = nullptr; bytes = 0;
+        cudaError_t e = cudaMalloc(&p, b);
+        if (e != cudaSuccess) return sgb_set_error(e, "cudaMalloc(zcgbsvx workspace)", __FILE__, __LINE__);
+        bytes = b;
+        return 0;
+    }
+};
+Scratch g_zc;
+}  // namespace
+
+__global__ void k_report_copy(int nsys, RefineState st, int *info, int *siter, int *diter,
+                              double *res, double *tolsc, char *fact)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nsys) return;
+    if (info) info[s] = st.info[s];
+    if (siter) siter[s] = st.siter[s];
+    if (diter) diter[s] = st.diter[s];
+    if (res) res[s] = st.res[s];
+    if (tolsc) tolsc[s] = st.tolsc[s];
+    if (fact) fact[s] = st.fact[s];
+}
+
+extern "C" int sgb_zcgbsvx_batched(int nsys, int N, int KL, int KU, char trans, const void *ab,
+                                   int ldab, long long ab_stride, const void *b, void *x,
+                                   const sgb_refine_spec *spec, const sgb_refine_report *report,
+                                   void *stream)
+{
+    trans = (char) toupper(trans);
+    if (trans != 'N' && trans != 'T' && trans != 'C') return fail("sgb_zcgbsvx_batched: bad trans", -4);
+    if (!geom_ok(N, KL, KU) || ldab < KL + KU + 1) return fail("sgb_zcgbsvx_batched: bad geometry", -5);
+    if (!spec || spec->tolsc < 0) return fail("sgb_zcgbsvx_batched: bad tolsc", -16);
+    if (spec->siter < 0 && spec->diter < 0) return fail("sgb_zcgbsvx_batched: siter and diter < 0", -99);
+    if (nsys == 0) return 0;
+    std::lock_guard<std::mutex> lk(g_zc.mu);
+    RefineProblem P;
+    P.nsys = nsys; P.g = {N, KL, KU}; P.trans = trans;
+    P.resid_trans = (trans == 'C') ? 'T' : trans;   // reference gbmv: 'C' == 'T'
+    P.model = false;
+    P.src = {reinterpret_cast<const double2 *>(ab), ab_stride, ldab, 0};
+    P.b = reinterpret_cast<const double2 *>(b); P.b_stride = N;
+    P.x = reinterpret_cast<double2 *>(x); P.x_stride = N;
+    P.aiter = spec->aiter; P.siter = spec->siter; P.diter = spec->diter; P.tolsc = spec->tolsc;
+    P.nslot64 = std::min(nsys, 4096);
+    int rc = g_zc.ensure(refine_workspace_bytes(P));
+    if (rc) return rc;
+    P.host_count = g_zc.hcount;
+    RefineOutputs out;
+    rc = refine_batched(P, g_zc.p, out, (cudaStream_t) stream);
+    if (rc) return sgb_set_error((cudaError_t) rc, "refine_batched", __FILE__, __LINE__);
+    if (report) {
+        k_report_copy<<<(nsys + 127) / 128, 128, 0, (cudaStream_t) stream>>>(
+            nsys, out.state, report->info, report->siter, report->diter, report->res,
+            report->tolsc, report->fact);
+        SGB_CUDA_TRY(cudaGetLastError());
+    }
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Plan: one resident case
+// ---------------------------------------------------------------------------
+struct sgb_plan {
+    sgb_case hc{};            // scalars of the case
+    sgb_case dc{};            // device copy
+    int nsys = 0, N = 0, KL = 0, KU = 0, nslot64 = 1;
+    double *kx = nullptr, *kz = nullptr, *gram = nullptr;
+    double *bands = nullptr, *coefs = nullptr;
+    double2 *b = nullptr, *x = nullptr, *u_stage = nullptr;
+    double phi_imp_last = 0;
+    // complex128 path
+    void *fac64 = nullptr; int *ipiv64 = nullptr, *info64 = nullptr; double2 *y64 = nullptr;
+    // mixed path
+    void *rws = nullptr; size_t rws_bytes = 0;
+    RefineOutputs last{};
+    char last_method = 0;
+    int *hcount = nullptr;
+    size_t dev_bytes = 0;
+    PhaseTimer timer;
+    std::vector<void *> allocs;
+    std::mutex mu;
+
+    int dalloc(void **p, size_t bytes, const char *what)
+    {
+        cudaError_t e = cudaMalloc(p, bytes);
+        if (e != cudaSuccess) return sgb_set_error(e, what, __FILE__, __LINE__);
+        allocs.push_back(*p);
+        dev_bytes += bytes;
+        return 0;
+    }
+    ModelSource ms(double phi) const
+    {
+        ModelSource m;
+        m.cs = dc; m.kx = kx; m.kz = kz; m.case_of = nullptr; m.phi = phi;
+        return m;
+    }
+};
+
+// Gram sums of the bands for the analytic ||A||_F (see k_afrob_model).
+static void band_gram(const sgb_case &c, double *G)
+{
+    const int n = c.n, ld = c.ld;
+    std::memset(G, 0, 18 * sizeof(double));
+    for (int j = 0; j < n; ++j)
+        for (int i = std::max(0, j - c.ku); i <= std::min(n - 1, j + c.kl); ++i) {
+            const size_t k = (size_t) j * ld + c.ku + i - j;
+            const double m = c.M[k], d1 = c.D1[k], d2 = c.D2[k];
+            const double v[6] = {m * m, m * d1, m * d2, d1 * d1, d1 * d2, d2 * d2};
+            for (int t = 0; t < 6; ++t) {
+                G[t] += v[t];
+                if (i == 0) G[6 + t] += v[t];
+                if (i == n - 1) G[12 + t] += v[t];
+            }
+        }
+}
+
+extern "C" sgb_plan *sgb_plan_create(const sgb_case *hcase, int nsys, const double *kx,
+                                     const double *kz, int max_double_slots)
+{
+    if (!hcase || nsys < 1 || !kx || !kz) { fail("sgb_plan_create: bad arguments"); return nullptr; }
+    const sgb_case &c = *hcase;
+    if (c.S < 1 || c.S > 8 || c.n < 2 || c.kl < 0 || c.ku < 0 || c.ld < c.kl + 1 + c.ku) {
+        fail("sgb_plan_create: bad case geometry");
+        return nullptr;
+    }
+    sgb_plan *p = new (std::nothrow) sgb_plan;
+    if (!p) { fail("sgb_plan_create: out of host memory"); return nullptr; }
+    p->hc = c;
+    p->nsys = nsys;
+    p->N = c.S * c.n;
+    p->KL = c.S * (c.kl + 1) - 1;
+    p->KU = c.S * (c.ku + 1) - 1;
+    if (!geom_ok(p->N, p->KL, p->KU)) { fail("sgb_plan_create: bandwidth too large"); delete p; return nullptr; }
+    p->nslot64 = std::max(1, std::min(nsys, max_double_slots > 0 ? max_double_slots : nsys));
+    const size_t nb = (size_t) c.ld * c.n, SS = (size_t) c.S * c.S;
+    int rc = 0;
+    rc |= p->dalloc((void **) &p->bands, 3 * nb * sizeof(double), "cudaMalloc(bands)");
+    rc |= p->dalloc((void **) &p->coefs, 4 * SS * sizeof(double), "cudaMalloc(coefs)");
+    rc |= p->dalloc((void **) &p->kx, nsys * sizeof(double), "cudaMalloc(kx)");
+    rc |= p->dalloc((void **) &p->kz, nsys * sizeof(double), "cudaMalloc(kz)");
+    rc |= p->dalloc((void **) &p->gram, 18 * sizeof(double), "cudaMalloc(gram)");
+    rc |= p->dalloc((void **) &p->b, (size_t) nsys * p->N * sizeof(double2), "cudaMalloc(b)");
+    rc |= p->dalloc((void **) &p->x, (size_t) nsys * p->N * sizeof(double2), "cudaMalloc(x)");
+    if (rc) { sgb_plan_destroy(p); return nullptr; }
+    cudaError_t e = cudaMallocHost(&p->hcount, sizeof(int));
+    if (e != cudaSuccess) { sgb_set_error(e, "cudaMallocHost", __FILE__, __LINE__); sgb_plan_destroy(p); return nullptr; }
+    double G[18];
+    band_gram(c, G);
+    e = cudaMemcpy(p->bands, c.M, nb * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(p->bands + nb, c.D1, nb * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(p->bands + 2 * nb, c.D2, nb * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(p->coefs, c.a, SS * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(p->coefs + SS, c.b, SS * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(p->coefs + 2 * SS, c.c, SS * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(p->coefs + 3 * SS, c.g, SS * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(p->kx, kx, nsys * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(p->kz, kz, nsys * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(p->gram, G, sizeof G, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) { sgb_set_error(e, "cudaMemcpy(plan)", __FILE__, __LINE__); sgb_plan_destroy(p); return nullptr; }
+    p->dc = c;
+    p->dc.M = p->bands; p->dc.D1 = p->bands + nb; p->dc.D2 = p->bands + 2 * nb;
+    p->dc.a = p->coefs; p->dc.b = p->coefs + SS; p->dc.c = p->coefs + 2 * SS; p->dc.g = p->coefs + 3 * SS;
+    return p;
+}
+
+extern "C" int sgb_plan_destroy(sgb_plan *p)
+{
+    if (!p) return 0;
+    for (void *a : p->allocs) cudaFree(a);
+    if (p->hcount) cudaFreeHost(p->hcount);
+    delete p;
+    return 0;
+}
+
+extern "C" size_t sgb_plan_device_bytes(const sgb_plan *p) { return p ? p->dev_bytes : 0; }
+
+static int plan_substep(sgb_plan *p, char method, double phi_exp, double phi_imp,
+                        const void *u_in, void *u_out, const sgb_refine_spec *spec,
+                        cudaStream_t st)
+{
+    const int nsys = p->nsys, N = p->N, S = p->hc.S, n = p->hc.n;
+    const long long tot = (long long) nsys * N;
+    const unsigned EB = (unsigned) ((tot + 255) / 256);
+    PhaseTimer &tm = p->timer;
+    // 1. explicit operator (or plain permutation) into b
+    tm.begin(phi_exp != 0.0 ? "explicit_apply_f64" : "permute_in", st);
+    count_launch(1);
+    if (phi_exp != 0.0) {
+        ApplyArgs aa;
+        aa.nsys = nsys; aa.ms = p->ms(phi_exp);
+        aa.u = reinterpret_cast<const double2 *>(u_in); aa.u_stride = N;
+        aa.y = p->b; aa.y_stride = N;
+        SGB_CUDA_TRY(launch_model_apply(aa, st));
+    } else {
+        k_permute<<<EB, 256, 0, st>>>(nsys, S, n, reinterpret_cast<const double2 *>(u_in), p->b, 0);
+        SGB_CUDA_TRY(cudaGetLastError());
+    }
+    tm.end(st);
+    FactorGeom g{N, p->KL, p->KU};
+    p->phi_imp_last = phi_imp;
+    if (method == 'Z') {
+        if (!p->fac64) {
+            int rc = p->dalloc(&p->fac64, (size_t) nsys * g.fac_elems() * sizeof(double2), "cudaMalloc(fac64)");
+            rc |= p->dalloc((void **) &p->ipiv64, (size_t) nsys * N * sizeof(int), "cudaMalloc(ipiv64)");
+            rc |= p->dalloc((void **) &p->info64, (size_t) nsys * sizeof(int), "cudaMalloc(info64)");
+            rc |= p->dalloc((void **) &p->y64, (size_t) nsys * N * sizeof(double2), "cudaMalloc(y64)");
+            if (rc) return rc;
+        }
+        GbtrfArgs fa;
+        fa.prec = 'Z'; fa.g = g; fa.nsys = nsys; fa.model = true; fa.ms = p->ms(phi_imp);
+        fa.fac = p->fac64; fa.fac_stride = g.fac_elems(); fa.ipiv = p->ipiv64; fa.info = p->info64;
+        fa.rhs = p->b; fa.rhs_stride = N; fa.y = p->y64; fa.y_stride = N;
+        tm.begin("factor_c128", st);
+        count_launch(1);
+        SGB_CUDA_TRY(launch_gbtrf(fa, st));
+        tm.end(st);
+        GbtrsArgs sa;
+        sa.prec = 'Z'; sa.trans = 'N'; sa.g = g; sa.nsys = nsys; sa.fac = p->fac64;
+        sa.fac_stride = g.fac_elems(); sa.ipiv = p->ipiv64; sa.fwd_done = true; sa.yin = p->y64;
+        sa.b_stride = N; sa.x = p->x; sa.x_stride = N;
+        tm.begin("backsolve_c128", st);
+        count_launch(1);
+        SGB_CUDA_TRY(launch_gbtrs(sa, st));
+        tm.end(st);
+    } else if (method == 'M') {
+        RefineProblem P;
+        P.nsys = nsys; P.g = g; P.trans = 'N'; P.resid_trans = 'N'; P.model = true;
+        P.ms = p->ms(phi_imp); P.gram = p->gram; P.b = p->b; P.b_stride = N;
+        P.x = p->x; P.x_stride = N;
+        P.aiter = spec ? spec->aiter : 5; P.siter = spec ? spec->siter : 25;
+        P.diter = spec ? spec->diter : 5; P.tolsc = spec ? spec->tolsc : 1.0;
+        P.nslot64 = p->nslot64; P.host_count = p->hcount;
+        P.timer = &p->timer;
+        const size_t need = refine_workspace_bytes(P);
+        if (need > p->rws_bytes) {
+            int rc = p->dalloc(&p->rws, need, "cudaMalloc(refine workspace)");
+            if (rc) return rc;
+            p->rws_bytes = need;
+        }
+        int rc = refine_batched(P, p->rws, p->last, st);
+        if (rc) return sgb_set_error((cudaError_t) rc, "refine_batched", __FILE__, __LINE__);
+    } else {
+        return fail("sgb_plan_substep: method must be 'Z' or 'M'");
+    }
+    p->last_method = method;
+    tm.begin("permute_out", st);
+    count_launch(1);
+    k_permute<<<EB, 256, 0, st>>>(nsys, S, n, p->x, reinterpret_cast<double2 *>(u_out), 1);
+    SGB_CUDA_TRY(cudaGetLastError());
+    tm.end(st);
+    return 0;
+}
+
+extern "C" int sgb_plan_set_timing(sgb_plan *p, int on)
+{
+    if (!p) return fail("sgb_plan_set_timing: null plan");
+    std::lock_guard<std::mutex> lk(p->mu);
+    p->timer.collect();
+    p->timer.acc.clear();
+    p->timer.on = on != 0;
+    return 0;
+}
+
+extern "C" int sgb_plan_timings(sgb_plan *p, char *buf, int buflen)
+{
+    if (!p || !buf || buflen < 1) return fail("sgb_plan_timings: bad arguments");
+    std::lock_guard<std::mutex> lk(p->mu);
+    p->timer.collect();
+    std::string s;
+    for (auto &kv : p->timer.acc) {
+        char line[256];
+        std::snprintf(line, sizeof line, "%s %.6f %lld\n", kv.first.c_str(), kv.second.first,
+                      kv.second.second);
+        s += line;
+    }
+    std::snprintf(buf, buflen, "%s", s.c_str());
+    return (int) s.size() < buflen ? 0 : fail("sgb_plan_timings: buffer too small", -2);
+}
+
+extern "C" int sgb_plan_substep(sgb_plan *p, char method, double phi_exp, double phi_imp,
+                                const void *u_in, void *u_out, const sgb_refine_spec *spec,
+                                void *stream)
+{
+    if (!p || !u_in || !u_out) return fail("sgb_plan_substep: null argument");
+    std::lock_guard<std::mutex> lk(p->mu);
+    return plan_substep(p, (char) toupper(method), phi_exp, phi_imp, u_in, u_out, spec,
+                        (cudaStream_t) stream);
+}
+
+extern "C" int sgb_plan_substep_host(sgb_plan *p, char method, double phi_exp, double phi_imp,
+                                     const void *u_in_host, void *u_out_host,
+                                     const sgb_refine_spec *spec, void *stream)
+{
+    if (!p || !u_in_host || !u_out_host) return fail("sgb_plan_substep_host: null argument");
+    std::lock_guard<std::mutex> lk(p->mu);
+    cudaStream_t st = (cudaStream_t) stream;
+    const size_t bytes = (size_t) p->nsys * p->N * sizeof(double2);
+    if (!p->u_stage) {
+        int rc = p->dalloc((void **) &p->u_stage, bytes, "cudaMalloc(u_stage)");
+        if (rc) return rc;
+    }
+    SGB_CUDA_TRY(cudaMemcpyAsync(p->u_stage, u_in_host, bytes, cudaMemcpyHostToDevice, st));
+    int rc = plan_substep(p, (char) toupper(method), phi_exp, phi_imp, p->u_stage, p->u_stage,
+                          spec, st);
+    if (rc) return rc;
+    SGB_CUDA_TRY(cudaMemcpyAsync(u_out_host, p->u_stage, bytes, cudaMemcpyDeviceToHost, st));
+    SGB_CUDA_TRY(cudaStreamSynchronize(st));
+    return 0;
+}
+
+extern "C" int sgb_plan_report(const sgb_plan *p, int *info, int *siter, int *diter,
+                               double *res, double *tolsc, char *fact)
+{
+    if (!p) return fail("sgb_plan_report: null plan");
+    const int nsys = p->nsys;
+    SGB_CUDA_TRY(cudaDeviceSynchronize());
+    if (p->last_method == 'Z') {
+        if (info) SGB_CUDA_TRY(cudaMemcpy(info, p->info64, nsys * sizeof(int), cudaMemcpyDeviceToHost));
+        if (siter) std::fill(siter, siter + nsys, 0);
+        if (diter) std::fill(diter, diter + nsys, 0);
+        if (res) std::fill(res, res + nsys, 0.0);
+        if (tolsc) std::fill(tolsc, tolsc + nsys, 0.0);
+        if (fact) std::fill(fact, fact + nsys, 'F');
+        return 0;
+    }
+    if (p->last_method != 'M') return fail("sgb_plan_report: no substep has run");
+    const RefineState &st = p->last.state;
+    if (info) SGB_CUDA_TRY(cudaMemcpy(info, st.info, nsys * sizeof(int), cudaMemcpyDeviceToHost));
+    if (siter) SGB_CUDA_TRY(cudaMemcpy(siter, st.siter, nsys * sizeof(int), cudaMemcpyDeviceToHost));
+    if (diter) SGB_CUDA_TRY(cudaMemcpy(diter, st.diter, nsys * sizeof(int), cudaMemcpyDeviceToHost));
+    if (res) SGB_CUDA_TRY(cudaMemcpy(res, st.res, nsys * sizeof(double), cudaMemcpyDeviceToHost));
+    if (tolsc) SGB_CUDA_TRY(cudaMemcpy(tolsc, st.tolsc, nsys * sizeof(double), cudaMemcpyDeviceToHost));
+    if (fact) SGB_CUDA_TRY(cudaMemcpy(fact, st.fact, nsys, cudaMemcpyDeviceToHost));
+    return 0;
+}
+
+// Normwise backward error per system: one warp per system, lanes over rows.
+__global__ void k_backward_error(int nsys, ModelSource ms, const double2 *__restrict__ b,
+                                 const double2 *__restrict__ x, double *__restrict__ out)
+{
+    const int s = blockIdx.x;
+    if (s >= nsys) return;
+    const sgb_case &cs = ms.cs;
+    const int S = cs.S, n = cs.n, N = S * n;
+    const double2 *xs = x + (long long) s * N, *bs = b + (long long) s * N;
+    double anorm = 0, rmax = 0, xmax = 0, bmax = 0;
+    sgb_coef cf[3][64];
+    for (int e = 0; e < S; ++e)
+        for (int f = 0; f < S; ++f)
+            sgb_block_coefs(&cs, e, f, ms.phi, ms.kx[s], ms.kz[s], &cf[0][e * S + f],
+                            &cf[1][e * S + f], &cf[2][e * S + f]);
+    for (int I = threadIdx.x; I < N; I += 32) {
+        const int p = I / S, e = I % S;
+        double2 ax = make_double2(0, 0);
+        double rowsum = 0;
+        if (((cs.dirichlet_mask >> e) & 1u) && (p == 0 || p == n - 1)) {
+            ax = xs[I];
+            rowsum = 1;
+        } else {
+            for (int q = imax(0, p - cs.kl); q <= imin(n - 1, p + cs.ku); ++q) {
+                const int k = cs.ku + p - q + q * cs.ld;
+                for (int f = 0; f < S; ++f) {
+                    double re, im;
+                    sgb_block_entry(cf[0][e * S + f], cf[1][e * S + f], cf[2][e * S + f],
+                                    cs.M[k], cs.D1[k], cs.D2[k], &re, &im);
+                    const double2 a = make_double2(re, im);
+                    ax = cfma(a, xs[q * S + f], ax);
+                    rowsum += fabs(re) + fabs(im);
+                }
+            }
+        }
+        const double2 r = csub(bs[I], ax);
+        rmax = fmax(rmax, fmax(fabs(r.x), fabs(r.y)));
+        anorm = fmax(anorm, rowsum);
+        xmax = fmax(xmax, fmax(fabs(xs[I].x), fabs(xs[I].y)));
+        bmax = fmax(bmax, fmax(fabs(bs[I].x), fabs(bs[I].y)));
+    }
+    for (int off = 16; off; off >>= 1) {
+        rmax = fmax(rmax, __shfl_xor_sync(0xffffffffu, rmax, off));
+        anorm = fmax(anorm, __shfl_xor_sync(0xffffffffu, anorm, off));
+        xmax = fmax(xmax, __shfl_xor_sync(0xffffffffu, xmax, off));
+        bmax = fmax(bmax, __shfl_xor_sync(0xffffffffu, bmax, off));
+    }
+    if (threadIdx.x == 0) out[s] = rmax / (anorm * xmax + bmax);
+}
+
+extern "C" int sgb_plan_backward_error(sgb_plan *p, double *berr_host, void *stream)
+{
+    if (!p || !berr_host) return fail("sgb_plan_backward_error: null argument");
+    if (p->hc.S * p->hc.S > 64) return fail("sgb_plan_backward_error: S too large");
+    std::lock_guard<std::mutex> lk(p->mu);
+    cudaStream_t st = (cudaStream_t) stream;
+    double *d = nullptr;
+    SGB_CUDA_TRY(cudaMallocAsync((void **) &d, p->nsys * sizeof(double), st));
+    k_backward_error<<<p->nsys, 32, 0, st>>>(p->nsys, p->ms(p->phi_imp_last), p->b, p->x, d);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(berr_host, d, p->nsys * sizeof(double), cudaMemcpyDeviceToHost, st);
+    cudaFreeAsync(d, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return sgb_set_error(e, "backward error", __FILE__, __LINE__);
+    return 0;
+}

@@ -1,0 +1,98 @@
+// Shared device/host helpers for the GB300 banded-solve kernels.
+//
+// Complex arithmetic is written out on float2/double2 so every operation is
+// explicit (the kernels choose where FMAs go).  Complex reciprocal follows
+// R. L. Smith, "Algorithm 116: Complex division", CACM 5(8), 1962.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define SGB_HD __host__ __device__ __forceinline__
+
+template <typename R> struct cplx;
+template <> struct cplx<float>  { using t = float2; };
+template <> struct cplx<double> { using t = double2; };
+template <typename R> using cplx_t = typename cplx<R>::t;
+
+template <typename R> SGB_HD cplx_t<R> mk(R re, R im) { cplx_t<R> z; z.x = re; z.y = im; return z; }
+SGB_HD float2  cadd(float2 a, float2 b)   { return make_float2(a.x + b.x, a.y + b.y); }
+SGB_HD double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+SGB_HD float2  csub(float2 a, float2 b)   { return make_float2(a.x - b.x, a.y - b.y); }
+SGB_HD double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+
+// a * b
+SGB_HD float2 cmul(float2 a, float2 b)
+{ return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x)); }
+SGB_HD double2 cmul(double2 a, double2 b)
+{ return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x)); }
+
+// c - a * b   (the rank-1 / axpy update of every kernel)
+SGB_HD float2 cfnma(float2 a, float2 b, float2 c)
+{
+    return make_float2(fmaf(a.y, b.y, fmaf(-a.x, b.x, c.x)),
+                       fmaf(-a.y, b.x, fmaf(-a.x, b.y, c.y)));
+}
+SGB_HD double2 cfnma(double2 a, double2 b, double2 c)
+{
+    return make_double2(fma(a.y, b.y, fma(-a.x, b.x, c.x)),
+                        fma(-a.y, b.x, fma(-a.x, b.y, c.y)));
+}
+// c + a * b
+SGB_HD float2 cfma(float2 a, float2 b, float2 c)
+{
+    return make_float2(fmaf(-a.y, b.y, fmaf(a.x, b.x, c.x)),
+                       fmaf(a.y, b.x, fmaf(a.x, b.y, c.y)));
+}
+SGB_HD double2 cfma(double2 a, double2 b, double2 c)
+{
+    return make_double2(fma(-a.y, b.y, fma(a.x, b.x, c.x)),
+                        fma(a.y, b.x, fma(a.x, b.y, c.y)));
+}
+SGB_HD float2  cconj(float2 a)  { return make_float2(a.x, -a.y); }
+SGB_HD double2 cconj(double2 a) { return make_double2(a.x, -a.y); }
+
+// 1 / z by Smith's method (range-safe for |re| >> |im| and vice versa).
+template <typename R> SGB_HD cplx_t<R> crcp(cplx_t<R> z)
+{
+    const R a = z.x, b = z.y;
+    if ((a < 0 ? -a : a) >= (b < 0 ? -b : b)) {
+        const R r = b / a, d = a + b * r;
+        return mk<R>(R(1) / d, -r / d);
+    } else {
+        const R r = a / b, d = a * r + b;
+        return mk<R>(r / d, R(-1) / d);
+    }
+}
+
+// LAPACK's IZAMAX metric |re| + |im|.
+template <typename R> SGB_HD R cabs1(cplx_t<R> z)
+{ return (z.x < 0 ? -z.x : z.x) + (z.y < 0 ? -z.y : z.y); }
+template <typename R> SGB_HD bool cnz(cplx_t<R> z) { return z.x != R(0) || z.y != R(0); }
+
+SGB_HD float2  demote(double2 z) { return make_float2((float) z.x, (float) z.y); }
+SGB_HD double2 promote(float2 z) { return make_double2((double) z.x, (double) z.y); }
+template <typename R> SGB_HD cplx_t<R> from_z(double2 z);
+template <> SGB_HD float2  from_z<float>(double2 z)  { return demote(z); }
+template <> SGB_HD double2 from_z<double>(double2 z) { return z; }
+template <typename R> SGB_HD double2 to_z(cplx_t<R> z);
+template <> SGB_HD double2 to_z<float>(float2 z)   { return promote(z); }
+template <> SGB_HD double2 to_z<double>(double2 z) { return z; }
+
+SGB_HD int imin(int a, int b) { return a < b ? a : b; }
+SGB_HD int imax(int a, int b) { return a > b ? a : b; }
+
+// Status words written per system instead of traps or asserts.
+enum sgb_status : int {
+    SGB_OK            = 0,
+    SGB_ACTIVE        = 1,   // still refining
+    SGB_BAD_GEOMETRY  = -900,
+};
+
+#define SGB_CUDA_TRY(call)                                                   \
+    do {                                                                     \
+        cudaError_t e__ = (call);                                            \
+        if (e__ != cudaSuccess) return sgb_set_error(e__, #call, __FILE__, __LINE__); \
+    } while (0)
+
+int sgb_set_error(cudaError_t e, const char *what, const char *file, int line);

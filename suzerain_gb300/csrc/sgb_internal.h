@@ -1,0 +1,89 @@
+// Internal launch interfaces shared by the .cu translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include "gbtrf.cuh"
+
+namespace sgb {
+
+struct GbtrfArgs {
+    char prec = 'Z';             // 'Z' complex128 factor, 'C' complex64
+    FactorGeom g{};
+    int nsys = 0;
+    bool model = false;
+    PackedSource src{};
+    ModelSource ms{};
+    void *fac = nullptr;         // row-panel factor, complex of prec
+    long long fac_stride = 0;    // complex elements between systems
+    int *ipiv = nullptr;         // nsys x N
+    int *info = nullptr;         // nsys
+    const double2 *rhs = nullptr;    // optional permuted RHS (fuses forward elimination)
+    long long rhs_stride = 0;
+    void *y = nullptr;           // forward-eliminated RHS (complex of prec)
+    long long y_stride = 0;
+    const int *sys_list = nullptr;   // optional subset of systems
+    int nlist = 0;                   // grid size when sys_list is set
+    const int *d_count = nullptr;    // optional device count bounding the list
+    bool slot_mode = false;          // factor/ipiv/info indexed by list position
+};
+cudaError_t launch_gbtrf(const GbtrfArgs &a, cudaStream_t st);
+size_t gbtrf_smem_bytes(int prec_bytes, const FactorGeom &g, int S);
+
+// Triangular solves with the row-panel factor.
+struct GbtrsArgs {
+    char prec = 'Z';
+    char trans = 'N';
+    FactorGeom g{};
+    int nsys = 0;
+    const void *fac = nullptr;
+    long long fac_stride = 0;
+    const int *ipiv = nullptr;
+    bool fwd_done = false;       // input already forward-eliminated (trans N only)
+    const double2 *b = nullptr;  // FP64 input when !yin
+    const void *yin = nullptr;   // input in factor precision (fwd_done)
+    long long b_stride = 0;
+    double2 *x = nullptr;        // FP64 output
+    long long x_stride = 0;
+    bool accumulate = false;     // x += solution instead of x = solution
+    const int *sys_list = nullptr;
+    int nlist = 0;
+    const int *d_count = nullptr;
+    bool slot_mode = false;      // factor/ipiv indexed by list position
+    const int *status = nullptr; // optional: skip systems whose status != status_want
+    int status_want = 0;
+    // optional natural-order scatter of the output: x[q(i)] instead of x[i]
+    int unpermute_S = 0, unpermute_n = 0;
+};
+cudaError_t launch_gbtrs(const GbtrsArgs &a, cudaStream_t st);
+
+// Packed band residual r = b - op(A) x (FP64), with per-system norms.
+struct ResidualArgs {
+    char trans = 'N';
+    int nsys = 0, N = 0, KL = 0, KU = 0;
+    bool model = false;
+    PackedSource src{};          // packed LD x N band (off = 0)
+    ModelSource ms{};
+    const double2 *b = nullptr; long long b_stride = 0;
+    const double2 *x = nullptr; long long x_stride = 0;
+    double2 *r = nullptr; long long r_stride = 0;
+    double *rnorm2 = nullptr;    // ||r||_2 per system (may be null)
+    double *xnorm2 = nullptr;    // ||x||_2 per system (may be null)
+    const int *sys_list = nullptr;
+    int nlist = 0;
+    const int *d_count = nullptr;
+    const int *status = nullptr;
+    int status_want = 0;
+};
+cudaError_t launch_residual(const ResidualArgs &a, cudaStream_t st);
+
+// Explicit operator apply of the synthetic model: y = P (M + phi L) u with
+// Dirichlet rows zeroed; u natural order, y permuted order.
+struct ApplyArgs {
+    int nsys = 0;
+    ModelSource ms{};
+    const double2 *u = nullptr; long long u_stride = 0;
+    double2 *y = nullptr; long long y_stride = 0;
+    double beta = 0;             // y = A u + beta * y_prev (permuted) when nonzero
+};
+cudaError_t launch_model_apply(const ApplyArgs &a, cudaStream_t st);
+
+}  // namespace sgb

@@ -1,0 +1,51 @@
+// Batched mixed-precision solve driver (zcgbsvx semantics), internal API.
+#pragma once
+#include "sgb_internal.h"
+
+namespace sgb {
+struct PhaseTimer;
+
+// Per-system refinement state (device arrays of length nsys).
+struct RefineState {
+    double *res = nullptr, *lastres = nullptr, *tolconst = nullptr, *tol = nullptr,
+           *tolsc = nullptr;
+    int *status = nullptr, *siter = nullptr, *diter = nullptr, *info = nullptr;
+    char *fact = nullptr;
+    bool use_eps = false;
+};
+
+struct RefineProblem {
+    int nsys = 0;
+    FactorGeom g{};
+    char trans = 'N';            // solve op(A) x = b
+    char resid_trans = 'N';      // op used by the residual (reference gbmv maps 'C' to 'T')
+    bool model = false;
+    PackedSource src{};          // packed LD x N complex128 band (packc layout)
+    ModelSource ms{};            // synthetic operator
+    const double *gram = nullptr;// per-case band Gram sums (model ||A||_F)
+    const double2 *b = nullptr; long long b_stride = 0;   // permuted RHS
+    double2 *x = nullptr; long long x_stride = 0;         // permuted solution
+    int aiter = 5, siter = 25, diter = 5;
+    double tolsc = 1.0;
+    double afrob_in = -1;        // ||A||_F supplied by the caller when >= 0
+    int nslot64 = 1;             // complex128 factor slots for the fallback
+    int *host_count = nullptr;   // pinned host int for list counts
+    struct PhaseTimer *timer = nullptr;   // optional per-phase event timing
+};
+
+struct RefineOutputs {
+    RefineState state;
+    double *rnorm = nullptr, *xnorm = nullptr;
+    double2 *r = nullptr;
+    int *info32 = nullptr;
+    double *afrob = nullptr;
+    void *fac32 = nullptr, *fac64 = nullptr;     // row-panel factors (slot 0 first)
+    int *ipiv32 = nullptr, *ipiv64 = nullptr;
+    int single_iters = 0, double_iters = 0, n_double = 0;
+};
+
+size_t refine_workspace_bytes(const RefineProblem &P);
+int refine_batched(const RefineProblem &P, void *workspace, RefineOutputs &out,
+                   cudaStream_t st);
+
+}  // namespace sgb

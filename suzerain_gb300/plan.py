@@ -1,0 +1,121 @@
+"""Resident batched substep driver (Python face of sgb_plan_*).
+
+A Plan holds one case's bands and coefficients, the wavenumber pairs of every
+system, and the device workspace; each substep() runs the explicit operator,
+the implicit band solve (complex128 LU, or complex64 LU with FP64
+refinement) and the permutations back to natural order, for all systems, in
+the stream it is given.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _native as nat
+from .synth import SynthCase
+
+
+def _ptr(x) -> int:
+    """Device/host address of a torch tensor, numpy array or int."""
+    if isinstance(x, int):
+        return x
+    if hasattr(x, "data_ptr"):
+        return x.data_ptr()
+    return x.ctypes.data
+
+
+class RefineSpec:
+    """zcgbsvx refinement controls (aiter, siter, diter, tolsc)."""
+
+    def __init__(self, aiter=5, siter=25, diter=5, tolsc=1.0):
+        self.aiter, self.siter, self.diter, self.tolsc = aiter, siter, diter, tolsc
+
+    def ctypes(self) -> nat.RefineSpec:
+        return nat.RefineSpec(self.aiter, self.siter, self.diter, self.tolsc)
+
+    @classmethod
+    def from_spec(cls, spec) -> "RefineSpec":
+        return cls(spec.aiter(), spec.siter(), spec.diter(), spec.tolsc())
+
+
+class Plan:
+    def __init__(self, case: SynthCase, kx: np.ndarray, kz: np.ndarray,
+                 max_double_slots: int = 0):
+        self.L = nat.load()
+        self.case = case
+        self.nsys = int(len(kx))
+        self.N = case.N
+        self._kx = np.ascontiguousarray(kx, dtype=np.float64)
+        self._kz = np.ascontiguousarray(kz, dtype=np.float64)
+        self._cs = case.ctypes_case()
+        h = self.L.sgb_plan_create(C.byref(self._cs), self.nsys,
+                                   self._kx.ctypes.data, self._kz.ctypes.data,
+                                   int(max_double_slots))
+        if not h:
+            raise RuntimeError(f"sgb_plan_create failed: {nat.last_error()}")
+        self.handle = h
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.L.sgb_plan_destroy(self.handle)
+            self.handle = None
+
+    __del__ = close
+
+    def device_bytes(self) -> int:
+        return int(self.L.sgb_plan_device_bytes(self.handle))
+
+    def substep(self, method: str, phi_exp: float, phi_imp: float, u_in, u_out,
+                spec: RefineSpec | None = None, stream=0) -> None:
+        sp = (spec or RefineSpec()).ctypes()
+        rc = self.L.sgb_plan_substep(self.handle, method.encode(), phi_exp,
+                                     phi_imp, _ptr(u_in), _ptr(u_out),
+                                     C.byref(sp), _ptr(stream))
+        nat.check(rc, "sgb_plan_substep")
+
+    def substep_host(self, method: str, phi_exp: float, phi_imp: float,
+                     u_in: np.ndarray, u_out: np.ndarray,
+                     spec: RefineSpec | None = None, stream=0) -> None:
+        sp = (spec or RefineSpec()).ctypes()
+        rc = self.L.sgb_plan_substep_host(self.handle, method.encode(),
+                                          phi_exp, phi_imp, _ptr(u_in),
+                                          _ptr(u_out), C.byref(sp),
+                                          _ptr(stream))
+        nat.check(rc, "sgb_plan_substep_host")
+
+    def report(self) -> dict:
+        n = self.nsys
+        info = np.zeros(n, np.int32)
+        siter = np.zeros(n, np.int32)
+        diter = np.zeros(n, np.int32)
+        res = np.zeros(n)
+        tolsc = np.zeros(n)
+        fact = np.zeros(n, np.uint8)
+        rc = self.L.sgb_plan_report(self.handle, info.ctypes.data,
+                                    siter.ctypes.data, diter.ctypes.data,
+                                    res.ctypes.data, tolsc.ctypes.data,
+                                    fact.ctypes.data)
+        nat.check(rc, "sgb_plan_report")
+        return dict(info=info, siter=siter, diter=diter, res=res, tolsc=tolsc,
+                    fact=fact.tobytes().decode())
+
+    def set_timing(self, on: bool) -> None:
+        nat.check(self.L.sgb_plan_set_timing(self.handle, int(on)), "sgb_plan_set_timing")
+
+    def timings(self) -> dict:
+        """{phase: (total_ms, calls)} recorded since set_timing(True)."""
+        buf = C.create_string_buffer(1 << 16)
+        nat.check(self.L.sgb_plan_timings(self.handle, buf, len(buf)), "sgb_plan_timings")
+        out = {}
+        for line in buf.value.decode().splitlines():
+            name, ms, calls = line.split()
+            out[name] = (float(ms), int(calls))
+        return out
+
+    def backward_error(self, stream=0) -> np.ndarray:
+        out = np.zeros(self.nsys)
+        nat.check(self.L.sgb_plan_backward_error(self.handle, out.ctypes.data,
+                                                 _ptr(stream)),
+                  "sgb_plan_backward_error")
+        return out

@@ -1,0 +1,470 @@
+"""GPU parity: the CUDA path through the C-ABI against the oracle.
+
+Bars: integer results (pivots, info) bit-exact; complex128 solutions within
+1e-11 relative of the oracle and normwise backward error <= 1e-13; mixed
+precision results with backward error <= 1e-12 and the reference's
+convergence decisions."""
+import ctypes as C
+import json
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.fail("GPU tests need a CUDA device")
+    return torch
+
+
+@pytest.fixture(scope="module")
+def lib(native, torch_cuda):
+    assert native.sgb_device_ok() == 0, native.sgb_last_error().decode()
+    return native
+
+
+def dev(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def rand_band(rng, n, kl, ku, extra=0, dtype=np.complex128):
+    ld = extra + kl + ku + 1
+    ab = np.zeros(ld * n, dtype=dtype)
+    for j in range(n):
+        for i in range(max(0, j - ku), min(n, j + kl + 1)):
+            ab[extra + ku + i - j + j * ld] = complex(rng.normal(), rng.normal())
+    return ab, ld
+
+
+GEOMS = [(40, 3, 5), (240, 34, 34), (13, 12, 0), (7, 0, 3), (97, 48, 48),
+         (64, 31, 2), (50, 33, 40), (1, 0, 0), (200, 24, 24)]
+
+
+@pytest.mark.parametrize("n,kl,ku", GEOMS)
+def test_gbtrf_batched_fp64_matches_zgbtf2(lib, oracle, torch_cuda, n, kl, ku):
+    torch = torch_cuda
+    rng = np.random.default_rng(100 + n + kl)
+    nsys = 5
+    bands = [rand_band(rng, n, kl, ku)[0] for _ in range(nsys)]
+    ld = kl + ku + 1
+    ab = dev(torch, np.stack(bands))
+    fe = lib.sgb_factor_elems(n, kl, ku)
+    fac = torch.zeros(nsys * fe, dtype=torch.complex128, device="cuda")
+    ipiv = torch.zeros(nsys * n, dtype=torch.int32, device="cuda")
+    info = torch.zeros(nsys, dtype=torch.int32, device="cuda")
+    assert lib.sgb_gbtrf_batched(b"Z", nsys, n, kl, ku, ab.data_ptr(), ld, ld * n,
+                                 fac.data_ptr(), ipiv.data_ptr(), info.data_ptr(), 0) == 0
+    ldab = 2 * kl + ku + 1
+    lap = torch.zeros(nsys * ldab * n, dtype=torch.complex128, device="cuda")
+    assert lib.sgb_factor_to_lapack(b"Z", nsys, n, kl, ku, fac.data_ptr(), lap.data_ptr(), 0) == 0
+    torch.cuda.synchronize()
+    lap = lap.cpu().numpy().reshape(nsys, -1)
+    ipiv = ipiv.cpu().numpy().reshape(nsys, n)
+    for s in range(nsys):
+        full = np.zeros(ldab * n, dtype=np.complex128)
+        for j in range(n):
+            full[kl + j * ldab: kl + j * ldab + ld] = bands[s][j * ld:(j + 1) * ld]
+        oinfo, opiv = oracle.zgbtrf(full, n, kl, ku, ldab)
+        assert info[s].item() == oinfo
+        assert np.array_equal(ipiv[s], opiv)
+        scale = max(1.0, np.abs(full).max())
+        assert np.max(np.abs(lap[s] - full)) <= 1e-12 * scale
+
+
+@pytest.mark.parametrize("n,kl,ku", [(40, 3, 5), (240, 34, 34), (97, 48, 48)])
+@pytest.mark.parametrize("trans", ["N", "T", "C"])
+@pytest.mark.parametrize("prec", ["Z", "C"])
+def test_gbtrs_batched(lib, oracle, torch_cuda, n, kl, ku, trans, prec):
+    torch = torch_cuda
+    rng = np.random.default_rng(7 + n)
+    nsys = 4
+    ld = kl + ku + 1
+    bands = [rand_band(rng, n, kl, ku)[0] for _ in range(nsys)]
+    b = rng.normal(size=(nsys, n)) + 1j * rng.normal(size=(nsys, n))
+    ab = dev(torch, np.stack(bands))
+    fe = lib.sgb_factor_elems(n, kl, ku)
+    fdt = torch.complex128 if prec == "Z" else torch.complex64
+    fac = torch.zeros(nsys * fe, dtype=fdt, device="cuda")
+    ipiv = torch.zeros(nsys * n, dtype=torch.int32, device="cuda")
+    info = torch.zeros(nsys, dtype=torch.int32, device="cuda")
+    assert lib.sgb_gbtrf_batched(prec.encode(), nsys, n, kl, ku, ab.data_ptr(), ld, ld * n,
+                                 fac.data_ptr(), ipiv.data_ptr(), info.data_ptr(), 0) == 0
+    db = dev(torch, b)
+    x = torch.zeros_like(db)
+    assert lib.sgb_gbtrs_batched(prec.encode(), trans.encode(), nsys, n, kl, ku, fac.data_ptr(),
+                                 ipiv.data_ptr(), db.data_ptr(), x.data_ptr(), 0) == 0
+    torch.cuda.synchronize()
+    x = x.cpu().numpy()
+    for s in range(nsys):
+        A = oracle.band_to_dense(bands[s], n, kl, ku, ld)
+        op = A if trans == "N" else (A.T if trans == "T" else A.conj().T)
+        berr = np.max(np.abs(op @ x[s] - b[s])) / (np.abs(op).sum(1).max() * np.abs(x[s]).max() + np.abs(b[s]).max())
+        assert berr <= (1e-14 if prec == "Z" else 1e-5), berr
+
+
+def test_singular_and_nan_systems(lib, oracle, torch_cuda):
+    torch = torch_cuda
+    n, kl, ku = 30, 2, 3
+    ld = kl + ku + 1
+    rng = np.random.default_rng(11)
+    bands = [rand_band(rng, n, kl, ku)[0] for _ in range(3)]
+    j = 17
+    for i in range(max(0, j - ku), min(n, j + kl + 1)):
+        bands[1][ku + i - j + j * ld] = 0          # system 1: zero column 17
+    ab = dev(torch, np.stack(bands))
+    fe = lib.sgb_factor_elems(n, kl, ku)
+    fac = torch.zeros(3 * fe, dtype=torch.complex128, device="cuda")
+    ipiv = torch.zeros(3 * n, dtype=torch.int32, device="cuda")
+    info = torch.zeros(3, dtype=torch.int32, device="cuda")
+    assert lib.sgb_gbtrf_batched(b"Z", 3, n, kl, ku, ab.data_ptr(), ld, ld * n,
+                                 fac.data_ptr(), ipiv.data_ptr(), info.data_ptr(), 0) == 0
+    torch.cuda.synchronize()
+    assert info.cpu().tolist() == [0, j + 1, 0]
+
+
+def _zcgbsvx_batch(lib, torch, bands, b, n, kl, ku, spec, trans="N"):
+    nsys = len(bands)
+    ld = kl + ku + 1
+    ab = dev(torch, np.stack(bands))
+    db = dev(torch, b)
+    x = torch.zeros_like(db)
+    rep = {k: torch.zeros(nsys, dtype=t, device="cuda") for k, t in
+           (("info", torch.int32), ("siter", torch.int32), ("diter", torch.int32),
+            ("res", torch.float64), ("tolsc", torch.float64), ("fact", torch.uint8))}
+    from suzerain_gb300 import _native as nat
+    R = nat.RefineReport(*(rep[k].data_ptr() for k in ("info", "siter", "diter", "res", "tolsc", "fact")))
+    S = nat.RefineSpec(*spec)
+    assert lib.sgb_zcgbsvx_batched(nsys, n, kl, ku, trans.encode(), ab.data_ptr(), ld, ld * n,
+                                   db.data_ptr(), x.data_ptr(), C.byref(S), C.byref(R), 0) == 0, \
+        lib.sgb_last_error().decode()
+    torch.cuda.synchronize()
+    out = {k: v.cpu().numpy() for k, v in rep.items()}
+    out["x"] = x.cpu().numpy()
+    return out
+
+
+@pytest.mark.parametrize("n,kl,ku", [(60, 5, 4), (240, 34, 34)])
+def test_zcgbsvx_batched_matches_oracle(lib, oracle, torch_cuda, n, kl, ku):
+    torch = torch_cuda
+    rng = np.random.default_rng(21)
+    nsys = 6
+    bands = []
+    for s in range(nsys):
+        ab, ld = rand_band(rng, n, kl, ku)
+        # diagonally weighted so complex64 refinement converges
+        for j in range(n):
+            ab[ku + j * ld] += 4 * (kl + ku + 1)
+        bands.append(ab)
+    b = rng.normal(size=(nsys, n)) + 1j * rng.normal(size=(nsys, n))
+    spec = (5, 25, 5, 1.0)
+    g = _zcgbsvx_batch(lib, torch, bands, b, n, kl, ku, spec)
+    for s in range(nsys):
+        o = oracle.zcgbsvx(bands[s], n, kl, ku, b[s], aiter=5, siter=25, diter=5, tolsc=1.0)
+        assert g["info"][s] == o["info"] == 0
+        assert chr(g["fact"][s]) == o["fact"] == "S"
+        assert abs(int(g["siter"][s]) - o["siter"]) <= 1
+        assert g["tolsc"][s] <= 1.0
+        A = oracle.band_to_dense(bands[s], n, kl, ku, kl + ku + 1)
+        xref = np.linalg.solve(A, b[s])
+        assert np.max(np.abs(g["x"][s] - xref)) <= 1e-11 * np.max(np.abs(xref))
+
+
+def test_zcgbsvx_batched_fallback_to_double(lib, oracle, torch_cuda):
+    """An ill-conditioned (Lotkin) system stalls in complex64 and must finish
+    on the complex128 factor, matching the oracle's fact/diter decisions."""
+    torch = torch_cuda
+    n = 10
+    A = np.array([[1.0 if i == 0 else 1.0 / (i + j + 1) for j in range(n)] for i in range(n)]) * (1 + 0.5j)
+    kl = ku = n - 1
+    ld = kl + ku + 1
+    ab = np.zeros(ld * n, dtype=np.complex128)
+    for j in range(n):
+        for i in range(n):
+            ab[ku + i - j + j * ld] = A[i, j]
+    xt = np.ones(n, dtype=np.complex128)
+    b = (A @ xt)[None, :]
+    good = np.zeros(ld * n, dtype=np.complex128)
+    for j in range(n):
+        good[ku + j * ld] = 2.0 + 0.1 * j
+    bg = (np.ones(n) * 3.0 + 0j)[None, :]
+    g = _zcgbsvx_batch(lib, torch, [ab, good], np.vstack([b, bg]), n, kl, ku, (5, 25, 10, 1.0))
+    o = oracle.zcgbsvx(ab, n, kl, ku, b[0], aiter=5, siter=25, diter=10, tolsc=1.0)
+    assert chr(g["fact"][0]) == o["fact"] == "D"
+    assert g["diter"][0] == o["diter"]
+    assert g["tolsc"][0] <= 1.0 and g["info"][0] == 0
+    assert np.linalg.norm(A @ g["x"][0] - b[0]) <= 10 * g["res"][0] + 1e-30
+    assert chr(g["fact"][1]) == "S" and g["info"][1] == 0
+
+
+# ---------------------------------------------------------------------------
+# Synthetic substep through the plan
+# ---------------------------------------------------------------------------
+def config0(complex_coupling=False):
+    from suzerain_gb300 import synth
+    c = synth.CONFIGS[0]
+    cs, kx, kz, u = c.batch(complex_coupling)
+    synth.zero_dirichlet_rows(cs, u)
+    return c, cs, kx, kz, u
+
+
+@pytest.mark.parametrize("complex_coupling", [False, True])
+@pytest.mark.parametrize("explicit", [False, True])
+def test_plan_plain_fp64_matches_oracle(lib, oracle, torch_cuda, complex_coupling, explicit):
+    torch = torch_cuda
+    from suzerain_gb300 import plan as P, synth
+    c, cs, kx, kz, u = config0(complex_coupling)
+    phi_e, phi_i = synth.smr91_phis(c.phi) if explicit else (0.0, c.phi)
+    pl = P.Plan(cs, kx, kz)
+    du = dev(torch, u)
+    out = torch.zeros_like(du)
+    pl.substep("Z", phi_e, phi_i, du, out)
+    torch.cuda.synchronize()
+    x = out.cpu().numpy()
+    rep = pl.report()
+    berr = pl.backward_error()
+    o = oracle.batch_solve(cs, kx, kz, u, phi_exp=phi_e, phi_imp=phi_i, nthreads=8)
+    assert (rep["info"] == o["info"]).all() and (o["info"] == 0).all()
+    rel = np.max(np.abs(x - o["x"]), axis=1) / np.max(np.abs(o["x"]), axis=1)
+    assert rel.max() <= 1e-11, rel.max()
+    assert berr.max() <= 1e-13, berr.max()
+
+
+@pytest.mark.parametrize("complex_coupling", [False, True])
+def test_plan_mixed_matches_oracle(lib, oracle, torch_cuda, complex_coupling):
+    torch = torch_cuda
+    from suzerain_gb300 import plan as P, synth
+    c, cs, kx, kz, u = config0(complex_coupling)
+    phi_e, phi_i = synth.smr91_phis(c.phi)
+    pl = P.Plan(cs, kx, kz)
+    du = dev(torch, u)
+    out = torch.zeros_like(du)
+    spec = P.RefineSpec(aiter=5, siter=25, diter=5, tolsc=145.0)
+    pl.substep("M", phi_e, phi_i, du, out, spec)
+    torch.cuda.synchronize()
+    x = out.cpu().numpy()
+    rep = pl.report()
+    berr = pl.backward_error()
+    o = oracle.batch_solve(cs, kx, kz, u, phi_exp=phi_e, phi_imp=phi_i, nthreads=8)
+    om = oracle.batch_solve(cs, kx, kz, u, phi_exp=phi_e, phi_imp=phi_i, mixed=True,
+                            tolsc=145.0, nthreads=8)
+    assert (rep["info"] == 0).all()
+    assert berr.max() <= 1e-12, berr.max()
+    assert (rep["tolsc"] <= 1.0).all()
+    rel = np.max(np.abs(x - o["x"]), axis=1) / np.max(np.abs(o["x"]), axis=1)
+    assert rel.max() <= 1e-9, rel.max()
+    # the same convergence decisions as the reference algorithm, per system
+    assert set(rep["fact"]) <= {"S", "D"}
+    agree = np.mean(np.abs(rep["siter"] - om["siter"]) <= 1)
+    assert agree >= 0.95, agree
+
+
+def test_plan_result_independent_of_batch(lib, torch_cuda):
+    """A system's result does not depend on which other systems share the batch."""
+    torch = torch_cuda
+    from suzerain_gb300 import plan as P
+    c, cs, kx, kz, u = config0()
+    full = P.Plan(cs, kx, kz)
+    sub_idx = np.array([3, 77, 200, 311])
+    part = P.Plan(cs, kx[sub_idx], kz[sub_idx])
+    for method in ("Z", "M"):
+        a = torch.zeros(u.shape, dtype=torch.complex128, device="cuda")
+        b = torch.zeros((len(sub_idx), u.shape[1]), dtype=torch.complex128, device="cuda")
+        full.substep(method, 0.0, c.phi, dev(torch, u), a, P.RefineSpec(tolsc=145.0))
+        part.substep(method, 0.0, c.phi, dev(torch, u[sub_idx]), b, P.RefineSpec(tolsc=145.0))
+        torch.cuda.synchronize()
+        assert np.array_equal(a.cpu().numpy()[sub_idx], b.cpu().numpy())
+
+
+def test_plan_host_entry_matches_device_entry(lib, torch_cuda):
+    torch = torch_cuda
+    from suzerain_gb300 import plan as P
+    c, cs, kx, kz, u = config0()
+    pl = P.Plan(cs, kx, kz)
+    a = torch.zeros(u.shape, dtype=torch.complex128, device="cuda")
+    pl.substep("M", 0.0, c.phi, dev(torch, u), a, P.RefineSpec(tolsc=145.0))
+    torch.cuda.synchronize()
+    h = np.zeros_like(u)
+    pl.substep_host("M", 0.0, c.phi, u, h, P.RefineSpec(tolsc=145.0))
+    assert np.array_equal(a.cpu().numpy(), h)
+
+
+# ---------------------------------------------------------------------------
+# Drop-in entry points
+# ---------------------------------------------------------------------------
+def test_dropin_kat_solve(lib, oracle):
+    """tests/test_bsmbsm.cpp:801-872 through the GPU drop-ins: zdpackf/zpackf,
+    zaPxpby, zgbsv, unpermute."""
+    from suzerain_gb300 import _native as nat
+    d = json.load(open(os.path.join(GOLD, "bsmbsm_kat.json")))
+    A = lib.suzerain_bsmbsm_construct(d["S"], d["n"], d["kl"], d["ku"])
+    papt = np.full((A.LD + A.KL) * A.N, np.nan, dtype=np.complex128)
+    for ih, row in enumerate(d["blocks"]):
+        for jh, blk in enumerate(row):
+            if blk is None:
+                rc = lib.suzerain_bsmbsm_zpackf(C.byref(A), ih, jh, nat.zc(0), None, papt.ctypes.data)
+            else:
+                b = np.array(d[blk[0]]) * blk[1]
+                rc = lib.suzerain_bsmbsm_zdpackf(C.byref(A), ih, jh, nat.zc(1), b.ctypes.data, papt.ctypes.data)
+            assert rc == 0, lib.sgb_last_error().decode()
+    br = np.array(d["BR"], dtype=np.complex128)
+    pb = np.zeros(A.N, dtype=np.complex128)
+    assert lib.suzerain_bsmbsm_zaPxpby(b"N", A.S, A.n, nat.zc(1), br.ctypes.data, 1, nat.zc(0), pb.ctypes.data, 1) == 0
+    ipiv = np.zeros(A.N, np.int32)
+    fact = C.create_string_buffer(b"N", 1)
+    assert lib.suzerain_lapackext_zgbsv(C.addressof(fact), b"N", A.N, A.KL, A.KU, 1, papt.ctypes.data,
+                                        A.LD + A.KL, ipiv.ctypes.data, pb.ctypes.data, A.N) == 0
+    assert fact.raw == b"F"
+    x = np.zeros(A.N, dtype=np.complex128)
+    assert lib.suzerain_bsmbsm_zaPxpby(b"T", A.S, A.n, nat.zc(1), pb.ctypes.data, 1, nat.zc(0), x.ctypes.data, 1) == 0
+    xr = np.array(d["XR"])
+    tol = np.finfo(float).eps * d["tolerance_eps_multiple"]
+    assert np.allclose(x.real, xr, rtol=tol, atol=tol * np.abs(xr).max())
+
+
+def test_dropin_pack_and_aPxpby_match_oracle(lib, oracle):
+    from suzerain_gb300 import _native as nat
+    rng = np.random.default_rng(5)
+    for (S, n, kl, ku) in [(1, 10, 2, 3), (3, 17, 4, 3), (5, 12, 6, 6)]:
+        g = oracle.bsmbsm(S, n, kl, ku)
+        b = rng.normal(size=g["ld"] * n) + 1j * rng.normal(size=g["ld"] * n)
+        p1 = np.full(g["LD"] * g["N"], np.nan, dtype=np.complex128)
+        p2 = p1.copy()
+        for ih in range(S):
+            for jh in range(S):
+                al = complex(ih + 2, jh - 1)
+                assert lib.suzerain_bsmbsm_zpack(S, n, ih, jh, kl, ku, nat.zc(al), b.ctypes.data, g["ld"],
+                                                 g["KL"], g["KU"], p1.ctypes.data, g["LD"]) == 0
+                oracle.lib().orc_zpack(S, n, ih, jh, kl, ku, oracle._z(al), b.ctypes.data, g["ld"],
+                                       g["KL"], g["KU"], p2.ctypes.data, g["LD"])
+        assert np.array_equal(np.isnan(p1), np.isnan(p2))
+        m = ~np.isnan(p1)
+        assert np.allclose(p1[m], p2[m], rtol=4e-16, atol=0)
+        for trans in "NT":
+            for incx, incy in ((1, 1), (-2, 3), (2, -1)):
+                N = S * n
+                x = rng.normal(size=N * abs(incx)) + 1j * rng.normal(size=N * abs(incx))
+                y = rng.normal(size=N * abs(incy)) + 1j * rng.normal(size=N * abs(incy))
+                y1, y2 = y.copy(), y.copy()
+                assert lib.suzerain_bsmbsm_zaPxpby(trans.encode(), S, n, nat.zc(3 - 1j), x.ctypes.data, incx,
+                                                   nat.zc(0.5j), y1.ctypes.data, incy) == 0
+                oracle.zaPxpby(trans, S, n, 3 - 1j, x, incx, 0.5j, y2, incy)
+                assert np.allclose(y1, y2, rtol=4 * np.finfo(float).eps, atol=1e-14)
+    assert lib.suzerain_bsmbsm_zaPxpby(b"X", 2, 2, nat.zc(1), None, 1, nat.zc(0), None, 1) == 1
+
+
+def test_dropin_zcgbsvx_lotkin(lib, oracle):
+    from suzerain_gb300 import _native as nat
+    for n in (4, 8, 12):
+        A = np.array([[1.0 if i == 0 else 1.0 / (i + j + 1) for j in range(n)] for i in range(n)]) * (1 - 0.25j)
+        kl = ku = n - 1
+        ld = kl + ku + 1
+        ab = np.zeros(ld * n, dtype=np.complex128)
+        for j in range(n):
+            for i in range(n):
+                ab[ku + i - j + j * ld] = A[i, j]
+        b = A @ np.ones(n)
+        o = oracle.zcgbsvx(ab, n, kl, ku, b, aiter=5, siter=25, diter=10, tolsc=1.0)
+        fact = C.create_string_buffer(b"N", 1)
+        apprx, afrob = C.c_int(0), C.c_double(-1)
+        afb = np.zeros((2 * kl + ku + 1) * n, dtype=np.complex128)
+        ipiv = np.zeros(n, np.int32)
+        x = np.zeros(n, dtype=np.complex128)
+        r = np.zeros(n, dtype=np.complex128)
+        si, di, ts, res = C.c_int(25), C.c_int(10), C.c_double(1.0), C.c_double(0)
+        info = lib.suzerain_lapackext_zcgbsvx(C.addressof(fact), C.addressof(apprx), 5, b"N", n, kl, ku,
+                                              ab.ctypes.data, C.addressof(afrob), afb.ctypes.data,
+                                              ipiv.ctypes.data, b.ctypes.data, x.ctypes.data,
+                                              C.addressof(si), C.addressof(di), C.addressof(ts),
+                                              r.ctypes.data, C.addressof(res))
+        assert info == o["info"] == 0
+        assert fact.raw.decode() == o["fact"]
+        assert ts.value <= 1.0
+        assert np.linalg.norm(A @ x - b) <= 10 * res.value + 1e-30
+        assert np.allclose(r, b - A @ x, rtol=0, atol=1e-12 * np.abs(b).max())
+        assert abs(afrob.value - o["afrob"]) <= 1e-12 * o["afrob"]
+
+
+def test_dropin_gbtrf_gbtrs_lapack_layout(lib, oracle):
+    n, kl, ku = 50, 6, 4
+    rng = np.random.default_rng(9)
+    ldab = 2 * kl + ku + 1
+    ab = np.zeros(ldab * n, dtype=np.complex128)
+    for j in range(n):
+        for i in range(max(0, j - ku), min(n, j + kl + 1)):
+            ab[kl + ku + i - j + j * ldab] = complex(rng.normal(), rng.normal())
+    a1, a2 = ab.copy(), ab.copy()
+    p1 = np.zeros(n, np.int32)
+    assert lib.suzerain_lapack_zgbtrf(n, n, kl, ku, a1.ctypes.data, ldab, p1.ctypes.data) == 0
+    info, p2 = oracle.zgbtrf(a2, n, kl, ku, ldab)
+    assert np.array_equal(p1, p2)
+    assert np.max(np.abs(a1 - a2)) <= 1e-12 * np.abs(a2).max()
+    for tr in "NTC":
+        b = rng.normal(size=(n, 2)) + 1j * rng.normal(size=(n, 2))
+        x1 = np.asfortranarray(b.copy())
+        assert lib.suzerain_lapack_zgbtrs(tr.encode(), n, kl, ku, 2, a1.ctypes.data, ldab, p1.ctypes.data,
+                                          x1.ctypes.data, n) == 0
+        x2 = b.copy()
+        oracle.zgbtrs(tr, a2, n, kl, ku, ldab, p2, x2)
+        assert np.allclose(x1, x2, rtol=1e-11, atol=1e-12)
+
+
+def test_dropin_gbmv_and_diffwave(lib, oracle):
+    from suzerain_gb300 import _native as nat
+    rng = np.random.default_rng(13)
+    for tr in "NTC":
+        m, n, kl, ku = 30, 30, 3, 5
+        lda = kl + ku + 2
+        a = rng.normal(size=lda * n) + 1j * rng.normal(size=lda * n)
+        x = rng.normal(size=n) + 1j * rng.normal(size=n)
+        y = rng.normal(size=m) + 1j * rng.normal(size=m)
+        y1, y2 = y.copy(), y.copy()
+        assert lib.suzerain_blas_zgbmv(tr.encode(), m, n, kl, ku, nat.zc(2 - 1j), a.ctypes.data, lda,
+                                       x.ctypes.data, 1, nat.zc(0.5), y1.ctypes.data, 1) == 0
+        oracle.zgbmv(tr, m, n, kl, ku, 2 - 1j, a, lda, x, 0.5, y2)
+        assert np.allclose(y1, y2, rtol=1e-13, atol=1e-13)
+    # diffwave: x <- alpha (i kx)^dx (i kz)^dz x on (Ny, Nx, Nz), dealiased
+    Ny, Nx, Nz, dNx, dNz = 4, 8, 6, 12, 9
+    Lx, Lz = 4.0, 3.0
+    for dx, dz in ((0, 0), (1, 0), (0, 2), (1, 1)):
+        f = rng.normal(size=(dNz, dNx, Ny)) + 1j * rng.normal(size=(dNz, dNx, Ny))
+        g = f.copy()
+        assert lib.suzerain_diffwave_apply(dx, dz, nat.zc(1.5 - 0.5j), g.ctypes.data, Lx, Lz, Ny, Nx, dNx,
+                                           0, dNx, Nz, dNz, 0, dNz) == 0
+        def keep_diff(N, dN, i):
+            return i if i < (N + 1) // 2 else (-dN + i if i >= dN - (N - 1) // 2 else 0)
+        def wabs(N, i):
+            return i if i < N // 2 + 1 else N - i
+        exp = np.zeros_like(f)
+        for nz in range(dNz):
+            for mx in range(dNx):
+                nf = keep_diff(Nz, dNz, nz) if dz else None
+                mf = keep_diff(Nx, dNx, mx) if dx else None
+                nk = nf != 0 if dz else wabs(dNz, nz) <= (Nz - 1) // 2
+                mk = mf != 0 if dx else wabs(dNx, mx) <= (Nx - 1) // 2
+                if nk and mk:
+                    sc = (1.5 - 0.5j) * (1j * 2 * np.pi / Lz * (nf or 0)) ** dz * (1j * 2 * np.pi / Lx * (mf or 0)) ** dx
+                    exp[nz, mx] = f[nz, mx] * sc
+        assert np.allclose(g, exp, rtol=1e-14, atol=1e-13)
+
+
+def test_dropin_bsplineop_accumulate_golden(lib):
+    from suzerain_gb300 import _native as nat
+    d = json.load(open(os.path.join(GOLD, "bsplineop_kat.json")))
+    bp = np.array(d["breakpoints"])
+    w = lib.sgb_bsplineop_alloc_breakpoints(d["k"], len(bp), bp.ctypes.data, 1)
+    try:
+        x = np.array([complex(a, b) for a, b in d["apply_complex_x"]])
+        y = np.zeros_like(x)
+        assert lib.suzerain_bsplineop_accumulate_complex(0, 1, nat.zc(1), x.ctypes.data, 1, len(x),
+                                                         nat.zc(0), y.ctypes.data, 1, len(x), w) == 0
+        good = np.array([complex(a, b) for a, b in d["apply_complex_good"]])
+        assert np.allclose(y, good, rtol=0, atol=1e-14)
+    finally:
+        lib.suzerain_bsplineop_free(w)

@@ -1,0 +1,144 @@
+"""Host-side product code (no GPU): the library loads and exports every
+declared symbol; B-spline collocation operators match the reference's golden
+bands and SciPy; the synthetic generator is deterministic with the expected
+geometry."""
+import ctypes as C
+import json
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLD = os.path.join(ROOT, "tests", "golden")
+
+
+def declared_symbols():
+    names = set()
+    for fn in os.listdir(os.path.join(ROOT, "include")):
+        if not fn.endswith(".h"):
+            continue
+        src = open(os.path.join(ROOT, "include", fn)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        for m in re.finditer(r"\b((?:suzerain|sgb)_[A-Za-z0-9_]+)\s*\(", src):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+def test_library_exports_every_declared_symbol(native):
+    missing = [n for n in declared_symbols() if not hasattr(native, n)]
+    assert not missing, missing
+    assert len(declared_symbols()) > 40
+
+
+def test_construct_q_qinv(native):
+    g = native.suzerain_bsmbsm_construct(5, 192, 6, 6)
+    assert (g.S, g.n, g.N, g.KL, g.KU, g.LD) == (5, 192, 960, 34, 34, 69)
+    d = json.load(open(os.path.join(GOLD, "bsmbsm_kat.json")))
+    for i, v in d["q_S5n9"]:
+        assert native.suzerain_bsmbsm_q(5, 9, i) == v
+    for i, v in d["qinv_S5n9"]:
+        assert native.suzerain_bsmbsm_qinv(5, 9, i) == v
+
+
+def collocation(native, k, bp, nderiv):
+    bp = np.ascontiguousarray(bp, dtype=np.float64)
+    n, kl, ku = C.c_int(), C.c_int(), C.c_int()
+    assert native.sgb_bspline_collocation_bands(k, len(bp), bp.ctypes.data, nderiv,
+                                                C.byref(n), C.byref(kl), C.byref(ku),
+                                                None, None) == 0
+    ld = kl.value + 1 + ku.value
+    bands = np.zeros((nderiv + 1) * ld * n.value)
+    xi = np.zeros(n.value)
+    assert native.sgb_bspline_collocation_bands(k, len(bp), bp.ctypes.data, nderiv,
+                                                C.byref(n), C.byref(kl), C.byref(ku),
+                                                bands.ctypes.data, xi.ctypes.data) == 0
+    return n.value, kl.value, ku.value, bands.reshape(nderiv + 1, n.value, ld), xi
+
+
+def test_collocation_matches_mathematica_golden(native):
+    """k=6 bands of tests/test_bsmbsm.cpp:700-800 (ld 9, kl=ku=4)."""
+    d = json.load(open(os.path.join(GOLD, "bsmbsm_kat.json")))
+    n, kl, ku, bands, _ = collocation(native, d["k"], d["breakpoints"], 2)
+    assert (n, kl, ku) == (10, 4, 4)
+    for m, nm in enumerate(("M", "D1", "D2")):
+        gold = np.array(d[nm]).reshape(n, 9)
+        scale = np.abs(gold).max()
+        assert np.allclose(bands[m], gold, rtol=0, atol=1e-13 * scale), nm
+
+
+def test_bsplineop_workspace_golden_k3(native):
+    """tests/test_bsplineop.cpp:465-540: transposed k=3 mass band."""
+    d = json.load(open(os.path.join(GOLD, "bsplineop_kat.json")))
+    bp = np.array(d["breakpoints"])
+    w = native.sgb_bsplineop_alloc_breakpoints(d["k"], len(bp), bp.ctypes.data, 1)
+    try:
+        ws = w.contents
+        assert ws.n == d["n"] and ws.kl[0] == d["kl"] and ws.ku[0] == d["ku"]
+        band = np.ctypeslib.as_array(ws.D_T[0], shape=(ws.ld * ws.n,))
+        gold = np.array(d["mass_D_T0_band"]).reshape(ws.n, d["ld"])
+        got = band.reshape(ws.n, ws.ld)
+        # compare the in-band entries (row offsets ku+i-j of each column)
+        for j in range(ws.n):
+            for i in range(max(0, j - d["ku"]), min(ws.n, j + d["kl"] + 1)):
+                assert abs(got[j, ws.ku[0] + i - j] - gold[j, d["ku"] + i - j]) <= 1e3 * np.finfo(float).eps
+    finally:
+        native.suzerain_bsplineop_free(w)
+
+
+@pytest.mark.parametrize("Ny,k", [(48, 8), (192, 8), (32, 6), (256, 6)])
+def test_collocation_matches_scipy(native, Ny, k):
+    interp = pytest.importorskip("scipy.interpolate")
+    from suzerain_gb300 import synth
+    nbreak = Ny - k + 2
+    bp = np.array([2 * native.suzerain_htstretch2(2.0, 1.0, i / (nbreak - 1))
+                   for i in range(nbreak)])
+    bp[0], bp[-1] = 0.0, 2.0
+    n, kl, ku, bands, xi = collocation(native, k, bp, 2)
+    assert n == Ny
+    assert kl == ku == k - 2
+    t = np.concatenate([[bp[0]] * (k - 1), bp, [bp[-1]] * (k - 1)])
+    assert np.allclose(xi, [t[i + 1:i + k].mean() for i in range(n)], rtol=0, atol=1e-14)
+    ld = kl + 1 + ku
+    for m in range(3):
+        dense = np.zeros((n, n))
+        for j in range(n):
+            c = np.zeros(n); c[j] = 1
+            sp = interp.BSpline(t, c, k - 1, extrapolate=False)
+            vals = sp.derivative(m)(xi) if m else sp(xi)
+            dense[:, j] = np.nan_to_num(vals)
+        # scipy's right endpoint is open; take the last point from the left
+        for j in range(n):
+            c = np.zeros(n); c[j] = 1
+            sp = interp.BSpline(t, c, k - 1, extrapolate=True)
+            dense[-1, j] = (sp.derivative(m) if m else sp)(xi[-1] - 0.0)
+        mine = np.zeros((n, n))
+        for j in range(n):
+            for i in range(max(0, j - ku), min(n, j + kl + 1)):
+                mine[i, j] = bands[m, j, ku + i - j]
+        scale = np.abs(dense).max()
+        assert np.allclose(mine, dense, rtol=0, atol=1e-10 * scale), m
+    # the synthetic generator uses exactly these bands
+    cs = synth.make_case(S=5, Ny=Ny, k=k)
+    assert (cs.kl, cs.ku) == (kl, ku)
+    assert np.array_equal(cs.M.reshape(n, ld), bands[0])
+
+
+def test_synth_deterministic_and_config_geometry(native):
+    from suzerain_gb300 import synth
+    c0 = synth.CONFIGS[0]
+    cs, kx, kz, u = c0.batch()
+    cs2, kx2, kz2, u2 = c0.batch()
+    assert c0.nsys == 312 and len(kx) == 312 and u.shape == (312, 240)
+    assert np.array_equal(u, u2) and np.array_equal(cs.a, cs2.a)
+    assert (cs.KL, cs.KU, cs.LD) == (34, 34, 69)
+    # wavenumbers: kx = 0.5 m, kz = 1.5 * inorder(24, iz)
+    assert np.allclose(kx[:13], 0.5 * np.arange(13))
+    assert np.isclose(kz[13 * 13], 1.5 * -11)
+    assert abs(u.real.mean()) < 0.05 and abs(u.real.std() - 1) < 0.05
+    diag = np.diag(cs.a.reshape(5, 5))
+    assert ((diag >= 0.5) & (diag < 1.5)).all()
+    off = cs.a.reshape(5, 5)[~np.eye(5, dtype=bool)]
+    assert (np.abs(off) <= 0.1).all()
+    assert native.suzerain_inorder_wavenumber(24, 13) == -11

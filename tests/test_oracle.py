@@ -1,0 +1,274 @@
+"""Pin the oracle: restated algorithm vs the reference's golden vectors and,
+where it was built here, the reference's own compiled C (oracle/_ref).
+
+Mirrors tests/test_bsmbsm.cpp (q/qinv KATs, aPxpby grid, pack NaN poisoning,
+the Mathematica solve KAT) and tests/test_lapackext.c (Lotkin matrices, run
+here against the complex zcgbsvx as well)."""
+import ctypes as C
+import json
+import os
+
+import numpy as np
+import pytest
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def kat():
+    with open(os.path.join(GOLD, "bsmbsm_kat.json")) as f:
+        return json.load(f)
+
+
+def test_q_qinv_golden(oracle):
+    d = kat()
+    for i, v in d["q_S5n9"]:
+        assert oracle.q(5, 9, i) == v
+    for i, v in d["qinv_S5n9"]:
+        assert oracle.qinv(5, 9, i) == v
+    for S in range(1, 5):
+        for n in range(1, 10):
+            for i in range(S * n):
+                assert oracle.qinv(S, n, oracle.q(S, n, i)) == i
+
+
+def _kat_papt(oracle, d, complex_op):
+    """Pack the S=3 KAT operator with packf (LD+KL rows), NaN-poisoned."""
+    g = oracle.bsmbsm(d["S"], d["n"], d["kl"], d["ku"])
+    rows = g["LD"] + g["KL"]
+    papt = np.full(rows * g["N"], np.nan, dtype=np.complex128)
+    L = oracle.lib()
+    scale = 1j if complex_op else 1.0
+    for ih, row in enumerate(d["blocks"]):
+        for jh, blk in enumerate(row):
+            if blk is None:
+                rc = L.orc_zpack(d["S"], d["n"], ih, jh, d["kl"], d["ku"],
+                                 oracle._z(0), None, g["ld"], g["KL"], g["KU"],
+                                 papt[g["KL"]:].ctypes.data, rows)
+            else:
+                b = np.array(d[blk[0]], dtype=np.complex128) * blk[1]
+                rc = L.orc_zpack(d["S"], d["n"], ih, jh, d["kl"], d["ku"],
+                                 oracle._z(scale), b.ctypes.data, g["ld"],
+                                 g["KL"], g["KU"], papt[g["KL"]:].ctypes.data,
+                                 rows)
+            assert rc == 0
+    return g, papt
+
+
+@pytest.mark.parametrize("complex_op", [False, True])
+def test_solve_kat(oracle, complex_op):
+    """tests/test_bsmbsm.cpp:801-966: pack, zgbsv, unpermute == XR."""
+    d = kat()
+    g, papt = _kat_papt(oracle, d, complex_op)
+    # no NaN left inside the band
+    A = oracle.band_to_dense(papt, g["N"], g["KL"], g["KU"], g["LD"] + g["KL"],
+                             off=g["KL"])
+    assert not np.isnan(A).any()
+    br = np.array(d["BR"], dtype=np.complex128)
+    pb = np.zeros(g["N"], dtype=np.complex128)
+    rhs = br * (1j if complex_op else 1.0)   # i*op x = i*BR
+    assert oracle.zaPxpby("N", g["S"], g["n"], 1, rhs, 1, 0, pb, 1) == 0
+    info, ipiv = oracle.zgbtrf(papt, g["N"], g["KL"], g["KU"],
+                               g["LD"] + g["KL"])
+    assert info == 0
+    oracle.zgbtrs("N", papt, g["N"], g["KL"], g["KU"], g["LD"] + g["KL"], ipiv,
+                  pb)
+    x = np.zeros(g["N"], dtype=np.complex128)
+    assert oracle.zaPxpby("T", g["S"], g["n"], 1, pb, 1, 0, x, 1) == 0
+    xr = np.array(d["XR"])
+    tol = np.finfo(float).eps * d["tolerance_eps_multiple"]
+    assert np.allclose(x.real, xr, rtol=tol, atol=tol * np.abs(xr).max())
+    assert np.abs(x.imag).max() <= tol * np.abs(xr).max()
+
+
+def _rand_band(rng, n, kl, ku, extra_rows):
+    ldab = extra_rows + kl + ku + 1
+    ab = np.zeros(ldab * n, dtype=np.complex128)
+    for j in range(n):
+        for i in range(max(0, j - ku), min(n, j + kl + 1)):
+            ab[extra_rows + ku + i - j + j * ldab] = complex(rng.normal(), rng.normal())
+    return ab, ldab
+
+
+@pytest.mark.parametrize("n,kl,ku", [(40, 3, 5), (240, 34, 34), (13, 12, 0),
+                                     (7, 0, 3), (60, 48, 48), (1, 0, 0)])
+def test_gbtrf_matches_reference_lapack(oracle, n, kl, ku):
+    R = oracle.ref()
+    if R is None:
+        pytest.skip("reference build absent (no reference checkout here)")
+    rng = np.random.default_rng(n * 1000 + kl)
+    ab, ldab = _rand_band(rng, n, kl, ku, kl)
+    a1, a2 = ab.copy(), ab.copy()
+    info1, p1 = oracle.zgbtrf(a1, n, kl, ku, ldab)
+    p2 = np.zeros(n, np.int32)
+    info2 = R.suzerain_lapack_zgbtrf(n, n, kl, ku, a2.ctypes.data, ldab,
+                                     p2.ctypes.data)
+    assert info1 == info2 == 0
+    assert np.array_equal(p1, p2)
+    assert np.max(np.abs(a1 - a2)) <= 1e-12 * max(1, np.max(np.abs(a2)))
+    A = oracle.band_to_dense(ab, n, kl, ku, ldab, off=kl)
+    for tr, op in (("N", A), ("T", A.T), ("C", A.conj().T)):
+        b = rng.normal(size=n) + 1j * rng.normal(size=n)
+        x1, x2 = b.copy(), b.copy()
+        oracle.zgbtrs(tr, a1, n, kl, ku, ldab, p1, x1)
+        R.suzerain_lapack_zgbtrs(tr.encode(), n, kl, ku, 1, a2.ctypes.data,
+                                 ldab, p2.ctypes.data, x2.ctypes.data, n)
+        assert np.max(np.abs(x1 - x2)) <= 1e-11 * np.max(np.abs(x2))
+        assert np.max(np.abs(op @ x1 - b)) <= 1e-11 * np.max(np.abs(b)) * n
+
+
+def test_zero_pivot_info(oracle):
+    n, kl, ku = 6, 1, 1
+    ab, ldab = _rand_band(np.random.default_rng(3), n, kl, ku, kl)
+    for i in range(max(0, 3 - ku), min(n, 3 + kl + 1)):
+        ab[kl + ku + i - 3 + 3 * ldab] = 0   # column 3 identically zero
+    info, _ = oracle.zgbtrf(ab.copy(), n, kl, ku, ldab)
+    assert info == 4
+    R = oracle.ref()
+    if R is not None:
+        p = np.zeros(n, np.int32)
+        assert R.suzerain_lapack_zgbtrf(n, n, kl, ku, ab.copy().ctypes.data,
+                                        ldab, p.ctypes.data) == 4
+
+
+def test_pack_matches_reference(oracle):
+    R = oracle.ref()
+    if R is None:
+        pytest.skip("reference build absent")
+    L = oracle.lib()
+    for (S, n, kl, ku) in [(1, 10, 2, 3), (2, 2, 0, 0), (3, 17, 4, 3), (5, 12, 6, 6)]:
+        g = oracle.bsmbsm(S, n, kl, ku)
+        rng = np.random.default_rng(S * n)
+        b = rng.normal(size=g["ld"] * n) + 1j * rng.normal(size=g["ld"] * n)
+        p1 = np.full(g["LD"] * g["N"], np.nan, dtype=np.complex128)
+        p2 = p1.copy()
+        for ih in range(S):
+            for jh in range(S):
+                al = oracle._z(complex(ih + 2, jh - 1))
+                assert L.orc_zpack(S, n, ih, jh, kl, ku, al, b.ctypes.data,
+                                   g["ld"], g["KL"], g["KU"], p1.ctypes.data,
+                                   g["LD"]) == 0
+                assert R.suzerain_bsmbsm_zpack(S, n, ih, jh, kl, ku, al,
+                                               b.ctypes.data, g["ld"], g["KL"],
+                                               g["KU"], p2.ctypes.data,
+                                               g["LD"]) == 0
+        assert np.array_equal(np.isnan(p1), np.isnan(p2))
+        m = ~np.isnan(p1)
+        assert np.array_equal(p1[m], p2[m])
+        # every in-band position of P A P^T was written
+        A = oracle.band_to_dense(p1, g["N"], g["KL"], g["KU"], g["LD"])
+        assert not np.isnan(A).any()
+
+
+@pytest.mark.parametrize("trans", ["N", "T"])
+def test_aPxpby_grid(oracle, trans):
+    """tests/test_bsmbsm.cpp:352-474 complex grid, against the reference."""
+    R = oracle.ref()
+    for S in (1, 2, 5):
+        for n in (1, 7, 10):
+            N = S * n
+            for alpha in (1, 3, complex(-2, 2)):
+                for incx in (1, 2, -1, -2):
+                    for beta in (0, 1, -3, complex(4, -2)):
+                        for incy in (1, 3, -1, -3):
+                            x = np.cumsum(np.full(N * abs(incx), 2 * alpha + 1, dtype=np.complex128))
+                            y = np.cumsum(np.full(N * abs(incy), alpha - 7 + 1j, dtype=np.complex128))
+                            y1 = y.copy()
+                            assert oracle.zaPxpby(trans, S, n, alpha, x, incx,
+                                                  beta, y1, incy) == 0
+                            # permute + axpby by hand
+                            xs = x[::abs(incx)][:N]
+                            if incx < 0:
+                                xs = xs[::-1]
+                            Sq, nq = (S, n) if trans == "N" else (n, S)
+                            px = np.array([xs[(i % Sq) * nq + i // Sq] for i in range(N)])
+                            y2 = y.copy()
+                            ys = y2[::abs(incy)][:N].copy()
+                            if incy < 0:
+                                ys = ys[::-1]
+                            ys = alpha * px + beta * ys
+                            if incy < 0:
+                                ys = ys[::-1]
+                            y2[::abs(incy)][:N] = ys
+                            tol = 4 * np.finfo(float).eps
+                            assert np.allclose(y1, y2, rtol=tol, atol=tol * np.abs(y2).max())
+                            if R is not None and incx > 0 and incy > 0:
+                                y3 = y.copy()
+                                R.suzerain_bsmbsm_zaPxpby(trans.encode(), S, n, oracle._z(alpha),
+                                                          x.ctypes.data, incx, oracle._z(beta),
+                                                          y3.ctypes.data, incy)
+                                assert np.allclose(y1, y3, rtol=tol, atol=tol * np.abs(y3).max())
+
+
+def lotkin(n):
+    """Lotkin (1955) matrix as a dense band (tests/test_lapackext.c:41-72)."""
+    A = np.array([[1.0 if i == 0 else 1.0 / (i + j + 1) for j in range(n)]
+                  for i in range(n)])
+    return A
+
+
+def dense_to_band(A, kl, ku):
+    n = A.shape[0]
+    ldab = kl + ku + 1
+    ab = np.zeros(ldab * n, dtype=np.complex128)
+    for j in range(n):
+        for i in range(max(0, j - ku), min(n, j + kl + 1)):
+            ab[ku + i - j + j * ldab] = A[i, j]
+    return ab
+
+
+@pytest.mark.parametrize("n", [2, 5, 8, 12])
+def test_zcgbsvx_lotkin(oracle, n):
+    """Complex Lotkin systems: the reference only pins dsgbsvx this way."""
+    A = lotkin(n) * (1 + 0.5j)
+    x_true = np.ones(n, dtype=np.complex128)
+    b = A @ x_true
+    ab = dense_to_band(A, n - 1, n - 1)
+    out = oracle.zcgbsvx(ab, n, n - 1, n - 1, b, aiter=5, siter=25, diter=10,
+                         tolsc=1.0)
+    assert out["info"] == 0
+    assert out["tolsc"] <= 1.0
+    ores = np.linalg.norm(A @ out["x"] - b)
+    assert ores <= 10 * out["res"] + 1e-30
+    R = oracle.ref()
+    if R is not None:
+        kl = ku = n - 1
+        fact = C.create_string_buffer(b"N", 1)
+        apprx, afrob = C.c_int(0), C.c_double(-1)
+        afb = np.zeros((2 * kl + ku + 1) * n, dtype=np.complex128)
+        ipiv = np.zeros(n, np.int32)
+        x = np.zeros(n, dtype=np.complex128)
+        r = np.zeros(n, dtype=np.complex128)
+        si, di, ts, res = C.c_int(25), C.c_int(10), C.c_double(1.0), C.c_double(0)
+        bb = b.copy()
+        info = R.suzerain_lapackext_zcgbsvx(C.addressof(fact), C.addressof(apprx), 5,
+                                            b"N", n, kl, ku, ab.ctypes.data,
+                                            C.addressof(afrob), afb.ctypes.data,
+                                            ipiv.ctypes.data, bb.ctypes.data,
+                                            x.ctypes.data, C.addressof(si),
+                                            C.addressof(di), C.addressof(ts),
+                                            r.ctypes.data, C.addressof(res))
+        assert info == 0
+        assert fact.raw.decode() == out["fact"]
+        assert si.value == out["siter"] and di.value == out["diter"]
+        assert np.max(np.abs(x - out["x"])) <= 1e-6 * np.max(np.abs(x))
+
+
+def test_gbmv_matches_reference(oracle):
+    R = oracle.ref()
+    if R is None:
+        pytest.skip("reference build absent")
+    rng = np.random.default_rng(7)
+    for tr in "NTC":
+        for (m, n, kl, ku) in [(30, 30, 3, 5), (20, 25, 2, 7)]:
+            lda = kl + ku + 2
+            a = rng.normal(size=lda * n) + 1j * rng.normal(size=lda * n)
+            lx = n if tr == "N" else m
+            ly = m if tr == "N" else n
+            x = rng.normal(size=lx) + 1j * rng.normal(size=lx)
+            y = rng.normal(size=ly) + 1j * rng.normal(size=ly)
+            y1, y2 = y.copy(), y.copy()
+            oracle.zgbmv(tr, m, n, kl, ku, 2 - 1j, a, lda, x, 0.5, y1)
+            R.suzerain_blas_zgbmv(tr.encode(), m, n, kl, ku, oracle._z(2 - 1j),
+                                  a.ctypes.data, lda, x.ctypes.data, 1,
+                                  oracle._z(0.5), y2.ctypes.data, 1)
+            assert np.allclose(y1, y2, rtol=1e-13, atol=1e-13)
