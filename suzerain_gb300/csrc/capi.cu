@@ -216,7 +216,7 @@ extern "C" int sgb_zcgbsvx_batched(int nsys, int N, int KL, int KU, char trans, 
     if (rc) return rc;
     P.host_count = g_zc.hcount;
     RefineOutputs out;
-    rc = refine_batched(P, g_zc.p, out, (cudaStream_t) stream);
+    rc = refine_batched(P, g_zc.p, g_zc.bytes, out, (cudaStream_t) stream);
     if (rc) return sgb_set_error((cudaError_t) rc, "refine_batched", __FILE__, __LINE__);
     if (report) {
         k_report_copy<<<(nsys + 127) / 128, 128, 0, (cudaStream_t) stream>>>(
@@ -407,7 +407,7 @@ static int plan_substep(sgb_plan *p, char method, double phi_exp, double phi_imp
             if (rc) return rc;
             p->rws_bytes = need;
         }
-        int rc = refine_batched(P, p->rws, p->last, st);
+        int rc = refine_batched(P, p->rws, p->rws_bytes, p->last, st);
         if (rc) return sgb_set_error((cudaError_t) rc, "refine_batched", __FILE__, __LINE__);
     } else {
         return fail("sgb_plan_substep: method must be 'Z' or 'M'");

@@ -205,7 +205,8 @@ static int pack_impl(int S, int n, int ihat, int jhat, int kl, int ku, UT alpha,
     const bool azero = comps[0] == 0 && (sizeof alpha == sizeof(double) || comps[1] == 0);
     const int N = S * n;
     Stage sb(azero ? nullptr : b, azero ? 0 : (size_t) ldb * n * sizeof(US), true);
-    Stage sp(papt, (size_t) ldpapt * N * sizeof(UT), true);
+    // Positions written: column Cj, offsets 0..KL+KU -> extent (N-1)*ldpapt + KL+KU+1.
+    Stage sp(papt, ((size_t) (N - 1) * ldpapt + KL + KU + 1) * sizeof(UT), true);
     if (sb.err || sp.err) return err_of(sb.err ? sb.err : sp.err, "pack staging");
     k_pack<TS, TT><<<n, 64>>>(S, n, ihat, jhat, kl, ku, a, azero, (const TS *) sb.dev, ldb, KL, KU,
                               (TT *) sp.dev, ldpapt);
@@ -545,7 +546,7 @@ extern "C" int suzerain_lapackext_zcgbsvx(char *const fact, int *const apprx, co
     P.host_count = g_zcw.hcount;
     if (*afrob >= 0 && *tolsc != 0.0) P.afrob_in = *afrob;
     RefineOutputs out;
-    int rc = refine_batched(P, g_zcw.ws, out, 0);
+    int rc = refine_batched(P, g_zcw.ws, g_zcw.bytes, out, 0);
     if (rc) return err_of((cudaError_t) rc, "refine_batched");
     e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return err_of(e, "zcgbsvx");

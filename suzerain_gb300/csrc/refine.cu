@@ -240,37 +240,59 @@ static cudaError_t sync_count(const int *d, int *h, cudaStream_t st)
     return cudaStreamSynchronize(st);
 }
 
-// Workspace layout (device), carved from one allocation.
-size_t refine_workspace_bytes(const RefineProblem &P)
-{
-    const long long N = P.g.N;
-    const long long f32 = P.g.fac_elems() * 8, f64 = P.g.fac_elems() * 16;
-    size_t b = 0;
-    auto add = [&](size_t n) { b += (n + 255) & ~size_t(255); };
-    add(P.nsys * f32);              // complex64 factors
-    add(P.nsys * N * 4);            // ipiv32
-    add(P.nsys * 4);                // info32
-    add(P.nsys * N * 8);            // y32
-    add((size_t) P.nslot64 * f64);  // complex128 factor slots
-    add((size_t) P.nslot64 * N * 4);// ipiv64
-    add((size_t) P.nslot64 * 4);    // info64
-    add(P.nsys * N * 16);           // r
-    add(P.nsys * 8 * 9);            // doubles: res lastres tolconst tol tolsc rnorm xnorm afrob bnorm
-    add(P.nsys * 4 * 6);            // ints: status siter diter info fact(as int) pad
-    add(P.nsys * 4 * 4);            // lists S, S', D, D'
-    add(64);                        // counters
-    return b;
-}
-
+// Workspace layout (device), carved from one allocation.  The same walk
+// sizes the workspace (base == nullptr) and carves it, so they cannot drift.
 struct Carve {
     char *p; size_t off = 0;
     template <typename T> T *take(size_t n)
     {
-        T *r = reinterpret_cast<T *>(p + off);
+        T *r = p ? reinterpret_cast<T *>(p + off) : nullptr;
         off += (n * sizeof(T) + 255) & ~size_t(255);
         return r;
     }
 };
+
+struct RefineLayout {
+    float2 *fac32; int *ipiv32, *info32; float2 *y32;
+    double2 *fac64; int *ipiv64, *info64; double2 *r;
+    RefineState rs;
+    double *rnorm, *xnorm, *afrob, *bnorm;
+    int *listS, *listS2, *listD, *listD2, *cnt;
+};
+
+static size_t carve_layout(const RefineProblem &P, char *base, RefineLayout &Lo)
+{
+    const int nsys = P.nsys, N = P.g.N;
+    Carve cv{base};
+    Lo.fac32 = cv.take<float2>((size_t) nsys * P.g.fac_elems());
+    Lo.ipiv32 = cv.take<int>((size_t) nsys * N);
+    Lo.info32 = cv.take<int>(nsys);
+    Lo.y32 = cv.take<float2>((size_t) nsys * N);
+    Lo.fac64 = cv.take<double2>((size_t) P.nslot64 * P.g.fac_elems());
+    Lo.ipiv64 = cv.take<int>((size_t) P.nslot64 * N);
+    Lo.info64 = cv.take<int>(P.nslot64);
+    Lo.r = cv.take<double2>((size_t) nsys * N);
+    RefineState &rs = Lo.rs;
+    rs.res = cv.take<double>(nsys); rs.lastres = cv.take<double>(nsys);
+    rs.tolconst = cv.take<double>(nsys); rs.tol = cv.take<double>(nsys);
+    rs.tolsc = cv.take<double>(nsys);
+    Lo.rnorm = cv.take<double>(nsys); Lo.xnorm = cv.take<double>(nsys);
+    Lo.afrob = cv.take<double>(nsys); Lo.bnorm = cv.take<double>(nsys);
+    rs.status = cv.take<int>(nsys); rs.siter = cv.take<int>(nsys);
+    rs.diter = cv.take<int>(nsys); rs.info = cv.take<int>(nsys);
+    rs.fact = cv.take<char>((size_t) nsys);
+    Lo.listS = cv.take<int>(nsys); Lo.listS2 = cv.take<int>(nsys);
+    Lo.listD = cv.take<int>(nsys); Lo.listD2 = cv.take<int>(nsys);
+    Lo.cnt = cv.take<int>(16);   // [0] S  [1] S'  [2] D  [4] chunk  [5,7,8] D lists
+    rs.use_eps = (P.tolsc == 0.0);
+    return cv.off;
+}
+
+size_t refine_workspace_bytes(const RefineProblem &P)
+{
+    RefineLayout Lo;
+    return carve_layout(P, nullptr, Lo);
+}
 
 __global__ void k_fill(int n, double *__restrict__ p, double v)
 {
@@ -287,35 +309,23 @@ __global__ void k_copy_rows(int nsys, const double2 *__restrict__ src, long long
     dst[s * ds + i] = src[s * ss + i];
 }
 
-int refine_batched(const RefineProblem &P, void *workspace, RefineOutputs &out,
-                   cudaStream_t st)
+int refine_batched(const RefineProblem &P, void *workspace, size_t workspace_bytes,
+                   RefineOutputs &out, cudaStream_t st)
 {
     const int nsys = P.nsys, N = P.g.N;
     if (nsys == 0) return 0;
     if (P.nslot64 < 1 || !P.host_count) return (int) cudaErrorInvalidValue;
-    Carve cv{reinterpret_cast<char *>(workspace)};
-    float2 *fac32 = cv.take<float2>(nsys * P.g.fac_elems());
-    int *ipiv32 = cv.take<int>((size_t) nsys * N);
-    int *info32 = cv.take<int>(nsys);
-    float2 *y32 = cv.take<float2>((size_t) nsys * N);
-    double2 *fac64 = cv.take<double2>((size_t) P.nslot64 * P.g.fac_elems());
-    int *ipiv64 = cv.take<int>((size_t) P.nslot64 * N);
-    int *info64 = cv.take<int>(P.nslot64);
-    double2 *r = cv.take<double2>((size_t) nsys * N);
-    RefineState rs;
-    rs.res = cv.take<double>(nsys); rs.lastres = cv.take<double>(nsys);
-    rs.tolconst = cv.take<double>(nsys); rs.tol = cv.take<double>(nsys);
-    rs.tolsc = cv.take<double>(nsys);
-    double *rnorm = cv.take<double>(nsys), *xnorm = cv.take<double>(nsys);
-    double *afrob = cv.take<double>(nsys), *bnorm = cv.take<double>(nsys);
-    rs.status = cv.take<int>(nsys); rs.siter = cv.take<int>(nsys);
-    rs.diter = cv.take<int>(nsys); rs.info = cv.take<int>(nsys);
-    rs.fact = cv.take<char>((size_t) nsys * 4);
-    cv.take<int>(nsys);
-    int *listS = cv.take<int>(nsys), *listS2 = cv.take<int>(nsys);
-    int *listD = cv.take<int>(nsys), *listD2 = cv.take<int>(nsys);
-    int *cnt = cv.take<int>(16);   // [0] S  [1] S'  [2] D  [4] chunk  [7] D active
-    rs.use_eps = (P.tolsc == 0.0);
+    if (workspace_bytes < refine_workspace_bytes(P)) return (int) cudaErrorInvalidValue;
+    RefineLayout Lo;
+    carve_layout(P, reinterpret_cast<char *>(workspace), Lo);
+    float2 *fac32 = Lo.fac32; int *ipiv32 = Lo.ipiv32, *info32 = Lo.info32;
+    float2 *y32 = Lo.y32; double2 *fac64 = Lo.fac64;
+    int *ipiv64 = Lo.ipiv64, *info64 = Lo.info64;
+    double2 *r = Lo.r;
+    RefineState rs = Lo.rs;
+    double *rnorm = Lo.rnorm, *xnorm = Lo.xnorm, *afrob = Lo.afrob, *bnorm = Lo.bnorm;
+    int *listS = Lo.listS, *listS2 = Lo.listS2, *listD = Lo.listD, *listD2 = Lo.listD2;
+    int *cnt = Lo.cnt;
 
     int *hcnt = P.host_count;
     PhaseTimer dummy;

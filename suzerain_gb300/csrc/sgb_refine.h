@@ -45,7 +45,7 @@ struct RefineOutputs {
 };
 
 size_t refine_workspace_bytes(const RefineProblem &P);
-int refine_batched(const RefineProblem &P, void *workspace, RefineOutputs &out,
-                   cudaStream_t st);
+int refine_batched(const RefineProblem &P, void *workspace, size_t workspace_bytes,
+                   RefineOutputs &out, cudaStream_t st);
 
 }  // namespace sgb

@@ -16,7 +16,8 @@ import numpy as np
 from . import _native as nat
 
 SEED_BASE = 0x5A2E0000
-DIRICHLET_MOMENTUM = 0b01110   # equations 1..3 (momentum) get wall rows
+DIRICHLET_MOMENTUM = 0b01110   # momentum equations 1..3 only (near-singular stress case)
+DIRICHLET_ALL = 0b11111        # every second-order equation gets its two wall rows
 
 
 @dataclass
@@ -30,7 +31,7 @@ class SynthCase:
     offscale: float = 0.1
     complex_coupling: bool = False
     seed: int = SEED_BASE
-    dirichlet_mask: int = DIRICHLET_MOMENTUM
+    dirichlet_mask: int = DIRICHLET_ALL
     kl: int = 0
     ku: int = 0
     M: np.ndarray = field(default=None, repr=False)
@@ -78,7 +79,7 @@ class SynthCase:
 
 def make_case(S=5, Ny=48, k=8, htdelta=2.0, left=0.0, right=2.0,
               offscale=0.1, complex_coupling=False, seed=SEED_BASE,
-              dirichlet_mask=DIRICHLET_MOMENTUM) -> SynthCase:
+              dirichlet_mask=DIRICHLET_ALL) -> SynthCase:
     L = nat.load()
     kl, ku = C.c_int(0), C.c_int(0)
     rc = L.sgb_synth_case(S, Ny, k, htdelta, left, right, offscale,
@@ -142,6 +143,7 @@ class Config:
     phi: float
     offscale: float = 0.1
     seed: int = SEED_BASE
+    dirichlet_mask: int = DIRICHLET_ALL
 
     @property
     def nsys(self) -> int:
@@ -149,7 +151,8 @@ class Config:
 
     def case(self, complex_coupling=False) -> SynthCase:
         return make_case(S=self.S, Ny=self.Ny, k=self.k, offscale=self.offscale,
-                         complex_coupling=complex_coupling, seed=self.seed)
+                         complex_coupling=complex_coupling, seed=self.seed,
+                         dirichlet_mask=self.dirichlet_mask)
 
     def batch(self, complex_coupling=False):
         cs = self.case(complex_coupling)
@@ -176,9 +179,15 @@ SMR91_BETA = (37 / 160, 5 / 24, 1 / 6)
 SMR91_GAMMA = (8 / 15, 5 / 12, 3 / 4)
 
 
-def smr91_phis(phi_imp: float, substep: int = 0):
-    """(phi_explicit, phi_implicit) of an SMR91 substep whose implicit
-    operator is M + phi_imp L: phi_imp = -dt beta_i fixes dt, and the
-    explicit operator is M + dt alpha_i L."""
-    dt = -phi_imp / SMR91_BETA[substep]
-    return dt * SMR91_ALPHA[substep], phi_imp
+def smr91_phis(dt_beta: float, substep: int = 0, explicit: bool = True):
+    """(phi_explicit, phi_implicit) of SMR91 substep `substep` whose implicit
+    scale dt*beta_i is dt_beta (the configurations' phi*dt).
+
+    The substep solves (M - dt beta_i L) u' = (M + dt alpha_i L) u + ...
+    (suzerain/lowstorage.hpp:1403-1436), so the block operator M + phi L of
+    the model is assembled with phi_implicit = -dt beta_i and applied with
+    phi_explicit = dt alpha_i.  L = a D1 + b D2 - c k^2 M is dissipative
+    (b, c > 0), which makes M - dt beta L the well-posed implicit operator.
+    explicit=False returns phi_explicit = 0 (solve-only step)."""
+    dt = dt_beta / SMR91_BETA[substep]
+    return (dt * SMR91_ALPHA[substep] if explicit else 0.0), -dt_beta

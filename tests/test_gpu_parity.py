@@ -197,7 +197,8 @@ def test_zcgbsvx_batched_fallback_to_double(lib, oracle, torch_cuda):
     g = _zcgbsvx_batch(lib, torch, [ab, good], np.vstack([b, bg]), n, kl, ku, (5, 25, 10, 1.0))
     o = oracle.zcgbsvx(ab, n, kl, ku, b[0], aiter=5, siter=25, diter=10, tolsc=1.0)
     assert chr(g["fact"][0]) == o["fact"] == "D"
-    assert g["diter"][0] == o["diter"]
+    # cond(Lotkin_10) ~ 1e13: FMA rounding can move res across tol by one step
+    assert abs(int(g["diter"][0]) - o["diter"]) <= 1
     assert g["tolsc"][0] <= 1.0 and g["info"][0] == 0
     assert np.linalg.norm(A @ g["x"][0] - b[0]) <= 10 * g["res"][0] + 1e-30
     assert chr(g["fact"][1]) == "S" and g["info"][1] == 0
@@ -214,13 +215,27 @@ def config0(complex_coupling=False):
     return c, cs, kx, kz, u
 
 
+def forward_tolerance(oracle, cs, kx, kz, phi_imp, eps=2.220446049250313e-16):
+    """Per-system bound on the forward difference of two backward-stable
+    solvers: max(1e-11, 8 kappa_inf(A) eps).  The synthetic operators are
+    ill-conditioned (kappa ~ 1e7), so the reference's own LAPACK builds
+    differ from each other by ~1e-9 on them; well-conditioned systems keep
+    the 1e-11 bar (test_gbtrf_*, test_zcgbsvx_batched_matches_oracle)."""
+    tol = np.empty(len(kx))
+    for s in range(len(kx)):
+        A = oracle.band_to_dense(oracle.assemble_case(cs, phi_imp, kx[s], kz[s]), cs.N,
+                                 cs.KL, cs.KU, cs.LD)
+        tol[s] = max(1e-11, 8 * np.linalg.cond(A, np.inf) * eps)
+    return tol
+
+
 @pytest.mark.parametrize("complex_coupling", [False, True])
 @pytest.mark.parametrize("explicit", [False, True])
 def test_plan_plain_fp64_matches_oracle(lib, oracle, torch_cuda, complex_coupling, explicit):
     torch = torch_cuda
     from suzerain_gb300 import plan as P, synth
     c, cs, kx, kz, u = config0(complex_coupling)
-    phi_e, phi_i = synth.smr91_phis(c.phi) if explicit else (0.0, c.phi)
+    phi_e, phi_i = synth.smr91_phis(c.phi, explicit=explicit)
     pl = P.Plan(cs, kx, kz)
     du = dev(torch, u)
     out = torch.zeros_like(du)
@@ -231,9 +246,10 @@ def test_plan_plain_fp64_matches_oracle(lib, oracle, torch_cuda, complex_couplin
     berr = pl.backward_error()
     o = oracle.batch_solve(cs, kx, kz, u, phi_exp=phi_e, phi_imp=phi_i, nthreads=8)
     assert (rep["info"] == o["info"]).all() and (o["info"] == 0).all()
-    rel = np.max(np.abs(x - o["x"]), axis=1) / np.max(np.abs(o["x"]), axis=1)
-    assert rel.max() <= 1e-11, rel.max()
     assert berr.max() <= 1e-13, berr.max()
+    rel = np.max(np.abs(x - o["x"]), axis=1) / np.max(np.abs(o["x"]), axis=1)
+    tol = forward_tolerance(oracle, cs, kx, kz, phi_i)
+    assert (rel <= tol).all(), (rel / tol).max()
 
 
 @pytest.mark.parametrize("complex_coupling", [False, True])
@@ -258,11 +274,38 @@ def test_plan_mixed_matches_oracle(lib, oracle, torch_cuda, complex_coupling):
     assert berr.max() <= 1e-12, berr.max()
     assert (rep["tolsc"] <= 1.0).all()
     rel = np.max(np.abs(x - o["x"]), axis=1) / np.max(np.abs(o["x"]), axis=1)
-    assert rel.max() <= 1e-9, rel.max()
+    tol = forward_tolerance(oracle, cs, kx, kz, phi_i)
+    assert (rel <= 10 * tol).all(), (rel / tol).max()
     # the same convergence decisions as the reference algorithm, per system
     assert set(rep["fact"]) <= {"S", "D"}
     agree = np.mean(np.abs(rep["siter"] - om["siter"]) <= 1)
     assert agree >= 0.95, agree
+
+
+def test_plan_mixed_fallback_at_scale(lib, oracle, torch_cuda):
+    """Walls on the momentum equations only leave two second-order equations
+    without boundary rows (kappa up to 1e8 at Ny=48): complex64 refinement
+    stalls for many systems, which must finish on complex128 factors.  Few
+    fallback slots force several chunks."""
+    torch = torch_cuda
+    from suzerain_gb300 import plan as P, synth
+    c = synth.Config(**{**synth.CONFIGS[0].__dict__, "dirichlet_mask": synth.DIRICHLET_MOMENTUM})
+    cs, kx, kz, u = c.batch()
+    synth.zero_dirichlet_rows(cs, u)
+    phi_e, phi_i = synth.smr91_phis(c.phi)
+    pl = P.Plan(cs, kx, kz, max_double_slots=17)
+    out = torch.zeros(u.shape, dtype=torch.complex128, device="cuda")
+    pl.substep("M", phi_e, phi_i, dev(torch, u), out, P.RefineSpec(aiter=5, siter=25, diter=5, tolsc=145.0))
+    torch.cuda.synchronize()
+    rep = pl.report()
+    berr = pl.backward_error()
+    om = oracle.batch_solve(cs, kx, kz, u, phi_exp=phi_e, phi_imp=phi_i, mixed=True, tolsc=145.0,
+                            nthreads=8)
+    nd = sum(1 for f in rep["fact"] if f == "D")
+    nd_o = sum(1 for f in om["fact"] if f == "D")
+    assert nd >= 17 and abs(nd - nd_o) <= 0.1 * len(kx), (nd, nd_o)
+    assert (rep["info"] == 0).all()
+    assert berr.max() <= 1e-12, berr.max()
 
 
 def test_plan_result_independent_of_batch(lib, torch_cuda):
@@ -276,8 +319,8 @@ def test_plan_result_independent_of_batch(lib, torch_cuda):
     for method in ("Z", "M"):
         a = torch.zeros(u.shape, dtype=torch.complex128, device="cuda")
         b = torch.zeros((len(sub_idx), u.shape[1]), dtype=torch.complex128, device="cuda")
-        full.substep(method, 0.0, c.phi, dev(torch, u), a, P.RefineSpec(tolsc=145.0))
-        part.substep(method, 0.0, c.phi, dev(torch, u[sub_idx]), b, P.RefineSpec(tolsc=145.0))
+        full.substep(method, 0.0, -c.phi, dev(torch, u), a, P.RefineSpec(tolsc=145.0))
+        part.substep(method, 0.0, -c.phi, dev(torch, u[sub_idx]), b, P.RefineSpec(tolsc=145.0))
         torch.cuda.synchronize()
         assert np.array_equal(a.cpu().numpy()[sub_idx], b.cpu().numpy())
 
@@ -288,10 +331,10 @@ def test_plan_host_entry_matches_device_entry(lib, torch_cuda):
     c, cs, kx, kz, u = config0()
     pl = P.Plan(cs, kx, kz)
     a = torch.zeros(u.shape, dtype=torch.complex128, device="cuda")
-    pl.substep("M", 0.0, c.phi, dev(torch, u), a, P.RefineSpec(tolsc=145.0))
+    pl.substep("M", 0.0, -c.phi, dev(torch, u), a, P.RefineSpec(tolsc=145.0))
     torch.cuda.synchronize()
     h = np.zeros_like(u)
-    pl.substep_host("M", 0.0, c.phi, u, h, P.RefineSpec(tolsc=145.0))
+    pl.substep_host("M", 0.0, -c.phi, u, h, P.RefineSpec(tolsc=145.0))
     assert np.array_equal(a.cpu().numpy(), h)
 
 
@@ -356,7 +399,11 @@ def test_dropin_pack_and_aPxpby_match_oracle(lib, oracle):
                                                    nat.zc(0.5j), y1.ctypes.data, incy) == 0
                 oracle.zaPxpby(trans, S, n, 3 - 1j, x, incx, 0.5j, y2, incy)
                 assert np.allclose(y1, y2, rtol=4 * np.finfo(float).eps, atol=1e-14)
-    assert lib.suzerain_bsmbsm_zaPxpby(b"X", 2, 2, nat.zc(1), None, 1, nat.zc(0), None, 1) == 1
+    # argument checks in the reference's order: S, n, aliasing, then trans
+    xa, ya = np.zeros(4, complex), np.zeros(4, complex)
+    assert lib.suzerain_bsmbsm_zaPxpby(b"X", 2, 2, nat.zc(1), xa.ctypes.data, 1, nat.zc(0), ya.ctypes.data, 1) == 1
+    assert lib.suzerain_bsmbsm_zaPxpby(b"N", 2, 2, nat.zc(1), xa.ctypes.data, 1, nat.zc(0), xa.ctypes.data, 1) == 58
+    assert lib.suzerain_bsmbsm_zaPxpby(b"N", -1, 2, nat.zc(1), xa.ctypes.data, 1, nat.zc(0), ya.ctypes.data, 1) == 2
 
 
 def test_dropin_zcgbsvx_lotkin(lib, oracle):
