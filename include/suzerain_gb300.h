@@ -275,6 +275,26 @@ int sgb_zcgbsvx_batched(int nsys, int N, int KL, int KU, char trans,
                         const void *b, void *x, const sgb_refine_spec *spec,
                         const sgb_refine_report *report, void *stream);
 
+/** sgb_zcgbsvx_batched for callers that cannot allocate device memory
+ *  (hosts that reserve all of HBM in their own arena, or solver loops that
+ *  must not enter the driver's allocator once stepping has begun).  Same
+ *  arguments and results; no counterpart in the reference.  It calls no
+ *  cudaMalloc/cudaFree and no allocating library routine: its scratch is a
+ *  fixed 64 MiB __device__ array inside this library, which every GPU that
+ *  loads the library holds until process exit.  Problems whose scratch
+ *  (about 2.4 MB per system at N = 960, KL = KU = 34) exceeds 64 MiB are
+ *  rejected with an error naming both sizes.  The first call on a device
+ *  looks up the array's device address (cudaGetSymbolAddress) with that
+ *  device current; make that first call before any stream capture.  All
+ *  calls share the one array: calls that overlap on the GPU (different
+ *  streams without synchronization) race; the kernels initialise every
+ *  value they read, so one call's leftovers never affect the next. */
+int sgb_zcgbsvx_batched_static(int nsys, int N, int KL, int KU, char trans,
+                               const void *ab, int ldab, long long ab_stride,
+                               const void *b, void *x,
+                               const sgb_refine_spec *spec,
+                               const sgb_refine_report *report, void *stream);
+
 /** One synthetic case (see sgb_case in the model header): bands and
  *  coefficients.  For sgb_plan_create the pointers are HOST pointers. */
 typedef struct sgb_case {

@@ -111,6 +111,9 @@ _SIGS = {
     "sgb_zcgbsvx_batched": (_i, [_i, _i, _i, _i, C.c_char, _p, _i, _ll, _p,
                                  _p, C.POINTER(RefineSpec),
                                  C.POINTER(RefineReport), _p]),
+    "sgb_zcgbsvx_batched_static": (_i, [_i, _i, _i, _i, C.c_char, _p, _i, _ll,
+                                        _p, _p, C.POINTER(RefineSpec),
+                                        C.POINTER(RefineReport), _p]),
     "sgb_plan_create": (_p, [C.POINTER(Case), _i, _p, _p, _i]),
     "sgb_plan_destroy": (_i, [_p]),
     "sgb_plan_device_bytes": (_sz, [_p]),
