@@ -181,6 +181,8 @@ def run_ours(args):
     if world > 1:   # weak scaling: each rank its own wavenumber block (seed)
         cfg = synth.Config(**{**cfg.__dict__, "seed": cfg.seed + 1000 * rank})
     cs, kx, kz, u = cfg.batch()
+    if args.nsys:          # first nsys systems of the same batch (profiling runs)
+        kx, kz, u = kx[:args.nsys], kz[:args.nsys], u[:args.nsys]
     nsys, N = u.shape
     phi_e, phi_i = synth.smr91_phis(cfg.phi)
     spec = P.RefineSpec(**SPEC)
@@ -332,6 +334,8 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=4096)
     ap.add_argument("--ref-sample", type=int, default=4096)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--nsys", type=int, default=0,
+                    help="use only the first NSYS systems of the batch (profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

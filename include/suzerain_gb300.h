@@ -244,6 +244,22 @@ int sgb_gbtrf_batched(char prec, int nsys, int N, int KL, int KU,
                       const void *ab, int ldab, long long ab_stride,
                       void *fac, int *ipiv, int *info, void *stream);
 
+/** sgb_gbtrf_batched with the kernel chosen explicitly: variant 0 is the
+ *  blocked kernel with panel width nb (4, 8 or 16; KL <= 52), variant 1 the
+ *  unblocked one (nb ignored).  Both produce zgbtf2's pivots and factor. */
+int sgb_gbtrf_batched_ex(char prec, int nsys, int N, int KL, int KU,
+                         const void *ab, int ldab, long long ab_stride,
+                         void *fac, int *ipiv, int *info, int variant, int nb,
+                         void *stream);
+
+/** Diagnostics: the blocked factor with cycle counters.  cycles_dev (6
+ *  device uint64, accumulated) receives the clock cycles all warps spent in
+ *  initial load, panel, interchanges+U12, GEMM, U output, retire/load. */
+int sgb_gbtrf_phase_cycles(char prec, int nsys, int N, int KL, int KU,
+                           const void *ab, int ldab, long long ab_stride,
+                           void *fac, int *ipiv, int *info, int nb,
+                           unsigned long long *cycles_dev, void *stream);
+
 /** Batched solve op(A) x = b with row-panel factors; b, x complex128
  *  (nsys x N, stride N).  x may equal b. */
 int sgb_gbtrs_batched(char prec, char trans, int nsys, int N, int KL, int KU,

@@ -105,6 +105,10 @@ _SIGS = {
     "sgb_factor_elems": (_ll, [_i, _i, _i]),
     "sgb_gbtrf_batched": (_i, [C.c_char, _i, _i, _i, _i, _p, _i, _ll, _p, _p,
                                _p, _p]),
+    "sgb_gbtrf_batched_ex": (_i, [C.c_char, _i, _i, _i, _i, _p, _i, _ll, _p,
+                                  _p, _p, _i, _i, _p]),
+    "sgb_gbtrf_phase_cycles": (_i, [C.c_char, _i, _i, _i, _i, _p, _i, _ll, _p,
+                                    _p, _p, _i, _p, _p]),
     "sgb_gbtrs_batched": (_i, [C.c_char, C.c_char, _i, _i, _i, _i, _p, _p, _p,
                                _p, _p]),
     "sgb_factor_to_lapack": (_i, [C.c_char, _i, _i, _i, _i, _p, _p, _p]),

@@ -72,6 +72,45 @@ extern "C" int sgb_gbtrf_batched(char prec, int nsys, int N, int KL, int KU, con
     a.prec = prec; a.g = {N, KL, KU}; a.nsys = nsys;
     a.src = {reinterpret_cast<const double2 *>(ab), ab_stride, ldab, 0};
     a.fac = fac; a.fac_stride = a.g.fac_elems(); a.ipiv = ipiv; a.info = info;
+    count_launch(1);
+    SGB_CUDA_TRY(launch_gbtrf(a, (cudaStream_t) stream));
+    return 0;
+}
+
+extern "C" int sgb_gbtrf_batched_ex(char prec, int nsys, int N, int KL, int KU, const void *ab,
+                                    int ldab, long long ab_stride, void *fac, int *ipiv,
+                                    int *info, int variant, int nb, void *stream)
+{
+    if (prec != 'Z' && prec != 'C') return fail("sgb_gbtrf_batched_ex: prec must be 'Z' or 'C'");
+    if (!geom_ok(N, KL, KU) || ldab < KL + KU + 1 || nsys < 0)
+        return fail("sgb_gbtrf_batched_ex: bad geometry");
+    if (variant != 0 && variant != 1) return fail("sgb_gbtrf_batched_ex: variant must be 0 or 1");
+    if (variant == 0 && !gbtrf_blk_supported({N, KL, KU}, nb))
+        return fail("sgb_gbtrf_batched_ex: blocked kernel needs nb in {4,8,16} and KL <= 52");
+    GbtrfArgs a;
+    a.prec = prec; a.g = {N, KL, KU}; a.nsys = nsys;
+    a.src = {reinterpret_cast<const double2 *>(ab), ab_stride, ldab, 0};
+    a.fac = fac; a.fac_stride = a.g.fac_elems(); a.ipiv = ipiv; a.info = info;
+    a.variant = variant; a.nb = nb;
+    count_launch(1);
+    SGB_CUDA_TRY(launch_gbtrf(a, (cudaStream_t) stream));
+    return 0;
+}
+
+extern "C" int sgb_gbtrf_phase_cycles(char prec, int nsys, int N, int KL, int KU, const void *ab,
+                                      int ldab, long long ab_stride, void *fac, int *ipiv,
+                                      int *info, int nb, unsigned long long *cycles_dev,
+                                      void *stream)
+{
+    if (prec != 'Z' && prec != 'C') return fail("sgb_gbtrf_phase_cycles: prec must be 'Z' or 'C'");
+    if (!geom_ok(N, KL, KU) || ldab < KL + KU + 1 || !gbtrf_blk_supported({N, KL, KU}, nb))
+        return fail("sgb_gbtrf_phase_cycles: bad geometry");
+    GbtrfArgs a;
+    a.prec = prec; a.g = {N, KL, KU}; a.nsys = nsys;
+    a.src = {reinterpret_cast<const double2 *>(ab), ab_stride, ldab, 0};
+    a.fac = fac; a.fac_stride = a.g.fac_elems(); a.ipiv = ipiv; a.info = info;
+    a.nb = nb; a.prof = cycles_dev;
+    count_launch(1);
     SGB_CUDA_TRY(launch_gbtrf(a, (cudaStream_t) stream));
     return 0;
 }

@@ -227,6 +227,7 @@ static cudaError_t launch_one(const GbtrfArgs &a, cudaStream_t st)
 
 cudaError_t launch_gbtrf(const GbtrfArgs &a, cudaStream_t st)
 {
+    if (a.variant == 0 && gbtrf_blk_supported(a.g, a.nb)) return launch_gbtrf_blk(a, a.nb, st);
     const bool fwd = a.rhs != nullptr;
     if (a.prec == 'Z') {
         if (a.model) return fwd ? launch_one<double, true, true>(a, st) : launch_one<double, true, false>(a, st);

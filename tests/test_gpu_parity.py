@@ -78,6 +78,43 @@ def test_gbtrf_batched_fp64_matches_zgbtf2(lib, oracle, torch_cuda, n, kl, ku):
         assert np.max(np.abs(lap[s] - full)) <= 1e-12 * scale
 
 
+@pytest.mark.parametrize("n,kl,ku", GEOMS)
+@pytest.mark.parametrize("prec", ["Z", "C"])
+def test_blocked_factor_equals_unblocked(lib, torch_cuda, n, kl, ku, prec):
+    """The blocked kernel defers the rank-1 updates into a GEMM but applies
+    the same multiply-adds in the same order: factors are bit-identical."""
+    torch = torch_cuda
+    rng = np.random.default_rng(300 + n + kl)
+    nsys = 5
+    bands = [rand_band(rng, n, kl, ku)[0] for _ in range(nsys)]
+    # make pivoting frequent: scale random rows up
+    for b_ in bands:
+        for j in range(n):
+            if rng.random() < 0.3:
+                for i in range(max(0, j - ku), min(n, j + kl + 1)):
+                    b_[ku + i - j + j * (kl + ku + 1)] *= 8.0
+    ld = kl + ku + 1
+    ab = dev(torch, np.stack(bands))
+    fe = lib.sgb_factor_elems(n, kl, ku)
+    dt = torch.complex128 if prec == "Z" else torch.complex64
+    outs = []
+    for variant, nb in ((1, 8), (0, 4), (0, 8), (0, 16)):
+        if variant == 0 and kl > 52:
+            continue
+        fac = torch.full((nsys * fe,), float("nan"), dtype=dt, device="cuda")
+        ipiv = torch.zeros(nsys * n, dtype=torch.int32, device="cuda")
+        info = torch.zeros(nsys, dtype=torch.int32, device="cuda")
+        assert lib.sgb_gbtrf_batched_ex(prec.encode(), nsys, n, kl, ku, ab.data_ptr(), ld, ld * n,
+                                        fac.data_ptr(), ipiv.data_ptr(), info.data_ptr(), variant,
+                                        nb, 0) == 0, lib.sgb_last_error().decode()
+        torch.cuda.synchronize()
+        outs.append((fac.cpu().numpy(), ipiv.cpu().numpy(), info.cpu().numpy()))
+    for fac, ipiv, info in outs[1:]:
+        assert np.array_equal(ipiv, outs[0][1]) and np.array_equal(info, outs[0][2])
+        assert np.array_equal(fac.view(np.float32 if prec == "C" else np.float64),
+                              outs[0][0].view(np.float32 if prec == "C" else np.float64))
+
+
 @pytest.mark.parametrize("n,kl,ku", [(40, 3, 5), (240, 34, 34), (97, 48, 48)])
 @pytest.mark.parametrize("trans", ["N", "T", "C"])
 @pytest.mark.parametrize("prec", ["Z", "C"])
