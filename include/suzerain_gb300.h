@@ -245,20 +245,31 @@ int sgb_gbtrf_batched(char prec, int nsys, int N, int KL, int KU,
                       void *fac, int *ipiv, int *info, void *stream);
 
 /** sgb_gbtrf_batched with the kernel chosen explicitly: variant 0 is the
- *  blocked kernel with panel width nb (4, 8 or 16; KL <= 52), variant 1 the
- *  unblocked one (nb ignored).  Both produce zgbtf2's pivots and factor. */
+ *  blocked kernel with panel width nb (4, 8 or 16) and nw warps per system
+ *  (1, 2 or 4; KL <= 52, 56, 64 respectively; N < 65536), variant 1 the
+ *  unblocked one (nb, nw ignored).  nb or nw 0 takes the shape recorded by
+ *  sgb_gbtrf_set_shape for (prec, N, KL, KU), else the built-in default.
+ *  Every shape produces zgbtf2's pivots and factor, bit for bit. */
 int sgb_gbtrf_batched_ex(char prec, int nsys, int N, int KL, int KU,
                          const void *ab, int ldab, long long ab_stride,
                          void *fac, int *ipiv, int *info, int variant, int nb,
-                         void *stream);
+                         int nw, void *stream);
 
 /** Diagnostics: the blocked factor with cycle counters.  cycles_dev (6
- *  device uint64, accumulated) receives the clock cycles all warps spent in
- *  initial load, panel, interchanges+U12, GEMM, U output, retire/load. */
+ *  device uint64, accumulated) receives the clock cycles the first warp of
+ *  every system spent in initial load, panel, interchanges+U12, GEMM, U
+ *  output, retire/load (waits at the phase barriers included). */
 int sgb_gbtrf_phase_cycles(char prec, int nsys, int N, int KL, int KU,
                            const void *ab, int ldab, long long ab_stride,
-                           void *fac, int *ipiv, int *info, int nb,
+                           void *fac, int *ipiv, int *info, int nb, int nw,
                            unsigned long long *cycles_dev, void *stream);
+
+/** Process-wide shape table of the blocked factor, keyed (prec, N, KL, KU):
+ *  set records (nb, nw) for every later factorization of that geometry (the
+ *  plan and the refinement driver included); get reports the shape in force.
+ *  The tuner (suzerain_gb300.tune) times the candidates and calls set. */
+int sgb_gbtrf_set_shape(char prec, int N, int KL, int KU, int nb, int nw);
+int sgb_gbtrf_get_shape(char prec, int N, int KL, int KU, int *nb, int *nw);
 
 /** Batched solve op(A) x = b with row-panel factors; b, x complex128
  *  (nsys x N, stride N).  x may equal b. */

@@ -106,9 +106,11 @@ _SIGS = {
     "sgb_gbtrf_batched": (_i, [C.c_char, _i, _i, _i, _i, _p, _i, _ll, _p, _p,
                                _p, _p]),
     "sgb_gbtrf_batched_ex": (_i, [C.c_char, _i, _i, _i, _i, _p, _i, _ll, _p,
-                                  _p, _p, _i, _i, _p]),
+                                  _p, _p, _i, _i, _i, _p]),
     "sgb_gbtrf_phase_cycles": (_i, [C.c_char, _i, _i, _i, _i, _p, _i, _ll, _p,
-                                    _p, _p, _i, _p, _p]),
+                                    _p, _p, _i, _i, _p, _p]),
+    "sgb_gbtrf_set_shape": (_i, [C.c_char, _i, _i, _i, _i, _i]),
+    "sgb_gbtrf_get_shape": (_i, [C.c_char, _i, _i, _i, _p, _p]),
     "sgb_gbtrs_batched": (_i, [C.c_char, C.c_char, _i, _i, _i, _i, _p, _p, _p,
                                _p, _p]),
     "sgb_factor_to_lapack": (_i, [C.c_char, _i, _i, _i, _i, _p, _p, _p]),

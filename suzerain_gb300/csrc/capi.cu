@@ -79,19 +79,23 @@ extern "C" int sgb_gbtrf_batched(char prec, int nsys, int N, int KL, int KU, con
 
 extern "C" int sgb_gbtrf_batched_ex(char prec, int nsys, int N, int KL, int KU, const void *ab,
                                     int ldab, long long ab_stride, void *fac, int *ipiv,
-                                    int *info, int variant, int nb, void *stream)
+                                    int *info, int variant, int nb, int nw, void *stream)
 {
     if (prec != 'Z' && prec != 'C') return fail("sgb_gbtrf_batched_ex: prec must be 'Z' or 'C'");
     if (!geom_ok(N, KL, KU) || ldab < KL + KU + 1 || nsys < 0)
         return fail("sgb_gbtrf_batched_ex: bad geometry");
     if (variant != 0 && variant != 1) return fail("sgb_gbtrf_batched_ex: variant must be 0 or 1");
-    if (variant == 0 && !gbtrf_blk_supported({N, KL, KU}, nb))
-        return fail("sgb_gbtrf_batched_ex: blocked kernel needs nb in {4,8,16} and KL <= 52");
+    if (variant == 0) {
+        gbtrf_blk_choice(prec, {N, KL, KU}, nb, nw);
+        if (!gbtrf_blk_supported({N, KL, KU}, nb, nw))
+            return fail("sgb_gbtrf_batched_ex: blocked kernel needs nb in {4,8,16}, nw in {1,2,4}, "
+                        "KL <= 52/56/64 for nw 1/2/4 and N < 65536");
+    }
     GbtrfArgs a;
     a.prec = prec; a.g = {N, KL, KU}; a.nsys = nsys;
     a.src = {reinterpret_cast<const double2 *>(ab), ab_stride, ldab, 0};
     a.fac = fac; a.fac_stride = a.g.fac_elems(); a.ipiv = ipiv; a.info = info;
-    a.variant = variant; a.nb = nb;
+    a.variant = variant; a.nb = nb; a.nw = nw;
     count_launch(1);
     SGB_CUDA_TRY(launch_gbtrf(a, (cudaStream_t) stream));
     return 0;
@@ -99,19 +103,38 @@ extern "C" int sgb_gbtrf_batched_ex(char prec, int nsys, int N, int KL, int KU, 
 
 extern "C" int sgb_gbtrf_phase_cycles(char prec, int nsys, int N, int KL, int KU, const void *ab,
                                       int ldab, long long ab_stride, void *fac, int *ipiv,
-                                      int *info, int nb, unsigned long long *cycles_dev,
+                                      int *info, int nb, int nw, unsigned long long *cycles_dev,
                                       void *stream)
 {
     if (prec != 'Z' && prec != 'C') return fail("sgb_gbtrf_phase_cycles: prec must be 'Z' or 'C'");
-    if (!geom_ok(N, KL, KU) || ldab < KL + KU + 1 || !gbtrf_blk_supported({N, KL, KU}, nb))
+    gbtrf_blk_choice(prec, {N, KL, KU}, nb, nw);
+    if (!geom_ok(N, KL, KU) || ldab < KL + KU + 1 || !gbtrf_blk_supported({N, KL, KU}, nb, nw))
         return fail("sgb_gbtrf_phase_cycles: bad geometry");
     GbtrfArgs a;
     a.prec = prec; a.g = {N, KL, KU}; a.nsys = nsys;
     a.src = {reinterpret_cast<const double2 *>(ab), ab_stride, ldab, 0};
     a.fac = fac; a.fac_stride = a.g.fac_elems(); a.ipiv = ipiv; a.info = info;
-    a.nb = nb; a.prof = cycles_dev;
+    a.nb = nb; a.nw = nw; a.prof = cycles_dev;
     count_launch(1);
     SGB_CUDA_TRY(launch_gbtrf(a, (cudaStream_t) stream));
+    return 0;
+}
+
+extern "C" int sgb_gbtrf_set_shape(char prec, int N, int KL, int KU, int nb, int nw)
+{
+    if (prec != 'Z' && prec != 'C') return fail("sgb_gbtrf_set_shape: prec must be 'Z' or 'C'");
+    if (!geom_ok(N, KL, KU) || !gbtrf_blk_supported({N, KL, KU}, nb, nw))
+        return fail("sgb_gbtrf_set_shape: unsupported (N, KL, KU, nb, nw)");
+    gbtrf_blk_set_choice(prec, {N, KL, KU}, nb, nw);
+    return 0;
+}
+
+extern "C" int sgb_gbtrf_get_shape(char prec, int N, int KL, int KU, int *nb, int *nw)
+{
+    int b = 0, w = 0;
+    gbtrf_blk_choice(prec, {N, KL, KU}, b, w);
+    if (nb) *nb = b;
+    if (nw) *nw = w;
     return 0;
 }
 
@@ -275,6 +298,7 @@ struct sgb_plan {
     int nsys = 0, N = 0, KL = 0, KU = 0, nslot64 = 1;
     double *kx = nullptr, *kz = nullptr, *gram = nullptr;
     double *bands = nullptr, *coefs = nullptr;
+    float4 *bandf = nullptr;  // (float) M, D1, D2 per band slot
     double2 *b = nullptr, *x = nullptr, *u_stage = nullptr;
     double phi_imp_last = 0;
     // complex128 path
@@ -300,7 +324,7 @@ struct sgb_plan {
     ModelSource ms(double phi) const
     {
         ModelSource m;
-        m.cs = dc; m.kx = kx; m.kz = kz; m.case_of = nullptr; m.phi = phi;
+        m.cs = dc; m.kx = kx; m.kz = kz; m.case_of = nullptr; m.phi = phi; m.mdf = bandf;
         return m;
     }
 };
@@ -344,6 +368,7 @@ extern "C" sgb_plan *sgb_plan_create(const sgb_case *hcase, int nsys, const doub
     const size_t nb = (size_t) c.ld * c.n, SS = (size_t) c.S * c.S;
     int rc = 0;
     rc |= p->dalloc((void **) &p->bands, 3 * nb * sizeof(double), "cudaMalloc(bands)");
+    rc |= p->dalloc((void **) &p->bandf, nb * sizeof(float4), "cudaMalloc(bandf)");
     rc |= p->dalloc((void **) &p->coefs, 4 * SS * sizeof(double), "cudaMalloc(coefs)");
     rc |= p->dalloc((void **) &p->kx, nsys * sizeof(double), "cudaMalloc(kx)");
     rc |= p->dalloc((void **) &p->kz, nsys * sizeof(double), "cudaMalloc(kz)");
@@ -358,6 +383,12 @@ extern "C" sgb_plan *sgb_plan_create(const sgb_case *hcase, int nsys, const doub
     e = cudaMemcpy(p->bands, c.M, nb * sizeof(double), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(p->bands + nb, c.D1, nb * sizeof(double), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(p->bands + 2 * nb, c.D2, nb * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        std::vector<float4> bf(nb);
+        for (size_t k = 0; k < nb; ++k)
+            bf[k] = make_float4((float) c.M[k], (float) c.D1[k], (float) c.D2[k], 0.0f);
+        e = cudaMemcpy(p->bandf, bf.data(), nb * sizeof(float4), cudaMemcpyHostToDevice);
+    }
     if (e == cudaSuccess) e = cudaMemcpy(p->coefs, c.a, SS * sizeof(double), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(p->coefs + SS, c.b, SS * sizeof(double), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(p->coefs + 2 * SS, c.c, SS * sizeof(double), cudaMemcpyHostToDevice);

@@ -227,7 +227,13 @@ static cudaError_t launch_one(const GbtrfArgs &a, cudaStream_t st)
 
 cudaError_t launch_gbtrf(const GbtrfArgs &a, cudaStream_t st)
 {
-    if (a.variant == 0 && gbtrf_blk_supported(a.g, a.nb)) return launch_gbtrf_blk(a, a.nb, st);
+    if (a.variant == 0) {
+        // complex64 assembly of the model reads the float band copies
+        if (a.model && a.prec == 'C' && !a.ms.mdf) return cudaErrorInvalidValue;
+        int nb = a.nb, nw = a.nw;
+        gbtrf_blk_choice(a.prec, a.g, nb, nw);
+        if (gbtrf_blk_supported(a.g, nb, nw)) return launch_gbtrf_blk(a, nb, nw, st);
+    }
     const bool fwd = a.rhs != nullptr;
     if (a.prec == 'Z') {
         if (a.model) return fwd ? launch_one<double, true, true>(a, st) : launch_one<double, true, false>(a, st);

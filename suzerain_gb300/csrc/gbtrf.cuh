@@ -55,6 +55,8 @@ struct ModelSource {
     const double *kx, *kz;   // per system wavenumbers
     const int *case_of;      // per system case index (unused: one case)
     double phi;
+    // (float) M, (float) D1, (float) D2 per band slot, for complex64 assembly
+    const float4 *mdf = nullptr;
 };
 
 template <typename R>

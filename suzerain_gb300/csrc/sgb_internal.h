@@ -25,13 +25,17 @@ struct GbtrfArgs {
     const int *d_count = nullptr;    // optional device count bounding the list
     bool slot_mode = false;          // factor/ipiv/info indexed by list position
     int variant = 0;                 // 0 blocked (default), 1 unblocked reference kernel
-    int nb = 8;                      // panel width of the blocked kernel (4, 8, 16)
+    int nb = 0;                      // panel width of the blocked kernel (4, 8, 16; 0 = default)
+    int nw = 0;                      // warps per system of the blocked kernel (1, 2, 4; 0 = default)
     unsigned long long *prof = nullptr;  // optional per-phase cycle counters (6)
 };
 cudaError_t launch_gbtrf(const GbtrfArgs &a, cudaStream_t st);
-cudaError_t launch_gbtrf_blk(const GbtrfArgs &a, int nb, cudaStream_t st);
-bool gbtrf_blk_supported(const FactorGeom &g, int nb);
-size_t gbtrf_blk_smem_bytes(int prec_bytes, const FactorGeom &g, int S, int nb);
+cudaError_t launch_gbtrf_blk(const GbtrfArgs &a, int nb, int nw, cudaStream_t st);
+bool gbtrf_blk_supported(const FactorGeom &g, int nb, int nw);
+// Fills nb / nw left at 0 from the tuned table, else the built-in default.
+void gbtrf_blk_choice(char prec, const FactorGeom &g, int &nb, int &nw);
+void gbtrf_blk_set_choice(char prec, const FactorGeom &g, int nb, int nw);
+size_t gbtrf_blk_smem_bytes(int prec_bytes, const FactorGeom &g, int S, int nb, int nw);
 size_t gbtrf_smem_bytes(int prec_bytes, const FactorGeom &g, int S);
 
 // Triangular solves with the row-panel factor.

@@ -98,21 +98,21 @@ def test_blocked_factor_equals_unblocked(lib, torch_cuda, n, kl, ku, prec):
     fe = lib.sgb_factor_elems(n, kl, ku)
     dt = torch.complex128 if prec == "Z" else torch.complex64
     outs = []
-    for variant, nb in ((1, 8), (0, 4), (0, 8), (0, 16)):
-        if variant == 0 and kl > 52:
-            continue
+    shapes = [(1, 8, 1)] + [(0, nb, nw) for nb in (4, 8, 16) for nw in (1, 2, 4)
+                            if kl <= {1: 52, 2: 56, 4: 64}[nw]]
+    for variant, nb, nw in shapes:
         fac = torch.full((nsys * fe,), float("nan"), dtype=dt, device="cuda")
         ipiv = torch.zeros(nsys * n, dtype=torch.int32, device="cuda")
         info = torch.zeros(nsys, dtype=torch.int32, device="cuda")
         assert lib.sgb_gbtrf_batched_ex(prec.encode(), nsys, n, kl, ku, ab.data_ptr(), ld, ld * n,
                                         fac.data_ptr(), ipiv.data_ptr(), info.data_ptr(), variant,
-                                        nb, 0) == 0, lib.sgb_last_error().decode()
+                                        nb, nw, 0) == 0, lib.sgb_last_error().decode()
         torch.cuda.synchronize()
         outs.append((fac.cpu().numpy(), ipiv.cpu().numpy(), info.cpu().numpy()))
-    for fac, ipiv, info in outs[1:]:
-        assert np.array_equal(ipiv, outs[0][1]) and np.array_equal(info, outs[0][2])
-        assert np.array_equal(fac.view(np.float32 if prec == "C" else np.float64),
-                              outs[0][0].view(np.float32 if prec == "C" else np.float64))
+    fv = np.float32 if prec == "C" else np.float64
+    for (variant, nb, nw), (fac, ipiv, info) in zip(shapes[1:], outs[1:]):
+        assert np.array_equal(ipiv, outs[0][1]) and np.array_equal(info, outs[0][2]), (nb, nw)
+        assert np.array_equal(fac.view(fv), outs[0][0].view(fv)), (nb, nw)
 
 
 @pytest.mark.parametrize("n,kl,ku", [(40, 3, 5), (240, 34, 34), (97, 48, 48)])
@@ -360,6 +360,42 @@ def test_plan_result_independent_of_batch(lib, torch_cuda):
         part.substep(method, 0.0, -c.phi, dev(torch, u[sub_idx]), b, P.RefineSpec(tolsc=145.0))
         torch.cuda.synchronize()
         assert np.array_equal(a.cpu().numpy()[sub_idx], b.cpu().numpy())
+
+
+def test_plan_result_independent_of_factor_shape(lib, torch_cuda):
+    """The plan assembles its bands inside the factor kernel; every blocked
+    shape (panel width, warps per system) and the unblocked kernel give the
+    same bits, in complex128 and through the complex64 refinement."""
+    torch = torch_cuda
+    from suzerain_gb300 import plan as P
+    c, cs, kx, kz, u = config0()
+    sel = np.arange(0, len(kx), 7)
+    kx, kz, u = kx[sel], kz[sel], u[sel]
+    N, KL, KU = cs.N, cs.KL, cs.KU
+    saved = {}
+    for prec in (b"Z", b"C"):
+        nb, nw = C.c_int(), C.c_int()
+        lib.sgb_gbtrf_get_shape(prec, N, KL, KU, C.byref(nb), C.byref(nw))
+        saved[prec] = (nb.value, nw.value)
+    results = []
+    try:
+        for nb, nw in [(4, 1), (8, 2), (16, 4), (8, 1), (4, 4), (16, 2)]:
+            for prec in (b"Z", b"C"):
+                assert lib.sgb_gbtrf_set_shape(prec, N, KL, KU, nb, nw) == 0
+            pl = P.Plan(cs, kx, kz)
+            row = []
+            for method in ("Z", "M"):
+                a = torch.zeros(u.shape, dtype=torch.complex128, device="cuda")
+                pl.substep(method, 0.0, -c.phi, dev(torch, u), a, P.RefineSpec(tolsc=145.0))
+                torch.cuda.synchronize()
+                row.append(a.cpu().numpy())
+            results.append(row)
+    finally:
+        for prec, (nb, nw) in saved.items():
+            lib.sgb_gbtrf_set_shape(prec, N, KL, KU, nb, nw)
+    for row in results[1:]:
+        for m in range(2):
+            assert np.array_equal(row[m], results[0][m])
 
 
 def test_plan_host_entry_matches_device_entry(lib, torch_cuda):
