@@ -277,6 +277,14 @@ int sgb_gbtrs_batched(char prec, char trans, int nsys, int N, int KL, int KU,
                       const void *fac, const int *ipiv, const void *b,
                       void *x, void *stream);
 
+/** sgb_gbtrs_batched with caller scratch: ywork (nsys x N complex of prec,
+ *  device memory) lets trans 'N' run the four-lanes-per-system sweeps (eight
+ *  systems per warp).  Same result up to the summation order of the row dot
+ *  products; other trans values ignore ywork. */
+int sgb_gbtrs_batched_ws(char prec, char trans, int nsys, int N, int KL, int KU,
+                         const void *fac, const int *ipiv, const void *b,
+                         void *x, void *ywork, void *stream);
+
 /** Row-panel factor -> LAPACK gbtrf storage ((2KL+KU+1) x N per system). */
 int sgb_factor_to_lapack(char prec, int nsys, int N, int KL, int KU,
                          const void *fac, void *ab, void *stream);

@@ -155,6 +155,24 @@ extern "C" int sgb_gbtrs_batched(char prec, char trans, int nsys, int N, int KL,
     return 0;
 }
 
+extern "C" int sgb_gbtrs_batched_ws(char prec, char trans, int nsys, int N, int KL, int KU,
+                                    const void *fac, const int *ipiv, const void *b, void *x,
+                                    void *ywork, void *stream)
+{
+    trans = (char) toupper(trans);
+    if (prec != 'Z' && prec != 'C') return fail("sgb_gbtrs_batched_ws: prec must be 'Z' or 'C'");
+    if (trans != 'N' && trans != 'T' && trans != 'C') return fail("sgb_gbtrs_batched_ws: bad trans");
+    if (!geom_ok(N, KL, KU) || nsys < 0) return fail("sgb_gbtrs_batched_ws: bad geometry");
+    GbtrsArgs a;
+    a.prec = prec; a.trans = trans; a.g = {N, KL, KU}; a.nsys = nsys; a.fac = fac;
+    a.fac_stride = a.g.fac_elems(); a.ipiv = ipiv;
+    a.b = reinterpret_cast<const double2 *>(b); a.b_stride = N;
+    a.x = reinterpret_cast<double2 *>(x); a.x_stride = N;
+    a.ywork = ywork;
+    SGB_CUDA_TRY(launch_gbtrs(a, (cudaStream_t) stream));
+    return 0;
+}
+
 template <typename T2>
 __global__ void k_factor_to_lapack(int nsys, FactorGeom g, const T2 *__restrict__ fac,
                                    T2 *__restrict__ ab)
@@ -457,6 +475,7 @@ static int plan_substep(sgb_plan *p, char method, double phi_exp, double phi_imp
         GbtrsArgs sa;
         sa.prec = 'Z'; sa.trans = 'N'; sa.g = g; sa.nsys = nsys; sa.fac = p->fac64;
         sa.fac_stride = g.fac_elems(); sa.ipiv = p->ipiv64; sa.fwd_done = true; sa.yin = p->y64;
+        sa.ywork = p->y64;
         sa.b_stride = N; sa.x = p->x; sa.x_stride = N;
         tm.begin("backsolve_c128", st);
         count_launch(1);

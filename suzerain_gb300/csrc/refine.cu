@@ -378,6 +378,7 @@ int refine_batched(const RefineProblem &P, void *workspace, size_t workspace_byt
         sa.fac_stride = P.g.fac_elems(); sa.ipiv = ipiv32; sa.x = P.x; sa.x_stride = P.x_stride;
         sa.fwd_done = fuse;
         if (fuse) { sa.yin = y32; sa.b_stride = N; } else { sa.b = P.b; sa.b_stride = P.b_stride; }
+        sa.ywork = y32;
         sa.accumulate = false; sa.sys_list = listS; sa.nlist = nsys; sa.d_count = cnt + 0;
         sa.status = rs.status; sa.status_want = ST_SINGLE;
         tm.begin(fuse ? "backsolve_c64" : "solve_c64", st);

@@ -62,6 +62,9 @@ struct GbtrsArgs {
     int status_want = 0;
     // optional natural-order scatter of the output: x[q(i)] instead of x[i]
     int unpermute_S = 0, unpermute_n = 0;
+    // optional writable nsys x N buffer (complex of prec, row s at s*N) that
+    // enables the quad-lane solve for trans 'N'; with fwd_done it must be yin
+    void *ywork = nullptr;
 };
 cudaError_t launch_gbtrs(const GbtrsArgs &a, cudaStream_t st);
 

@@ -146,6 +146,48 @@ def test_gbtrs_batched(lib, oracle, torch_cuda, n, kl, ku, trans, prec):
         assert berr <= (1e-14 if prec == "Z" else 1e-5), berr
 
 
+@pytest.mark.parametrize("n,kl,ku", [(1, 0, 0), (7, 0, 3), (13, 12, 0), (40, 3, 5),
+                                     (240, 34, 34), (97, 48, 48), (50, 33, 40)])
+@pytest.mark.parametrize("prec", ["Z", "C"])
+def test_gbtrs_quad_path(lib, oracle, torch_cuda, n, kl, ku, prec):
+    """The four-lanes-per-system solve (enabled by caller scratch) against the
+    one-warp solve and the dense backward error, with a batch that leaves the
+    last warp's eight-system group partly empty; b and x alias."""
+    torch = torch_cuda
+    rng = np.random.default_rng(11 + n + kl)
+    nsys = 13
+    ld = kl + ku + 1
+    bands = [rand_band(rng, n, kl, ku)[0] for _ in range(nsys)]
+    b = rng.normal(size=(nsys, n)) + 1j * rng.normal(size=(nsys, n))
+    ab = dev(torch, np.stack(bands))
+    fe = lib.sgb_factor_elems(n, kl, ku)
+    fdt = torch.complex128 if prec == "Z" else torch.complex64
+    fac = torch.zeros(nsys * fe, dtype=fdt, device="cuda")
+    ipiv = torch.zeros(nsys * n, dtype=torch.int32, device="cuda")
+    info = torch.zeros(nsys, dtype=torch.int32, device="cuda")
+    assert lib.sgb_gbtrf_batched(prec.encode(), nsys, n, kl, ku, ab.data_ptr(), ld, ld * n,
+                                 fac.data_ptr(), ipiv.data_ptr(), info.data_ptr(), 0) == 0
+    x1 = dev(torch, b)
+    assert lib.sgb_gbtrs_batched(prec.encode(), b"N", nsys, n, kl, ku, fac.data_ptr(),
+                                 ipiv.data_ptr(), x1.data_ptr(), x1.data_ptr(), 0) == 0
+    x2 = dev(torch, b)
+    yw = torch.full((nsys * n,), float("nan"), dtype=fdt, device="cuda")
+    assert lib.sgb_gbtrs_batched_ws(prec.encode(), b"N", nsys, n, kl, ku, fac.data_ptr(),
+                                    ipiv.data_ptr(), x2.data_ptr(), x2.data_ptr(),
+                                    yw.data_ptr(), 0) == 0, lib.sgb_last_error().decode()
+    torch.cuda.synchronize()
+    x1, x2 = x1.cpu().numpy(), x2.cpu().numpy()
+    for s in range(nsys):
+        A = oracle.band_to_dense(bands[s], n, kl, ku, ld)
+        scale = np.abs(A).sum(1).max() * np.abs(x2[s]).max() + np.abs(b[s]).max()
+        berr = np.max(np.abs(A @ x2[s] - b[s])) / scale
+        assert berr <= (1e-14 if prec == "Z" else 1e-5), (s, berr)
+        # the same factor and the same forward sweep: only the dot products'
+        # summation order differs from the one-warp solve
+        d = np.max(np.abs(x2[s] - x1[s])) / np.abs(x1[s]).max()
+        assert d <= (1e-9 if prec == "Z" else 1e-2), (s, d)
+
+
 def test_singular_and_nan_systems(lib, oracle, torch_cuda):
     torch = torch_cuda
     n, kl, ku = 30, 2, 3
