@@ -246,8 +246,10 @@ int sgb_gbtrf_batched(char prec, int nsys, int N, int KL, int KU,
 
 /** sgb_gbtrf_batched with the kernel chosen explicitly: variant 0 is the
  *  blocked kernel with panel width nb (4, 8 or 16) and nw warps per system
- *  (1, 2 or 4; KL <= 52, 56, 64 respectively; N < 65536), variant 1 the
- *  unblocked one (nb, nw ignored).  nb or nw 0 takes the shape recorded by
+ *  (1, 2 or 4; KL <= 52, 56, 64 respectively; N < 65536), variant 2 its
+ *  lookahead form (nw 2 or 4: the next panel is factored while the other
+ *  warps apply the previous panel's update), variant 1 the unblocked kernel
+ *  (nb, nw ignored).  nb or nw 0 takes the shape recorded by
  *  sgb_gbtrf_set_shape for (prec, N, KL, KU), else the built-in default.
  *  Every shape produces zgbtf2's pivots and factor, bit for bit. */
 int sgb_gbtrf_batched_ex(char prec, int nsys, int N, int KL, int KU,
@@ -258,7 +260,8 @@ int sgb_gbtrf_batched_ex(char prec, int nsys, int N, int KL, int KU,
 /** Diagnostics: the blocked factor with cycle counters.  cycles_dev (6
  *  device uint64, accumulated) receives the clock cycles the first warp of
  *  every system spent in initial load, panel, interchanges+U12, GEMM, U
- *  output, retire/load (waits at the phase barriers included). */
+ *  output, retire/load (waits at the phase barriers included); nw < 0
+ *  selects the lookahead form with -nw warps. */
 int sgb_gbtrf_phase_cycles(char prec, int nsys, int N, int KL, int KU,
                            const void *ab, int ldab, long long ab_stride,
                            void *fac, int *ipiv, int *info, int nb, int nw,
@@ -267,7 +270,8 @@ int sgb_gbtrf_phase_cycles(char prec, int nsys, int N, int KL, int KU,
 /** Process-wide shape table of the blocked factor, keyed (prec, N, KL, KU):
  *  set records (nb, nw) for every later factorization of that geometry (the
  *  plan and the refinement driver included); get reports the shape in force.
- *  The tuner (suzerain_gb300.tune) times the candidates and calls set. */
+ *  nw = -2 or -4 records the lookahead form.  The tuner
+ *  (suzerain_gb300.tune) times the candidates and calls set. */
 int sgb_gbtrf_set_shape(char prec, int N, int KL, int KU, int nb, int nw);
 int sgb_gbtrf_get_shape(char prec, int N, int KL, int KU, int *nb, int *nw);
 

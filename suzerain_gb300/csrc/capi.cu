@@ -84,9 +84,10 @@ extern "C" int sgb_gbtrf_batched_ex(char prec, int nsys, int N, int KL, int KU, 
     if (prec != 'Z' && prec != 'C') return fail("sgb_gbtrf_batched_ex: prec must be 'Z' or 'C'");
     if (!geom_ok(N, KL, KU) || ldab < KL + KU + 1 || nsys < 0)
         return fail("sgb_gbtrf_batched_ex: bad geometry");
-    if (variant != 0 && variant != 1) return fail("sgb_gbtrf_batched_ex: variant must be 0 or 1");
-    if (variant == 0) {
+    if (variant < 0 || variant > 2) return fail("sgb_gbtrf_batched_ex: variant must be 0, 1 or 2");
+    if (variant != 1) {
         gbtrf_blk_choice(prec, {N, KL, KU}, nb, nw);
+        if (nw < 0) { variant = 2; nw = -nw; }
         if (!gbtrf_blk_supported({N, KL, KU}, nb, nw))
             return fail("sgb_gbtrf_batched_ex: blocked kernel needs nb in {4,8,16}, nw in {1,2,4}, "
                         "KL <= 52/56/64 for nw 1/2/4 and N < 65536");
@@ -108,13 +109,15 @@ extern "C" int sgb_gbtrf_phase_cycles(char prec, int nsys, int N, int KL, int KU
 {
     if (prec != 'Z' && prec != 'C') return fail("sgb_gbtrf_phase_cycles: prec must be 'Z' or 'C'");
     gbtrf_blk_choice(prec, {N, KL, KU}, nb, nw);
+    const int variant = nw < 0 ? 2 : 0;     // negative nw: the lookahead form
+    if (nw < 0) nw = -nw;
     if (!geom_ok(N, KL, KU) || ldab < KL + KU + 1 || !gbtrf_blk_supported({N, KL, KU}, nb, nw))
         return fail("sgb_gbtrf_phase_cycles: bad geometry");
     GbtrfArgs a;
     a.prec = prec; a.g = {N, KL, KU}; a.nsys = nsys;
     a.src = {reinterpret_cast<const double2 *>(ab), ab_stride, ldab, 0};
     a.fac = fac; a.fac_stride = a.g.fac_elems(); a.ipiv = ipiv; a.info = info;
-    a.nb = nb; a.nw = nw; a.prof = cycles_dev;
+    a.variant = variant; a.nb = nb; a.nw = nw; a.prof = cycles_dev;
     count_launch(1);
     SGB_CUDA_TRY(launch_gbtrf(a, (cudaStream_t) stream));
     return 0;
@@ -123,7 +126,7 @@ extern "C" int sgb_gbtrf_phase_cycles(char prec, int nsys, int N, int KL, int KU
 extern "C" int sgb_gbtrf_set_shape(char prec, int N, int KL, int KU, int nb, int nw)
 {
     if (prec != 'Z' && prec != 'C') return fail("sgb_gbtrf_set_shape: prec must be 'Z' or 'C'");
-    if (!geom_ok(N, KL, KU) || !gbtrf_blk_supported({N, KL, KU}, nb, nw))
+    if (!geom_ok(N, KL, KU) || nw == -1 || !gbtrf_blk_supported({N, KL, KU}, nb, nw < 0 ? -nw : nw))
         return fail("sgb_gbtrf_set_shape: unsupported (N, KL, KU, nb, nw)");
     gbtrf_blk_set_choice(prec, {N, KL, KU}, nb, nw);
     return 0;

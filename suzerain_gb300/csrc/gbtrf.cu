@@ -227,12 +227,14 @@ static cudaError_t launch_one(const GbtrfArgs &a, cudaStream_t st)
 
 cudaError_t launch_gbtrf(const GbtrfArgs &a, cudaStream_t st)
 {
-    if (a.variant == 0) {
+    if (a.variant == 0 || a.variant == 2) {
         // complex64 assembly of the model reads the float band copies
         if (a.model && a.prec == 'C' && !a.ms.mdf) return cudaErrorInvalidValue;
         int nb = a.nb, nw = a.nw;
         gbtrf_blk_choice(a.prec, a.g, nb, nw);
-        if (gbtrf_blk_supported(a.g, nb, nw)) return launch_gbtrf_blk(a, nb, nw, st);
+        GbtrfArgs b = a;
+        if (nw < 0) { b.variant = 2; nw = -nw; }   // the shape table's lookahead entries
+        if (gbtrf_blk_supported(a.g, nb, nw)) return launch_gbtrf_blk(b, nb, nw, st);
     }
     const bool fwd = a.rhs != nullptr;
     if (a.prec == 'Z') {

@@ -10,25 +10,34 @@
 
 namespace sgb {
 
+// nw > 0: the phased kernel with nw warps (nw > 1 stages the entering
+// rows); nw < 0: the lookahead kernel with -nw warps.
 size_t gbtrf_blk_smem_bytes(int prec_bytes, const FactorGeom &g, int S, int nb, int nw)
 {
     const size_t el = 2 * (size_t) prec_bytes;
-    const int WR = g.KL + nb, WC = g.KL + g.KU + nb, P = blk_pitch(WC);
-    const size_t stage = nw > 1 ? (size_t) nb * WC + nb : 0;
-    return ((size_t) WR * P + WR + stage + 3 * (size_t) S * S) * el
-         + (size_t) nb * sizeof(int) + 2 * sizeof(int) + 16;
+    if (nw > 0) {
+        const int WR = g.KL + nb, WC = g.KL + g.KU + nb, P = blk_pitch(WC);
+        const size_t stage = nw > 1 ? (size_t) nb * WC + nb : 0;
+        return ((size_t) WR * P + WR + stage + 3 * (size_t) S * S) * el
+             + (size_t) nb * sizeof(int) + 4 * sizeof(int) + 16;
+    }
+    // lookahead: panel J-1's rows and columns stay, plus the staged rows
+    const int WR = g.KL + 2 * nb, WC = g.KL + g.KU + 2 * nb, P = blk_pitch(WC);
+    return ((size_t) WR * P + WR + (size_t) nb * WC + nb + 3 * (size_t) S * S) * el
+         + (size_t) nb * sizeof(int) + 4 * sizeof(int) + 16;
 }
 
 // Rows of the trailing update per thread: KL <= 4 NW MAXTR (MAXTR 13, 7, 4
-// for NW 1, 2, 4); row and column indices of the model's band assembly below
-// 65536; the window within one CTA's shared memory.
+// for NW 1, 2, 4); the panel's rows per lane; row and column indices of the
+// model's band assembly below 65536; the window within one CTA's shared
+// memory (either kernel).
 bool gbtrf_blk_supported(const FactorGeom &g, int nb, int nw)
 {
     if (nb != 4 && nb != 8 && nb != 16) return false;
     if (nw != 1 && nw != 2 && nw != 4) return false;
     const int maxkl = nw == 1 ? 52 : nw == 2 ? 56 : 64;
     if (g.KL > maxkl || g.N >= 65536) return false;
-    return gbtrf_blk_smem_bytes(sizeof(double), g, 8, nb, nw) <= 227 * 1024;
+    return gbtrf_blk_smem_bytes(sizeof(double), g, 8, nb, -(nw > 1 ? nw : 2)) <= 227 * 1024;
 }
 
 namespace {

@@ -146,11 +146,242 @@ __device__ __forceinline__ int warp_argmax_rows(const cplx_t<R> (&v)[RS][NB], in
     return ip;
 }
 
+// Panel factorization of columns j0 .. j0+nbk-1 by one warp (zgbtf2 steps
+// with the deferred trailing update).  The panel lives in registers: lane l
+// holds panel rows l, l+32, .. (rows j0 + i at window slot rsl(i) for
+// i < nrows, columns j0 + c at slot csl(c)); row k of step k is row k of slot
+// 0, on lane k.  Writes the pivots, the L columns (zgbtf2's unswapped
+// storage, column k at step k), pvoff (the interchange offsets, for the
+// trailing columns), shv[0] = ju and shv[1] = info, and with FWD the forward
+// elimination of the row-slot RHS rs into y.
+template <typename R, int NB, int RS, bool FWD>
+__device__ __forceinline__ void panel_factor(cplx_t<R> *__restrict__ win, int P, int WR, int WC,
+                                             int rb, int cb, int nrows, cplx_t<R> *__restrict__ rs,
+                                             int *__restrict__ pvoff, int *__restrict__ shv,
+                                             int j0, int nbk, int N, int KL, int KU,
+                                             cplx_t<R> *__restrict__ fl, int *__restrict__ pv,
+                                             cplx_t<R> *__restrict__ ys, int lane)
+{
+    using T2 = cplx_t<R>;
+    const T2 zero = mk<R>(R(0), R(0));
+    auto rsl = [&](int i) { int t = rb + i; return t >= WR ? t - WR : t; };
+    auto csl = [&](int c) { int t = cb + c; return t >= WC ? t - WC : t; };
+    int ju = shv[0], inf = shv[1];
+    T2 v[RS][NB];
+    T2 rv[RS];
+#pragma unroll
+    for (int q = 0; q < RS; ++q) {
+        const int i = lane + 32 * q;
+        const bool ok = i < nrows;
+        const int ro = ok ? rsl(i) * P : 0;
+#pragma unroll
+        for (int c = 0; c < NB; ++c) v[q][c] = (ok && c < nbk) ? win[ro + csl(c)] : zero;
+        if (FWD) rv[q] = ok ? rs[rsl(i)] : zero;
+    }
+#pragma unroll
+    for (int k = 0; k < NB; ++k) {
+        if (k >= nbk) break;
+        const int jj = j0 + k;
+        const int km = imin(KL, N - 1 - jj);
+        // IZAMAX over rows k..k+km: the largest key, then the
+        // smallest row holding it
+        const int ip = warp_argmax_rows<R, RS>(v, k, km, lane);
+        const int bt = ip - k, lp = ip & 31, qp = ip >> 5;
+        const T2 piv = shfl_c<R>(pick<R, RS, NB>(v, qp, k), lp);
+        if (lane == 0) pv[jj] = jj + bt + 1;
+        if (cnz<R>(piv)) {
+            ju = imax(ju, imin(jj + KU + bt, N - 1));
+            if (bt != 0) {
+#pragma unroll
+                for (int c = 0; c < NB; ++c) {
+                    if (c < nbk) {
+                        const T2 a = shfl_c<R>(v[0][c], k);
+                        const T2 b = shfl_c<R>(pick<R, RS, NB>(v, qp, c), lp);
+                        if (lane == k) v[0][c] = b;
+                        if (lane == lp) put_slot<R, RS, NB>(v, qp, c, a);
+                    }
+                }
+                if (FWD) {
+                    const T2 a = shfl_c<R>(rv[0], k);
+                    T2 bq = rv[0];
+#pragma unroll
+                    for (int q = 1; q < RS; ++q) if (qp == q) bq = rv[q];
+                    const T2 b = shfl_c<R>(bq, lp);
+                    if (lane == k) rv[0] = b;
+                    if (lane == lp) {
+#pragma unroll
+                        for (int q = 0; q < RS; ++q) if (qp == q) rv[q] = a;
+                    }
+                }
+            }
+            if (lane == 0) pvoff[k] = bt;
+            const T2 rp = crcp<R>(piv);
+#pragma unroll
+            for (int q = 0; q < RS; ++q) {
+                const int i = lane + 32 * q;
+                if (i > k && i <= k + km) v[q][k] = cmul(v[q][k], rp);
+                if (i > k && i <= k + KL)
+                    fl[(long long) jj * KL + (i - k - 1)] = (i <= k + km) ? v[q][k] : zero;
+            }
+            if (FWD) {
+                const T2 yj = shfl_c<R>(rv[0], k);
+                if (lane == 0) ys[jj] = yj;
+#pragma unroll
+                for (int q = 0; q < RS; ++q) {
+                    const int i = lane + 32 * q;
+                    if (i > k && i <= k + km) rv[q] = cfnma(v[q][k], yj, rv[q]);
+                }
+            }
+            // rank-1 update of the remaining panel columns
+#pragma unroll
+            for (int c = k + 1; c < NB; ++c) {
+                if (c < nbk) {
+                    const T2 u = shfl_c<R>(v[0][c], k);
+                    if (cnz<R>(u)) {
+#pragma unroll
+                        for (int q = 0; q < RS; ++q) {
+                            const int i = lane + 32 * q;
+                            if (i > k && i <= k + km) v[q][c] = cfnma(v[q][k], u, v[q][c]);
+                        }
+                    }
+                }
+            }
+        } else {
+            if (inf == 0) inf = jj + 1;
+            if (lane == 0) pvoff[k] = 0;
+#pragma unroll
+            for (int q = 0; q < RS; ++q) {
+                const int i = lane + 32 * q;
+                if (i > k && i <= k + KL) fl[(long long) jj * KL + (i - k - 1)] = zero;
+            }
+            if (FWD) {
+                const T2 yj = shfl_c<R>(rv[0], k);
+                if (lane == 0) ys[jj] = yj;
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < RS; ++q) {
+        const int i = lane + 32 * q;
+        if (i < nrows) {
+            const int ro = rsl(i) * P;
+#pragma unroll
+            for (int c = 0; c < NB; ++c)
+                if (c < nbk) win[ro + csl(c)] = v[q][c];
+            if (FWD) rs[rsl(i)] = rv[q];
+        }
+    }
+    if (lane == 0) { shv[0] = ju; shv[1] = inf; }
+}
+
+// Rows r0 .. r0+nr-1 of A (rows outside 0..N-1 read as zero) at columns
+// cbase + cc, 0 <= cc < WC (columns outside 0..N-1 zero), handed to
+// put(k, cc, value) for every k < nr, cc < WC.  One warp, lanes over cc.  The
+// band reads of a group of rows x three column passes are all issued before
+// any value is formed, so the latency of the source (the float band copies
+// in L2 for the model, HBM for a packed band) is paid once per group instead
+// of once per entry.
+template <typename R, bool MODEL> struct BandRaw { using type = double2; };
+template <> struct BandRaw<float, true> { using type = float4; };
+template <> struct BandRaw<double, true> { using type = double3; };
+
+template <typename R, bool MODEL, typename Put>
+__device__ __forceinline__ void assemble_rows(const PackedSource &src, const ModelSource &ms,
+                                              const cplx_t<R> *coef, unsigned magic, int s, int N,
+                                              int KL, int KU, int WC, int r0, int nr, int cbase,
+                                              int lane, Put &&put)
+{
+    using T2 = cplx_t<R>;
+    using Raw = typename BandRaw<R, MODEL>::type;
+    constexpr int GR = 2;                                    // rows per group
+    constexpr int GC = 3;                                    // column passes per group
+    const int S = MODEL ? ms.cs.S : 1, SS = S * S;
+    for (int k0 = 0; k0 < nr; k0 += GR) {
+        for (int c0 = 0; c0 < WC; c0 += 32 * GC) {
+            Raw raw[GR][GC];
+            int tag[GR][GC];       // -1 zero, -2 one (wall diagonal), else coefficient index
+#pragma unroll
+            for (int kk = 0; kk < GR; ++kk) {
+                const int k = k0 + kk, r = r0 + k;
+                const bool rv = k < nr && r >= 0 && r < N;
+                int p = 0, e = 0;
+                bool dir = false;
+                if constexpr (MODEL) {
+                    if (rv) {
+                        p = div_small(r, magic);
+                        e = r - p * S;
+                        dir = ((ms.cs.dirichlet_mask >> e) & 1u) && (p == 0 || p == ms.cs.n - 1);
+                    }
+                }
+#pragma unroll
+                for (int ii = 0; ii < GC; ++ii) {
+                    const int cc = c0 + lane + 32 * ii, col = cbase + cc;
+                    int t = -1;
+                    if (rv && cc < WC && col >= 0 && col < N) {
+                        if constexpr (MODEL) {
+                            if (dir) {
+                                t = col == r ? -2 : -1;
+                            } else {
+                                const int q = div_small(col, magic), f = col - q * S, d = p - q;
+                                if (d <= ms.cs.kl && -d <= ms.cs.ku) {
+                                    const int bk = ms.cs.ku + d + q * ms.cs.ld;
+                                    t = e * S + f;
+                                    if constexpr (sizeof(R) == 8)
+                                        raw[kk][ii] = make_double3(__ldg(ms.cs.M + bk), __ldg(ms.cs.D1 + bk),
+                                                                   __ldg(ms.cs.D2 + bk));
+                                    else
+                                        raw[kk][ii] = __ldg(ms.mdf + bk);
+                                }
+                            }
+                        } else {
+                            if (col - r <= KU && r - col <= KL) {
+                                t = 0;
+                                raw[kk][ii] = src.entry(s, KU, r, col);
+                            }
+                        }
+                    }
+                    tag[kk][ii] = t;
+                }
+            }
+#pragma unroll
+            for (int kk = 0; kk < GR; ++kk) {
+#pragma unroll
+                for (int ii = 0; ii < GC; ++ii) {
+                    const int k = k0 + kk, cc = c0 + lane + 32 * ii;
+                    if (k < nr && cc < WC) {
+                        const int t = tag[kk][ii];
+                        T2 v = mk<R>(t == -2 ? R(1) : R(0), R(0));
+                        if (t >= 0) {
+                            if constexpr (MODEL) {
+                                const T2 a = coef[t], b = coef[SS + t], c = coef[2 * SS + t];
+                                if constexpr (sizeof(R) == 8) {
+                                    sgb_coef cM{a.x, a.y}, cD1{b.x, b.y}, cD2{c.x, c.y};
+                                    double re, im;
+                                    sgb_block_entry(cM, cD1, cD2, raw[kk][ii].x, raw[kk][ii].y,
+                                                    raw[kk][ii].z, &re, &im);
+                                    v = mk<R>(re, im);
+                                } else {
+                                    const float4 w = raw[kk][ii];
+                                    v = mk<R>(fmaf(c.x, w.z, fmaf(b.x, w.y, a.x * w.x)),
+                                              fmaf(c.y, w.z, fmaf(b.y, w.y, a.y * w.x)));
+                                }
+                            } else {
+                                v = from_z<R>(raw[kk][ii]);
+                            }
+                        }
+                        put(k, cc, v);
+                    }
+                }
+            }
+        }
+    }
+}
+
 // Resident CTAs per SM the register budget is cut for: the window of one
 // system (KL = KU = 34, NB = 4 or 8) leaves room for about 8 complex64 or 4
 // complex128 systems per SM.
 template <typename R, int NW>
-constexpr int blk_min_blocks() { return sizeof(R) == 8 ? (NW == 4 ? 3 : 4) : (NW == 4 ? 5 : 8); }
+constexpr int blk_min_blocks() { return sizeof(R) == 8 ? (NW == 4 ? 3 : 4) : (NW == 4 ? 4 : 8); }
 
 template <typename R, int NB, int NW, int MAXTR, bool MODEL, bool FWD>
 __global__ void __launch_bounds__(32 * NW, (blk_min_blocks<R, NW>()))
@@ -215,29 +446,12 @@ k_gbtrf_cta(FactorGeom g, int nsys, PackedSource src, ModelSource ms,
         }
         __syncthreads();
     }
-    // Row r < N of A at columns cbase + cc, cc = lane, lane + 32, ... < WC,
-    // handed to put(cc, value).
-    auto row_to = [&](int r, int cbase, auto put) {
-        if constexpr (MODEL) {
-            const int p = div_small(r, magic), e = r - p * S;
-            const bool dir = ((ms.cs.dirichlet_mask >> e) & 1u) && (p == 0 || p == ms.cs.n - 1);
-            for (int cc = lane; cc < WC; cc += 32)
-                put(cc, model_entry<R>(ms, coef, magic, p, e, dir, r, cbase + cc, N));
-        } else {
-            for (int cc = lane; cc < WC; cc += 32) {
-                const int col = cbase + cc;
-                T2 v = zero;
-                if (col < N && col - r <= KU && r - col <= KL) v = from_z<R>(src.entry(s, KU, r, col));
-                put(cc, v);
-            }
-        }
-    };
 
     // Initial window: rows 0..WR-1, columns 0..WC-1 (slots equal indices).
-    for (int r = warp; r < WR; r += NW) {
-        T2 *dst = win + r * P;
-        if (r < N) row_to(r, 0, [&](int cc, T2 v) { dst[cc] = v; });
-        else for (int cc = lane; cc < WC; cc += 32) dst[cc] = zero;
+    {
+        const int rb0 = WR * warp / NW, re0 = WR * (warp + 1) / NW;
+        assemble_rows<R, MODEL>(src, ms, coef, magic, s, N, KL, KU, WC, rb0, re0 - rb0, 0, lane,
+                                [&](int k, int cc, T2 v) { win[(rb0 + k) * P + cc] = v; });
     }
     if (FWD)
         for (int r = tid; r < WR; r += NT)
@@ -257,121 +471,15 @@ k_gbtrf_cta(FactorGeom g, int nsys, PackedSource src, ModelSource ms,
         // The panel lives in registers: lane l holds rows l, l+32, .. of the
         // nbk panel columns (row k of step k is row k of slot 0, on lane k).
         if (warp == 0) {
-            int ju = shv[0], inf = shv[1];
-            T2 v[RS][NB];
-            T2 rv[RS];
-#pragma unroll
-            for (int q = 0; q < RS; ++q) {
-                const int i = lane + 32 * q;
-                const bool ok = i < WR;
-                const int ro = ok ? rsl(i) * P : 0;
-#pragma unroll
-                for (int c = 0; c < NB; ++c) v[q][c] = (ok && c < nbk) ? win[ro + csl(c)] : zero;
-                if (FWD) rv[q] = ok ? rs[rsl(i)] : zero;
-            }
-#pragma unroll
-            for (int k = 0; k < NB; ++k) {
-                if (k >= nbk) break;
-                const int jj = j0 + k;
-                const int km = imin(KL, N - 1 - jj);
-                // IZAMAX over rows k..k+km: the largest key, then the
-                // smallest row holding it
-                const int ip = warp_argmax_rows<R, RS>(v, k, km, lane);
-                const int bt = ip - k, lp = ip & 31, qp = ip >> 5;
-                const T2 piv = shfl_c<R>(pick<R, RS, NB>(v, qp, k), lp);
-                if (lane == 0) pv[jj] = jj + bt + 1;
-                if (cnz<R>(piv)) {
-                    ju = imax(ju, imin(jj + KU + bt, N - 1));
-                    if (bt != 0) {
-#pragma unroll
-                        for (int c = 0; c < NB; ++c) {
-                            if (c < nbk) {
-                                const T2 a = shfl_c<R>(v[0][c], k);
-                                const T2 b = shfl_c<R>(pick<R, RS, NB>(v, qp, c), lp);
-                                if (lane == k) v[0][c] = b;
-                                if (lane == lp) put_slot<R, RS, NB>(v, qp, c, a);
-                            }
-                        }
-                        if (FWD) {
-                            const T2 a = shfl_c<R>(rv[0], k);
-                            T2 bq = rv[0];
-#pragma unroll
-                            for (int q = 1; q < RS; ++q) if (qp == q) bq = rv[q];
-                            const T2 b = shfl_c<R>(bq, lp);
-                            if (lane == k) rv[0] = b;
-                            if (lane == lp) {
-#pragma unroll
-                                for (int q = 0; q < RS; ++q) if (qp == q) rv[q] = a;
-                            }
-                        }
-                    }
-                    if (lane == 0) pvoff[k] = bt;
-                    const T2 rp = crcp<R>(piv);
-#pragma unroll
-                    for (int q = 0; q < RS; ++q) {
-                        const int i = lane + 32 * q;
-                        if (i > k && i <= k + km) v[q][k] = cmul(v[q][k], rp);
-                        if (i > k && i <= k + KL)
-                            fl[(long long) jj * KL + (i - k - 1)] = (i <= k + km) ? v[q][k] : zero;
-                    }
-                    if (FWD) {
-                        const T2 yj = shfl_c<R>(rv[0], k);
-                        if (lane == 0) y[s * y_stride + jj] = yj;
-#pragma unroll
-                        for (int q = 0; q < RS; ++q) {
-                            const int i = lane + 32 * q;
-                            if (i > k && i <= k + km) rv[q] = cfnma(v[q][k], yj, rv[q]);
-                        }
-                    }
-                    // rank-1 update of the remaining panel columns
-#pragma unroll
-                    for (int c = k + 1; c < NB; ++c) {
-                        if (c < nbk) {
-                            const T2 u = shfl_c<R>(v[0][c], k);
-                            if (cnz<R>(u)) {
-#pragma unroll
-                                for (int q = 0; q < RS; ++q) {
-                                    const int i = lane + 32 * q;
-                                    if (i > k && i <= k + km) v[q][c] = cfnma(v[q][k], u, v[q][c]);
-                                }
-                            }
-                        }
-                    }
-                } else {
-                    if (inf == 0) inf = jj + 1;
-                    if (lane == 0) pvoff[k] = 0;
-#pragma unroll
-                    for (int q = 0; q < RS; ++q) {
-                        const int i = lane + 32 * q;
-                        if (i > k && i <= k + KL) fl[(long long) jj * KL + (i - k - 1)] = zero;
-                    }
-                    if (FWD) {
-                        const T2 yj = shfl_c<R>(rv[0], k);
-                        if (lane == 0) y[s * y_stride + jj] = yj;
-                    }
-                }
-            }
-#pragma unroll
-            for (int q = 0; q < RS; ++q) {
-                const int i = lane + 32 * q;
-                if (i < WR) {
-                    const int ro = rsl(i) * P;
-#pragma unroll
-                    for (int c = 0; c < NB; ++c)
-                        if (c < nbk) win[ro + csl(c)] = v[q][c];
-                    if (FWD) rs[rsl(i)] = rv[q];
-                }
-            }
-            if (lane == 0) { shv[0] = ju; shv[1] = inf; }
+            panel_factor<R, NB, RS, FWD>(win, P, WR, WC, rb, cb, WR, rs, pvoff, shv, j0, nbk, N, KL,
+                                         KU, fl, pv, FWD ? y + s * y_stride : nullptr, lane);
         } else if constexpr (STAGE) {
             // the next nbk rows of A, at the next window's columns
             if (more) {
-                for (int k = warp - 1; k < nbk; k += NW - 1) {
-                    const int r = j0 + WR + k;
-                    T2 *dst = stg + k * WC;
-                    if (r < N) row_to(r, j0 + nbk, [&](int cc, T2 v) { dst[cc] = v; });
-                    else for (int cc = lane; cc < WC; cc += 32) dst[cc] = zero;
-                }
+                const int kb = nbk * (warp - 1) / (NW - 1), ke = nbk * warp / (NW - 1);
+                assemble_rows<R, MODEL>(src, ms, coef, magic, s, N, KL, KU, WC, j0 + WR + kb, ke - kb,
+                                        j0 + nbk, lane,
+                                        [&](int k, int cc, T2 v) { stg[(kb + k) * WC + cc] = v; });
                 if (FWD)
                     for (int k = tid - 32; k < nbk; k += NT - 32) {
                         const int r = j0 + WR + k;
@@ -475,21 +583,20 @@ k_gbtrf_cta(FactorGeom g, int nsys, PackedSource src, ModelSource ms,
                 if (i >= nbk && c < nbk) win[rsl(i) * P + csl(c)] = zero;
             }
             // retired row slots take rows j0+WR.. at columns j0+nbk ..
-            for (int k = warp; k < nbk; k += NW) {
-                T2 *dst = win + rsl(k) * P;
-                auto put = [&](int cc, T2 v) {
-                    int cs = cb + nbk + cc;          // < 3 WC: wrap at most twice
-                    if (cs >= WC) cs -= WC;
-                    if (cs >= WC) cs -= WC;
-                    dst[cs] = v;
-                };
-                if constexpr (STAGE) {
-                    for (int cc = lane; cc < WC; cc += 32) put(cc, stg[k * WC + cc]);
-                } else {
-                    const int r = j0 + WR + k;
-                    if (r < N) row_to(r, j0 + nbk, put);
-                    else for (int cc = lane; cc < WC; cc += 32) put(cc, zero);
-                }
+            auto put = [&](int k, int cc, T2 v) {
+                int cs = cb + nbk + cc;          // < 3 WC: wrap at most twice
+                if (cs >= WC) cs -= WC;
+                if (cs >= WC) cs -= WC;
+                win[rsl(k) * P + cs] = v;
+            };
+            if constexpr (STAGE) {
+                for (int k = warp; k < nbk; k += NW)
+                    for (int cc = lane; cc < WC; cc += 32) put(k, cc, stg[k * WC + cc]);
+            } else {
+                const int kb = nbk * warp / NW, ke = nbk * (warp + 1) / NW;
+                assemble_rows<R, MODEL>(src, ms, coef, magic, s, N, KL, KU, WC, j0 + WR + kb, ke - kb,
+                                        j0 + nbk, lane,
+                                        [&](int k, int cc, T2 v) { put(kb + k, cc, v); });
             }
             if (FWD)
                 for (int k = tid; k < nbk; k += NT) {
@@ -510,12 +617,283 @@ k_gbtrf_cta(FactorGeom g, int nsys, PackedSource src, ModelSource ms,
         for (int ph = 0; ph < 6; ++ph) atomicAdd(prof + ph, tph[ph]);
 }
 
-template <typename R, int NB, int NW, int MAXTR, bool MODEL, bool FWD>
+// Lookahead form (NW >= 2): warp 0 factors panel J while warps 1..NW-1 apply
+// panel J-1's deferred update to the columns beyond panel J, write panel
+// J-1's U rows and assemble the rows that enter after panel J; the panel's
+// sequential latency is hidden behind the trailing update.  Panel J-1's rows
+// and columns therefore stay one panel longer: the window spans rows
+// j0-NB .. j0+KL+NB-1 and columns j0-NB .. j0+KL+KU+NB-1 (logical row lr is
+// row j0-NB+lr, logical column lc is column j0-NB+lc).  Per panel J:
+//   A. warp 0: panel J;  workers: A(j0.., j0+NB..ju_{J-1}) -= L21_{J-1}
+//      U12_{J-1}, U rows of panel J-1 out, rows j0+KL+NB.. staged;
+//   B. all: panel J's interchanges and U12 on its trailing columns;
+//   C. all: panel J+1's columns -= L21_J U12_J, panel J-1's columns retire
+//      (zeroed), its row slots take the staged rows.
+// Each element still receives the multiply-adds of zgbtf2 in zgbtf2's order:
+// panel J-1's update of a column always precedes panel J's.
+template <typename R, int NB, int NW, bool MODEL, bool FWD>
+__global__ void __launch_bounds__(32 * NW, (blk_min_blocks<R, NW>()))
+k_gbtrf_la(FactorGeom g, int nsys, PackedSource src, ModelSource ms,
+           cplx_t<R> *__restrict__ fac, long long fac_stride,
+           int *__restrict__ ipiv, int *__restrict__ info,
+           const double2 *__restrict__ rhs, long long rhs_stride,
+           cplx_t<R> *__restrict__ y, long long y_stride,
+           const int *__restrict__ sys_list, const int *__restrict__ d_count,
+           bool slot_mode, unsigned long long *__restrict__ prof)
+{
+    static_assert(NW >= 2, "the lookahead form needs worker warps");
+    using T2 = cplx_t<R>;
+    constexpr int NT = 32 * NW, NWK = NW - 1, NTK = 32 * NWK;
+    constexpr int TC = sizeof(R) == 8 ? 3 : 5;      // worker GEMM columns per thread per pass
+    constexpr int MT = 3;                             // worker GEMM rows per thread per pass
+    constexpr int RGW = NTK / 8;                      // worker GEMM row groups
+    constexpr int RS = 3;                             // panel rows per lane: KL + NB <= 96
+    constexpr int LNB = NB == 4 ? 2 : NB == 8 ? 3 : 4;
+    static_assert((1 << LNB) == NB, "NB must be 4, 8 or 16");
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (d_count && (int) blockIdx.x >= *d_count) return;
+    const int s = sys_list ? sys_list[blockIdx.x] : (int) blockIdx.x;
+    if (s < 0 || s >= nsys) return;
+    const long long fi = slot_mode ? (long long) blockIdx.x : (long long) s;
+
+    const int N = g.N, KL = g.KL, KU = g.KU, UW = g.UW();
+    const int WR = KL + 2 * NB, WC = KL + KU + 2 * NB, P = blk_pitch(WC);
+    const int S = MODEL ? ms.cs.S : 1;
+    const unsigned magic = (MODEL && S > 1) ? (unsigned) ((0x100000000ull + S - 1) / S) : 0u;
+
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T2 *win = reinterpret_cast<T2 *>(smem_raw);       // WR x WC, row pitch P
+    T2 *rs = win + WR * P;                            // RHS per row slot
+    T2 *stg = rs + WR;                                // NB x WC staged rows
+    T2 *stgr = stg + NB * WC;                         // NB staged RHS entries
+    T2 *coef = stgr + NB;                             // 3 S^2 (model)
+    int *pvoff = reinterpret_cast<int *>(coef + (MODEL ? 3 * S * S : 0));   // NB
+    int *shv = pvoff + NB;                            // [0] ju, [1] info, [2] ju of panel J-1
+
+    T2 *fu = fac + fi * fac_stride;
+    T2 *fl = fu + (long long) N * UW;
+    int *pv = ipiv + fi * N;
+    const T2 zero = mk<R>(R(0), R(0));
+
+    // Optional per-phase cycle counters (diagnostics), read on thread 0:
+    // 0 init, 1 phase A, 2 phase B, 3 phase C, 4 last U rows.
+    unsigned long long tph[6] = {0, 0, 0, 0, 0, 0};
+    long long tmark = prof ? clock64() : 0;
+    auto tick = [&](int ph) {
+        if (prof) { const long long t = clock64(); tph[ph] += (unsigned long long) (t - tmark); tmark = t; }
+    };
+
+    if (MODEL) {
+        const double kx = ms.kx[s], kz = ms.kz[s];
+        for (int idx = tid; idx < S * S; idx += NT) {
+            sgb_coef cM, cD1, cD2;
+            sgb_block_coefs(&ms.cs, idx / S, idx % S, ms.phi, kx, kz, &cM, &cD1, &cD2);
+            coef[idx] = mk<R>((R) cM.re, (R) cM.im);
+            coef[S * S + idx] = mk<R>((R) cD1.re, (R) cD1.im);
+            coef[2 * S * S + idx] = mk<R>((R) cD2.re, (R) cD2.im);
+        }
+        __syncthreads();
+    }
+
+    // Initial window (rb = cb = 0): slot lr holds row lr-NB, slot lc column
+    // lc-NB; rows and columns before 0 are zero.
+    {
+        const int lb = WR * warp / NW, le = WR * (warp + 1) / NW;
+        assemble_rows<R, MODEL>(src, ms, coef, magic, s, N, KL, KU, WC, lb - NB, le - lb, -NB, lane,
+                                [&](int k, int cc, T2 v) { win[(lb + k) * P + cc] = v; });
+    }
+    if (FWD)
+        for (int lr = tid; lr < WR; lr += NT) {
+            const int r = lr - NB;
+            rs[lr] = (r >= 0 && r < N) ? from_z<R>(rhs[s * rhs_stride + r]) : zero;
+        }
+    if (tid == 0) { shv[0] = 0; shv[1] = 0; shv[2] = 0; }
+    __syncthreads();
+    tick(0);
+
+    int rb = 0, cb = 0, nbp = 0;      // nbp: columns of panel J-1 (0 before the first)
+    int j0 = 0;
+    for (; j0 < N; j0 += NB) {
+        const int nbk = imin(NB, N - j0);
+        const bool more = j0 + nbk < N;
+        auto rsl = [&](int lr) { int t = rb + lr; return t >= WR ? t - WR : t; };
+        auto csl = [&](int lc) { int t = cb + lc; return t >= WC ? t - WC : t; };
+
+        // ---------------- A. panel J | update of panel J-1, staging --------
+        if (warp == 0) {
+            const int rbp = rsl(NB), cbp = csl(NB);
+            panel_factor<R, NB, RS, FWD>(win, P, WR, WC, rbp, cbp, KL + NB, rs, pvoff, shv, j0, nbk,
+                                         N, KL, KU, fl, pv, FWD ? y + s * y_stride : nullptr, lane);
+        } else {
+            const int wt = tid - 32;
+            if (nbp > 0) {
+                // A(j0+i, j0+NB .. ju_{J-1}) -= L21_{J-1} U12_{J-1}
+                const int cep = shv[2] - (j0 - NB);      // last column, logical
+                const int ntr = cep - 2 * NB + 1;
+                const int nrow = imin(KL, N - j0);       // rows lr = NB + i
+                const int rg = wt >> 3, cg = wt & 7;
+                for (int r0 = 0; r0 < nrow && ntr > 0; r0 += RGW * MT) {
+                    int roff[MT];
+#pragma unroll
+                    for (int t = 0; t < MT; ++t) {
+                        const int i = r0 + rg + RGW * t;
+                        roff[t] = (i < nrow) ? rsl(NB + i) * P : -1;
+                    }
+                    for (int c0 = 0; c0 < ntr; c0 += 8 * TC) {
+                        int coff[TC];
+#pragma unroll
+                        for (int u = 0; u < TC; ++u) {
+                            const int c = c0 + cg + 8 * u;
+                            coff[u] = (c < ntr) ? csl(2 * NB + c) : -1;
+                        }
+                        T2 acc[MT][TC];
+#pragma unroll
+                        for (int t = 0; t < MT; ++t)
+#pragma unroll
+                            for (int u = 0; u < TC; ++u)
+                                acc[t][u] = (roff[t] >= 0 && coff[u] >= 0) ? win[roff[t] + coff[u]] : zero;
+#pragma unroll
+                        for (int m = 0; m < NB; ++m) {
+                            if (m < nbp) {
+                                const int cm = csl(m), rm = rsl(m) * P;
+                                T2 l[MT], uu[TC];
+#pragma unroll
+                                for (int t = 0; t < MT; ++t) l[t] = roff[t] >= 0 ? win[roff[t] + cm] : zero;
+#pragma unroll
+                                for (int u = 0; u < TC; ++u) uu[u] = coff[u] >= 0 ? win[rm + coff[u]] : zero;
+#pragma unroll
+                                for (int t = 0; t < MT; ++t)
+#pragma unroll
+                                    for (int u = 0; u < TC; ++u)
+                                        acc[t][u] = cfnma(l[t], uu[u], acc[t][u]);
+                            }
+                        }
+#pragma unroll
+                        for (int t = 0; t < MT; ++t)
+#pragma unroll
+                            for (int u = 0; u < TC; ++u)
+                                if (roff[t] >= 0 && coff[u] >= 0) win[roff[t] + coff[u]] = acc[t][u];
+                    }
+                }
+                // U rows of panel J-1 (rows j0-NB+m, slot lr = m)
+                for (int m = warp - 1; m < nbp; m += NWK) {
+                    const long long jr = j0 - NB + m;
+                    const int ro = rsl(m) * P;
+                    for (int t = lane; t < UW; t += 32) fu[jr * UW + t] = win[ro + csl(m + t)];
+                }
+            }
+            // rows j0+KL+NB+k enter after this panel, at the next window's
+            // columns j0 .. j0+WC-1
+            if (more) {
+                const int kb = NB * (warp - 1) / NWK, ke = NB * warp / NWK;
+                assemble_rows<R, MODEL>(src, ms, coef, magic, s, N, KL, KU, WC, j0 + KL + NB + kb,
+                                        ke - kb, j0, lane,
+                                        [&](int k, int cc, T2 v) { stg[(kb + k) * WC + cc] = v; });
+                if (FWD)
+                    for (int k = wt; k < NB; k += NTK) {
+                        const int r = j0 + KL + NB + k;
+                        stgr[k] = r < N ? from_z<R>(rhs[s * rhs_stride + r]) : zero;
+                    }
+            }
+        }
+        __syncthreads();
+        tick(1);
+
+        // ---------------- B. interchanges and U12 of panel J ---------------
+        const int ju = shv[0];
+        const int ce = ju - (j0 - NB);       // last trailing column, logical (< WC)
+        for (int c = NB + nbk + tid; c <= ce; c += NT) {
+            const int cc = csl(c);
+            for (int k = 0; k < nbk; ++k) {
+                const int bt = pvoff[k];
+                if (bt) {
+                    T2 &a = win[rsl(NB + k) * P + cc], &b = win[rsl(NB + k + bt) * P + cc];
+                    const T2 t = a; a = b; b = t;
+                }
+            }
+            T2 u[NB];
+#pragma unroll
+            for (int k = 0; k < NB; ++k) {
+                if (k < nbk) {
+                    const int ro = rsl(NB + k) * P;
+                    T2 v = win[ro + cc];
+#pragma unroll
+                    for (int m = 0; m < NB; ++m)
+                        if (m < k) v = cfnma(win[ro + csl(NB + m)], u[m], v);
+                    u[k] = v;
+                    win[ro + cc] = v;
+                }
+            }
+        }
+        __syncthreads();
+        if (tid == 0) shv[2] = ju;           // read by the workers in the next phase A
+        tick(2);
+
+        // ---------------- C. panel J+1's columns; retire / enter -----------
+        if (more) {
+            const int nrow = imin(KL, N - j0 - nbk);            // rows lr = NB + nbk + i
+            const int ncol = imin(NB, ce - (NB + nbk) + 1);     // columns lc = NB + nbk + c
+            for (int idx = tid; idx < nrow * NB; idx += NT) {
+                const int i = idx >> LNB, c = idx & (NB - 1);
+                if (c < ncol) {
+                    const int ro = rsl(NB + nbk + i) * P, cc = csl(NB + nbk + c);
+                    T2 acc = win[ro + cc];
+#pragma unroll
+                    for (int m = 0; m < NB; ++m)
+                        if (m < nbk) acc = cfnma(win[ro + csl(NB + m)], win[rsl(NB + m) * P + cc], acc);
+                    win[ro + cc] = acc;
+                }
+            }
+            // panel J-1's columns (lc < NB) become columns j0+KL+KU+NB.. of the
+            // staying rows: zero
+            for (int idx = tid; idx < WR * NB; idx += NT) {
+                const int lr = idx >> LNB, c = idx & (NB - 1);
+                if (lr >= NB) win[rsl(lr) * P + csl(c)] = zero;
+            }
+            // panel J-1's row slots take rows j0+KL+NB+k (next columns j0 + cc)
+            for (int k = warp; k < NB; k += NW) {
+                T2 *dst = win + rsl(k) * P;
+                for (int cc = lane; cc < WC; cc += 32) {
+                    int cs = cb + NB + cc;           // < 3 WC: wrap at most twice
+                    if (cs >= WC) cs -= WC;
+                    if (cs >= WC) cs -= WC;
+                    dst[cs] = stg[k * WC + cc];
+                }
+            }
+            if (FWD)
+                for (int k = tid; k < NB; k += NT) rs[rsl(k)] = stgr[k];
+            __syncthreads();
+        }
+        tick(3);
+        rb += NB; if (rb >= WR) rb -= WR;
+        cb += NB; if (cb >= WC) cb -= WC;
+        nbp = nbk;
+    }
+    // U rows of the last panel (rows j0-NB+m, slot lr = m after the shift)
+    {
+        auto rsl = [&](int lr) { int t = rb + lr; return t >= WR ? t - WR : t; };
+        auto csl = [&](int lc) { int t = cb + lc; return t >= WC ? t - WC : t; };
+        for (int m = warp; m < nbp; m += NW) {
+            const long long jr = j0 - NB + m;
+            const int ro = rsl(m) * P;
+            for (int t = lane; t < UW; t += 32) fu[jr * UW + t] = win[ro + csl(m + t)];
+        }
+    }
+    tick(4);
+    if (tid == 0) info[fi] = shv[1];
+    if (prof && tid == 0)
+        for (int ph = 0; ph < 6; ++ph) atomicAdd(prof + ph, tph[ph]);
+}
+
+template <typename R, int NB, int NW, int MAXTR, bool LA, bool MODEL, bool FWD>
 cudaError_t launch_cta_one(const GbtrfArgs &a, cudaStream_t st)
 {
     const int S = MODEL ? a.ms.cs.S : 1;
-    const size_t smem = gbtrf_blk_smem_bytes(sizeof(R), a.g, S, NB, NW);
-    auto kern = k_gbtrf_cta<R, NB, NW, MAXTR, MODEL, FWD>;
+    const size_t smem = gbtrf_blk_smem_bytes(sizeof(R), a.g, S, NB, LA ? -NW : NW);
+    auto kern = [] {
+        if constexpr (LA) return k_gbtrf_la<R, NB, NW, MODEL, FWD>;
+        else return k_gbtrf_cta<R, NB, NW, MAXTR, MODEL, FWD>;
+    }();
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
     if (e != cudaSuccess) return e;
     const int grid = a.sys_list ? a.nlist : a.nsys;
@@ -528,24 +906,28 @@ cudaError_t launch_cta_one(const GbtrfArgs &a, cudaStream_t st)
     return cudaGetLastError();
 }
 
-template <typename R, int NB, int NW, int MAXTR>
+template <typename R, int NB, int NW, int MAXTR, bool LA>
 cudaError_t launch_cta_r(const GbtrfArgs &a, cudaStream_t st)
 {
     const bool fwd = a.rhs != nullptr;
-    if (a.model) return fwd ? launch_cta_one<R, NB, NW, MAXTR, true, true>(a, st)
-                            : launch_cta_one<R, NB, NW, MAXTR, true, false>(a, st);
-    return fwd ? launch_cta_one<R, NB, NW, MAXTR, false, true>(a, st)
-               : launch_cta_one<R, NB, NW, MAXTR, false, false>(a, st);
+    if (a.model) return fwd ? launch_cta_one<R, NB, NW, MAXTR, LA, true, true>(a, st)
+                            : launch_cta_one<R, NB, NW, MAXTR, LA, true, false>(a, st);
+    return fwd ? launch_cta_one<R, NB, NW, MAXTR, LA, false, true>(a, st)
+               : launch_cta_one<R, NB, NW, MAXTR, LA, false, false>(a, st);
 }
 
-// Rows per GEMM thread for NW warps: KL <= (4 NW) * MAXTR.
+// The phased kernel: KL <= (4 NW) MAXTR rows of the trailing update per
+// thread.  The lookahead kernel (variant 2, NW = 2 or 4) loops its worker
+// update over row passes.
 template <typename R, int NB>
 cudaError_t launch_cta_nw(const GbtrfArgs &a, int nw, cudaStream_t st)
 {
     const int KL = a.g.KL;
-    if (nw == 1) return KL <= 36 ? launch_cta_r<R, NB, 1, 9>(a, st) : launch_cta_r<R, NB, 1, 13>(a, st);
-    if (nw == 2) return KL <= 40 ? launch_cta_r<R, NB, 2, 5>(a, st) : launch_cta_r<R, NB, 2, 7>(a, st);
-    return KL <= 48 ? launch_cta_r<R, NB, 4, 3>(a, st) : launch_cta_r<R, NB, 4, 4>(a, st);
+    if (a.variant == 2 && nw > 1)
+        return nw == 2 ? launch_cta_r<R, NB, 2, 1, true>(a, st) : launch_cta_r<R, NB, 4, 1, true>(a, st);
+    if (nw == 1) return KL <= 36 ? launch_cta_r<R, NB, 1, 9, false>(a, st) : launch_cta_r<R, NB, 1, 13, false>(a, st);
+    if (nw == 2) return KL <= 40 ? launch_cta_r<R, NB, 2, 5, false>(a, st) : launch_cta_r<R, NB, 2, 7, false>(a, st);
+    return KL <= 48 ? launch_cta_r<R, NB, 4, 3, false>(a, st) : launch_cta_r<R, NB, 4, 4, false>(a, st);
 }
 
 // One translation unit per (precision, NB) instantiates the kernels.

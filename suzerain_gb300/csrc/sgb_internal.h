@@ -24,7 +24,7 @@ struct GbtrfArgs {
     int nlist = 0;                   // grid size when sys_list is set
     const int *d_count = nullptr;    // optional device count bounding the list
     bool slot_mode = false;          // factor/ipiv/info indexed by list position
-    int variant = 0;                 // 0 blocked (default), 1 unblocked reference kernel
+    int variant = 0;                 // 0 blocked (default), 1 unblocked, 2 blocked with lookahead
     int nb = 0;                      // panel width of the blocked kernel (4, 8, 16; 0 = default)
     int nw = 0;                      // warps per system of the blocked kernel (1, 2, 4; 0 = default)
     unsigned long long *prof = nullptr;  // optional per-phase cycle counters (6)

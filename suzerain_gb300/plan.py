@@ -46,6 +46,7 @@ class Plan:
         self.case = case
         self.nsys = int(len(kx))
         self.N = case.N
+        self.KL, self.KU = case.KL, case.KU
         self._kx = np.ascontiguousarray(kx, dtype=np.float64)
         self._kz = np.ascontiguousarray(kz, dtype=np.float64)
         self._cs = case.ctypes_case()

@@ -81,8 +81,9 @@ def test_gbtrf_batched_fp64_matches_zgbtf2(lib, oracle, torch_cuda, n, kl, ku):
 @pytest.mark.parametrize("n,kl,ku", GEOMS)
 @pytest.mark.parametrize("prec", ["Z", "C"])
 def test_blocked_factor_equals_unblocked(lib, torch_cuda, n, kl, ku, prec):
-    """The blocked kernel defers the rank-1 updates into a GEMM but applies
-    the same multiply-adds in the same order: factors are bit-identical."""
+    """The blocked kernels (phased and lookahead) defer the rank-1 updates
+    into GEMMs but apply the same multiply-adds in the same order: factors
+    are bit-identical to the unblocked kernel's."""
     torch = torch_cuda
     rng = np.random.default_rng(300 + n + kl)
     nsys = 5
@@ -99,7 +100,8 @@ def test_blocked_factor_equals_unblocked(lib, torch_cuda, n, kl, ku, prec):
     dt = torch.complex128 if prec == "Z" else torch.complex64
     outs = []
     shapes = [(1, 8, 1)] + [(0, nb, nw) for nb in (4, 8, 16) for nw in (1, 2, 4)
-                            if kl <= {1: 52, 2: 56, 4: 64}[nw]]
+                            if kl <= {1: 52, 2: 56, 4: 64}[nw]] \
+        + [(2, nb, nw) for nb in (4, 8, 16) for nw in (2, 4) if kl <= {2: 56, 4: 64}[nw]]
     for variant, nb, nw in shapes:
         fac = torch.full((nsys * fe,), float("nan"), dtype=dt, device="cuda")
         ipiv = torch.zeros(nsys * n, dtype=torch.int32, device="cuda")
@@ -630,3 +632,18 @@ def test_dropin_bsplineop_accumulate_golden(lib):
         assert np.allclose(y, good, rtol=0, atol=1e-14)
     finally:
         lib.suzerain_bsplineop_free(w)
+
+
+def test_tuner_records_a_supported_shape(lib, torch_cuda):
+    """tune_packed times every candidate and records the fastest; the
+    recorded shape is then what the batched factor uses by default."""
+    from suzerain_gb300 import tune
+    n, kl, ku = 120, 9, 9
+    saved = tune.get_shape("C", n, kl, ku)
+    try:
+        res = tune.tune_packed("C", n, kl, ku, nsys=64, reps=1)
+        best = res["best"]
+        assert best in res and all(v > 0 for k, v in res.items() if k != "best")
+        assert tune.get_shape("C", n, kl, ku) == best
+    finally:
+        tune.set_shape("C", n, kl, ku, *saved)
