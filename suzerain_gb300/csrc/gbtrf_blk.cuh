@@ -29,8 +29,9 @@
 namespace sgb {
 
 // Row pitch of the shared-memory window: odd, so that a column walked by the
-// lanes of a warp spreads over the banks.
-__host__ __device__ __forceinline__ int blk_pitch(int wc) { return wc | 1; }
+// lanes of a warp spreads over the banks, and above WC, so that column WC of
+// every row is a sink for the trailing update (below).
+__host__ __device__ __forceinline__ int blk_pitch(int wc) { return (wc + 1) | 1; }
 
 // floor(x / S) for 0 <= x < 65536 and 2 <= S <= 65536 by a multiply-high
 // with m = ceil(2^32 / S) = (2^32 + e) / S, 0 <= e < S: x m / 2^32 exceeds
@@ -300,6 +301,16 @@ __device__ __forceinline__ void assemble_rows(const PackedSource &src, const Mod
         for (int c0 = 0; c0 < WC; c0 += 32 * GC) {
             Raw raw[GR][GC];
             int tag[GR][GC];       // -1 zero, -2 one (wall diagonal), else coefficient index
+            // per column: in range, block column q and equation f (model)
+            int cq[GC], cf[GC];
+            bool cok[GC];
+#pragma unroll
+            for (int ii = 0; ii < GC; ++ii) {
+                const int cc = c0 + lane + 32 * ii, col = cbase + cc;
+                cok[ii] = cc < WC && col >= 0 && col < N;
+                cq[ii] = MODEL && cok[ii] ? div_small(col, magic) : 0;
+                cf[ii] = col - cq[ii] * S;
+            }
 #pragma unroll
             for (int kk = 0; kk < GR; ++kk) {
                 const int k = k0 + kk, r = r0 + k;
@@ -315,17 +326,17 @@ __device__ __forceinline__ void assemble_rows(const PackedSource &src, const Mod
                 }
 #pragma unroll
                 for (int ii = 0; ii < GC; ++ii) {
-                    const int cc = c0 + lane + 32 * ii, col = cbase + cc;
+                    const int col = cbase + c0 + lane + 32 * ii;
                     int t = -1;
-                    if (rv && cc < WC && col >= 0 && col < N) {
+                    if (rv && cok[ii]) {
                         if constexpr (MODEL) {
                             if (dir) {
                                 t = col == r ? -2 : -1;
                             } else {
-                                const int q = div_small(col, magic), f = col - q * S, d = p - q;
+                                const int q = cq[ii], d = p - q;
                                 if (d <= ms.cs.kl && -d <= ms.cs.ku) {
                                     const int bk = ms.cs.ku + d + q * ms.cs.ld;
-                                    t = e * S + f;
+                                    t = e * S + cf[ii];
                                     if constexpr (sizeof(R) == 8)
                                         raw[kk][ii] = make_double3(__ldg(ms.cs.M + bk), __ldg(ms.cs.D1 + bk),
                                                                    __ldg(ms.cs.D2 + bk));
@@ -413,8 +424,11 @@ k_gbtrf_cta(FactorGeom g, int nsys, PackedSource src, ModelSource ms,
     const unsigned magic = (MODEL && S > 1) ? (unsigned) ((0x100000000ull + S - 1) / S) : 0u;
 
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T2 *win = reinterpret_cast<T2 *>(smem_raw);       // WR x WC, row pitch P
-    T2 *rs = win + WR * P;                            // RHS per row slot
+    // WR x WC, row pitch P, plus the sink row WR: the trailing update's
+    // out-of-range rows and columns read and write row WR and column WC
+    // instead of being predicated; nothing else reads the sinks.
+    T2 *win = reinterpret_cast<T2 *>(smem_raw);
+    T2 *rs = win + (WR + 1) * P;                      // RHS per row slot
     T2 *stg = rs + WR;                                // NB x WC staged rows (STAGE)
     T2 *stgr = stg + (STAGE ? NB * WC : 0);           // NB staged RHS entries (STAGE)
     T2 *coef = stgr + (STAGE ? NB : 0);               // 3 S^2 (model)
@@ -529,30 +543,30 @@ k_gbtrf_cta(FactorGeom g, int nsys, PackedSource src, ModelSource ms,
 #pragma unroll
             for (int t = 0; t < MAXTR; ++t) {
                 const int i = rg + RGN * t;
-                roff[t] = (i < nrow) ? rsl(nbk + i) * P : -1;
+                roff[t] = (i < nrow) ? rsl(nbk + i) * P : WR * P;
             }
             for (int c0 = 0; c0 < ntr; c0 += 8 * TC) {
                 int coff[TC];
 #pragma unroll
                 for (int u = 0; u < TC; ++u) {
                     const int c = c0 + cg + 8 * u;
-                    coff[u] = (c < ntr) ? csl(nbk + c) : -1;
+                    coff[u] = (c < ntr) ? csl(nbk + c) : WC;
                 }
                 T2 acc[MAXTR][TC];
 #pragma unroll
                 for (int t = 0; t < MAXTR; ++t)
 #pragma unroll
                     for (int u = 0; u < TC; ++u)
-                        acc[t][u] = (roff[t] >= 0 && coff[u] >= 0) ? win[roff[t] + coff[u]] : zero;
+                        acc[t][u] = win[roff[t] + coff[u]];
 #pragma unroll
                 for (int m = 0; m < NB; ++m) {
                     if (m < nbk) {
                         const int cm = csl(m), rm = rsl(m) * P;
                         T2 l[MAXTR], uu[TC];
 #pragma unroll
-                        for (int t = 0; t < MAXTR; ++t) l[t] = roff[t] >= 0 ? win[roff[t] + cm] : zero;
+                        for (int t = 0; t < MAXTR; ++t) l[t] = win[roff[t] + cm];
 #pragma unroll
-                        for (int u = 0; u < TC; ++u) uu[u] = coff[u] >= 0 ? win[rm + coff[u]] : zero;
+                        for (int u = 0; u < TC; ++u) uu[u] = win[rm + coff[u]];
 #pragma unroll
                         for (int t = 0; t < MAXTR; ++t)
 #pragma unroll
@@ -564,7 +578,7 @@ k_gbtrf_cta(FactorGeom g, int nsys, PackedSource src, ModelSource ms,
                 for (int t = 0; t < MAXTR; ++t)
 #pragma unroll
                     for (int u = 0; u < TC; ++u)
-                        if (roff[t] >= 0 && coff[u] >= 0) win[roff[t] + coff[u]] = acc[t][u];
+                        win[roff[t] + coff[u]] = acc[t][u];
             }
         }
         for (int k = warp; k < nbk; k += NW) {
@@ -662,8 +676,8 @@ k_gbtrf_la(FactorGeom g, int nsys, PackedSource src, ModelSource ms,
     const unsigned magic = (MODEL && S > 1) ? (unsigned) ((0x100000000ull + S - 1) / S) : 0u;
 
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T2 *win = reinterpret_cast<T2 *>(smem_raw);       // WR x WC, row pitch P
-    T2 *rs = win + WR * P;                            // RHS per row slot
+    T2 *win = reinterpret_cast<T2 *>(smem_raw);       // WR x WC, pitch P, + sink row WR
+    T2 *rs = win + (WR + 1) * P;                      // RHS per row slot
     T2 *stg = rs + WR;                                // NB x WC staged rows
     T2 *stgr = stg + NB * WC;                         // NB staged RHS entries
     T2 *coef = stgr + NB;                             // 3 S^2 (model)
@@ -737,30 +751,30 @@ k_gbtrf_la(FactorGeom g, int nsys, PackedSource src, ModelSource ms,
 #pragma unroll
                     for (int t = 0; t < MT; ++t) {
                         const int i = r0 + rg + RGW * t;
-                        roff[t] = (i < nrow) ? rsl(NB + i) * P : -1;
+                        roff[t] = (i < nrow) ? rsl(NB + i) * P : WR * P;
                     }
                     for (int c0 = 0; c0 < ntr; c0 += 8 * TC) {
                         int coff[TC];
 #pragma unroll
                         for (int u = 0; u < TC; ++u) {
                             const int c = c0 + cg + 8 * u;
-                            coff[u] = (c < ntr) ? csl(2 * NB + c) : -1;
+                            coff[u] = (c < ntr) ? csl(2 * NB + c) : WC;
                         }
                         T2 acc[MT][TC];
 #pragma unroll
                         for (int t = 0; t < MT; ++t)
 #pragma unroll
                             for (int u = 0; u < TC; ++u)
-                                acc[t][u] = (roff[t] >= 0 && coff[u] >= 0) ? win[roff[t] + coff[u]] : zero;
+                                acc[t][u] = win[roff[t] + coff[u]];
 #pragma unroll
                         for (int m = 0; m < NB; ++m) {
                             if (m < nbp) {
                                 const int cm = csl(m), rm = rsl(m) * P;
                                 T2 l[MT], uu[TC];
 #pragma unroll
-                                for (int t = 0; t < MT; ++t) l[t] = roff[t] >= 0 ? win[roff[t] + cm] : zero;
+                                for (int t = 0; t < MT; ++t) l[t] = win[roff[t] + cm];
 #pragma unroll
-                                for (int u = 0; u < TC; ++u) uu[u] = coff[u] >= 0 ? win[rm + coff[u]] : zero;
+                                for (int u = 0; u < TC; ++u) uu[u] = win[rm + coff[u]];
 #pragma unroll
                                 for (int t = 0; t < MT; ++t)
 #pragma unroll
@@ -772,7 +786,7 @@ k_gbtrf_la(FactorGeom g, int nsys, PackedSource src, ModelSource ms,
                         for (int t = 0; t < MT; ++t)
 #pragma unroll
                             for (int u = 0; u < TC; ++u)
-                                if (roff[t] >= 0 && coff[u] >= 0) win[roff[t] + coff[u]] = acc[t][u];
+                                win[roff[t] + coff[u]] = acc[t][u];
                     }
                 }
                 // U rows of panel J-1 (rows j0-NB+m, slot lr = m)
