@@ -365,6 +365,22 @@ int sgb_plan_substep(sgb_plan *p, char method, double phi_exp, double phi_imp,
                      const void *u_in, void *u_out,
                      const sgb_refine_spec *spec, void *stream);
 
+/** sgb_plan_substep in a form that can be recorded into a CUDA graph: no
+ *  host synchronization, allocation or host-to-device copy.  Call
+ *  sgb_plan_substep once with the same method first (it allocates the
+ *  workspace).  Method 'M' runs min(siter + 1, 4) complex64 correction solves
+ *  whose grids are bounded by device-side counts (exactly the reference's
+ *  bound when siter <= 3; with a larger siter, systems still refining after
+ *  four solves move to the complex128 fallback as if siter were exhausted),
+ *  and one fallback chunk of at most max_double_slots systems with the
+ *  reference's diter bound.  sgb_plan_unserved reports, after the work has
+ *  run, how many fallback systems did not fit the chunk (their solution is
+ *  the complex64 one, flagged fact = 'S' with tolsc > 1). */
+int sgb_plan_substep_capturable(sgb_plan *plan, char method, double phi_exp,
+                                double phi_imp, const void *u_in, void *u_out,
+                                const sgb_refine_spec *spec, void *stream);
+int sgb_plan_unserved(sgb_plan *plan, int *count);
+
 /** Same, from and to host memory (copies inside the call). */
 int sgb_plan_substep_host(sgb_plan *p, char method, double phi_exp,
                           double phi_imp, const void *u_in_host,

@@ -129,6 +129,9 @@ _SIGS = {
                               C.POINTER(RefineSpec), _p]),
     "sgb_plan_substep_host": (_i, [_p, C.c_char, _d, _d, _p, _p,
                                    C.POINTER(RefineSpec), _p]),
+    "sgb_plan_substep_capturable": (_i, [_p, C.c_char, _d, _d, _p, _p,
+                                         C.POINTER(RefineSpec), _p]),
+    "sgb_plan_unserved": (_i, [_p, _p]),
     "sgb_plan_report": (_i, [_p, _p, _p, _p, _p, _p, _p]),
     "sgb_plan_backward_error": (_i, [_p, _p, _p]),
     "sgb_plan_set_timing": (_i, [_p, _i]),

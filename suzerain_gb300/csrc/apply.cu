@@ -197,7 +197,7 @@ cudaError_t launch_residual(const ResidualArgs &a, cudaStream_t st)
         const int S = a.ms.cs.S, N = S * a.ms.cs.n;
         if (S > 8) return cudaErrorInvalidValue;
         const size_t smem = ((size_t) N + 3 * S * S) * sizeof(double2);
-        cudaError_t e = cudaFuncSetAttribute(k_model_op<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+        cudaError_t e = smem_attr((const void *) k_model_op<0>, smem);
         if (e != cudaSuccess) return e;
         k_model_op<0><<<grid, 32, smem, st>>>(a.nsys, a.ms, a.b, a.b_stride, a.x, a.x_stride,
                                               a.r, a.r_stride, a.rnorm2, a.xnorm2, a.sys_list, a.d_count,
@@ -209,7 +209,7 @@ cudaError_t launch_residual(const ResidualArgs &a, cudaStream_t st)
     void (*kern)(int, int, int, int, PackedSource, const double2 *, long long,
                  const double2 *, long long, double2 *, long long, double *, double *,
                  const int *, const int *, const int *, int) = t == 0 ? k_residual_packed<0> : (t == 1 ? k_residual_packed<1> : k_residual_packed<2>);
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+    cudaError_t e = smem_attr((const void *) kern, smem);
     if (e != cudaSuccess) return e;
     kern<<<grid, 32, smem, st>>>(a.nsys, a.N, a.KL, a.KU, a.src, a.b, a.b_stride, a.x, a.x_stride,
                                  a.r, a.r_stride, a.rnorm2, a.xnorm2, a.sys_list, a.d_count,
@@ -223,7 +223,7 @@ cudaError_t launch_model_apply(const ApplyArgs &a, cudaStream_t st)
     const int S = a.ms.cs.S, N = S * a.ms.cs.n;
     if (S > 8) return cudaErrorInvalidValue;
     const size_t smem = ((size_t) N + 3 * S * S) * sizeof(double2);
-    cudaError_t e = cudaFuncSetAttribute(k_model_op<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+    cudaError_t e = smem_attr((const void *) k_model_op<1>, smem);
     if (e != cudaSuccess) return e;
     k_model_op<1><<<a.nsys, 32, smem, st>>>(a.nsys, a.ms, nullptr, 0, a.u, a.u_stride,
                                             a.y, a.y_stride, nullptr, nullptr, nullptr, nullptr,

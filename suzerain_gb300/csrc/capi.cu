@@ -6,6 +6,7 @@
 #include "sgb_timer.h"
 
 #include <algorithm>
+#include <map>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -60,6 +61,23 @@ static bool geom_ok(int N, int KL, int KU)
 {
     return N >= 1 && KL >= 0 && KU >= 0 && KL + 1 <= 64 && KL + KU + 1 <= 192;
 }
+
+namespace sgb {
+cudaError_t smem_attr(const void *kernel, size_t bytes)
+{
+    static std::mutex mu;
+    static std::map<std::pair<const void *, int>, size_t> done;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lk(mu);
+    size_t &have = done[{kernel, dev}];
+    if (bytes <= have) return cudaSuccess;
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) bytes);
+    if (e == cudaSuccess) have = bytes;
+    return e;
+}
+}  // namespace sgb
 
 extern "C" int sgb_gbtrf_batched(char prec, int nsys, int N, int KL, int KU, const void *ab,
                                  int ldab, long long ab_stride, void *fac, int *ipiv,
@@ -435,14 +453,18 @@ extern "C" int sgb_plan_destroy(sgb_plan *p)
 
 extern "C" size_t sgb_plan_device_bytes(const sgb_plan *p) { return p ? p->dev_bytes : 0; }
 
+// capturable: no host synchronization, no allocation, no host-to-device copy
+// (the refinement runs its capped, device-counted form), so the call can be
+// recorded into a CUDA graph after one ordinary call of the same method.
 static int plan_substep(sgb_plan *p, char method, double phi_exp, double phi_imp,
                         const void *u_in, void *u_out, const sgb_refine_spec *spec,
-                        cudaStream_t st)
+                        cudaStream_t st, bool capturable = false)
 {
     const int nsys = p->nsys, N = p->N, S = p->hc.S, n = p->hc.n;
     const long long tot = (long long) nsys * N;
     const unsigned EB = (unsigned) ((tot + 255) / 256);
-    PhaseTimer &tm = p->timer;
+    PhaseTimer nop;
+    PhaseTimer &tm = capturable ? nop : p->timer;
     // 1. explicit operator (or plain permutation) into b
     tm.begin(phi_exp != 0.0 ? "explicit_apply_f64" : "permute_in", st);
     count_launch(1);
@@ -460,6 +482,8 @@ static int plan_substep(sgb_plan *p, char method, double phi_exp, double phi_imp
     FactorGeom g{N, p->KL, p->KU};
     p->phi_imp_last = phi_imp;
     if (method == 'Z') {
+        if (!p->fac64 && capturable)
+            return fail("sgb_plan_substep_capturable: run sgb_plan_substep with method 'Z' first");
         if (!p->fac64) {
             int rc = p->dalloc(&p->fac64, (size_t) nsys * g.fac_elems() * sizeof(double2), "cudaMalloc(fac64)");
             rc |= p->dalloc((void **) &p->ipiv64, (size_t) nsys * N * sizeof(int), "cudaMalloc(ipiv64)");
@@ -492,8 +516,15 @@ static int plan_substep(sgb_plan *p, char method, double phi_exp, double phi_imp
         P.aiter = spec ? spec->aiter : 5; P.siter = spec ? spec->siter : 25;
         P.diter = spec ? spec->diter : 5; P.tolsc = spec ? spec->tolsc : 1.0;
         P.nslot64 = p->nslot64; P.host_count = p->hcount;
-        P.timer = &p->timer;
+        P.timer = capturable ? nullptr : &p->timer;
+        if (capturable) {
+            P.graph = true;
+            P.graph_siter = P.siter < 0 ? 0 : std::min(P.siter + 1, 4);
+            P.graph_diter = P.diter + 2;
+        }
         const size_t need = refine_workspace_bytes(P);
+        if (need > p->rws_bytes && capturable)
+            return fail("sgb_plan_substep_capturable: run sgb_plan_substep with method 'M' first");
         if (need > p->rws_bytes) {
             int rc = p->dalloc(&p->rws, need, "cudaMalloc(refine workspace)");
             if (rc) return rc;
@@ -547,6 +578,26 @@ extern "C" int sgb_plan_substep(sgb_plan *p, char method, double phi_exp, double
     std::lock_guard<std::mutex> lk(p->mu);
     return plan_substep(p, (char) toupper(method), phi_exp, phi_imp, u_in, u_out, spec,
                         (cudaStream_t) stream);
+}
+
+extern "C" int sgb_plan_substep_capturable(sgb_plan *p, char method, double phi_exp,
+                                           double phi_imp, const void *u_in, void *u_out,
+                                           const sgb_refine_spec *spec, void *stream)
+{
+    if (!p || !u_in || !u_out) return fail("sgb_plan_substep_capturable: null argument");
+    std::lock_guard<std::mutex> lk(p->mu);
+    return plan_substep(p, (char) toupper(method), phi_exp, phi_imp, u_in, u_out, spec,
+                        (cudaStream_t) stream, true);
+}
+
+extern "C" int sgb_plan_unserved(sgb_plan *p, int *count)
+{
+    if (!p || !count) return fail("sgb_plan_unserved: null argument");
+    std::lock_guard<std::mutex> lk(p->mu);
+    *count = 0;
+    if (p->last_method != 'M' || !p->last.d_unserved) return 0;
+    SGB_CUDA_TRY(cudaMemcpy(count, p->last.d_unserved, sizeof(int), cudaMemcpyDeviceToHost));
+    return 0;
 }
 
 extern "C" int sgb_plan_substep_host(sgb_plan *p, char method, double phi_exp, double phi_imp,

@@ -213,7 +213,7 @@ static cudaError_t launch_one(const GbtrfArgs &a, cudaStream_t st)
     const int S = MODEL ? a.ms.cs.S : 1;
     const size_t smem = gbtrf_smem_bytes(sizeof(R), a.g, S);
     auto kern = k_gbtrf<R, MODEL, FWD>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+    cudaError_t e = smem_attr((const void *) kern, smem);
     if (e != cudaSuccess) return e;
     const int grid = a.sys_list ? a.nlist : a.nsys;
     if (grid == 0) return cudaSuccess;

@@ -908,7 +908,7 @@ cudaError_t launch_cta_one(const GbtrfArgs &a, cudaStream_t st)
         if constexpr (LA) return k_gbtrf_la<R, NB, NW, MODEL, FWD>;
         else return k_gbtrf_cta<R, NB, NW, MAXTR, MODEL, FWD>;
     }();
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+    cudaError_t e = smem_attr((const void *) kern, smem);
     if (e != cudaSuccess) return e;
     const int grid = a.sys_list ? a.nlist : a.nsys;
     if (grid == 0) return cudaSuccess;

@@ -479,7 +479,7 @@ static cudaError_t launch_quad(const GbtrsArgs &a, cudaStream_t st)
     if (!a.fwd_done) {
         const QuadFwdLayout<R> L(a.g);
         const size_t smem = (size_t) QSYS * L.SE * sizeof(T2);
-        e = cudaFuncSetAttribute(k_gbtrs_fwd_quad<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+        e = smem_attr((const void *) k_gbtrs_fwd_quad<R>, smem);
         if (e != cudaSuccess) return e;
         k_gbtrs_fwd_quad<R><<<grid, 32, smem, st>>>(a.g, a.nsys, reinterpret_cast<const T2 *>(a.fac),
                                                      a.fac_stride, a.ipiv, a.b, a.b_stride, yw,
@@ -491,7 +491,7 @@ static cudaError_t launch_quad(const GbtrsArgs &a, cudaStream_t st)
     const QuadBwdLayout<R> L(a.g);
     const size_t smem = (size_t) QSYS * L.SE * sizeof(T2);
     auto kern = a.accumulate ? k_gbtrs_bwd_quad<R, true> : k_gbtrs_bwd_quad<R, false>;
-    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+    e = smem_attr((const void *) kern, smem);
     if (e != cudaSuccess) return e;
     kern<<<grid, 32, smem, st>>>(a.g, a.nsys, reinterpret_cast<const T2 *>(a.fac), a.fac_stride, yw,
                                  a.x, a.x_stride, a.sys_list, a.nlist, a.d_count, a.slot_mode,
@@ -518,7 +518,7 @@ static cudaError_t launch_t(const GbtrsArgs &a, cudaStream_t st)
     const size_t smem = ((size_t) a.g.N + (size_t) PD * (a.g.UW() + a.g.KL)) * sizeof(cplx_t<R>)
                       + PD * sizeof(int);
     auto kern = k_gbtrs<R, TRANS, FWD_DONE, ACCUM>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+    cudaError_t e = smem_attr((const void *) kern, smem);
     if (e != cudaSuccess) return e;
     const int grid = a.sys_list ? a.nlist : a.nsys;
     if (grid == 0) return cudaSuccess;

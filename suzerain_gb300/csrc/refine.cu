@@ -141,6 +141,35 @@ __global__ void k_refine_enter_double(RefineState st, const int *__restrict__ li
     next[atomicAdd(ncount, 1)] = s;
 }
 
+// Capturable form: systems still refining in complex64 after the fixed
+// number of correction solves leave as if siter were exhausted
+// (dsgbsvx.def:223-230): to complex128 when allowed and not converged.
+__global__ void k_refine_cap(RefineState st, const int *__restrict__ list,
+                             const int *__restrict__ count, int dmax, int *__restrict__ listD,
+                             int *__restrict__ countD)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= *count) return;
+    const int s = list[k];
+    if (st.status[s] != ST_SINGLE) return;
+    if (dmax >= 0 && st.res[s] > st.tol[s]) {
+        st.status[s] = ST_NEED_D;
+        listD[atomicAdd(countD, 1)] = s;
+    } else {
+        st.status[s] = ST_DONE;
+        st.diter[s] = 0;
+    }
+}
+
+// chunk = min(count, cap); unserved = count - chunk
+__global__ void k_chunk_count(const int *__restrict__ count, int cap, int *__restrict__ chunk,
+                              int *__restrict__ unserved)
+{
+    const int c = *count;
+    *chunk = c < cap ? c : cap;
+    *unserved = c > cap ? c - cap : 0;
+}
+
 __global__ void k_refine_finalize(int nsys, RefineState st, double2 *__restrict__ x,
                                   long long x_stride, int N)
 {
@@ -388,81 +417,130 @@ int refine_batched(const RefineProblem &P, void *workspace, size_t workspace_byt
 
         int *cur = listS, *nxt = listS2, *ccur = cnt + 0, *cnxt = cnt + 1;
         int ncur = nsys;
-        for (;;) {
-            ra.sys_list = cur; ra.nlist = ncur; ra.d_count = ccur;
-            ra.status = rs.status; ra.status_want = ST_SINGLE;
-            tm.begin("residual_f64", st);
-            count_launch(2);
-            TRY(launch_residual(ra, st));
-            tm.end(st);
-            TRY(cudaMemsetAsync(cnxt, 0, sizeof(int), st));
-            k_refine_decide<<<B, T, 0, st>>>(rs, 0, rnorm, xnorm, P.aiter, P.siter, P.diter,
-                                             cur, ccur, nxt, cnxt, listD, cnt + 2);
-            TRY(cudaGetLastError());
-            TRY(sync_count(cnxt, hcnt, st));
-            ++iters;
-            if (*hcnt == 0 || iters > P.siter + 1) break;
-            ncur = *hcnt;
-            GbtrsArgs ca = sa;
-            ca.fwd_done = false; ca.yin = nullptr; ca.b = r; ca.b_stride = N;
-            ca.accumulate = true; ca.sys_list = nxt; ca.nlist = ncur; ca.d_count = cnxt;
-            tm.begin("solve_c64", st);
-            count_launch(1);
-            TRY(launch_gbtrs(ca, st));
-            tm.end(st);
-            std::swap(cur, nxt); std::swap(ccur, cnxt);
+        if (P.graph) {
+            // capturable: a fixed number of correction solves, grids bounded
+            // by the device counts; a final residual + decision, then the cap
+            for (int it = 0; it <= P.graph_siter; ++it) {
+                ra.sys_list = cur; ra.nlist = nsys; ra.d_count = ccur;
+                ra.status = rs.status; ra.status_want = ST_SINGLE;
+                count_launch(4);
+                TRY(launch_residual(ra, st));
+                TRY(cudaMemsetAsync(cnxt, 0, sizeof(int), st));
+                k_refine_decide<<<B, T, 0, st>>>(rs, 0, rnorm, xnorm, P.aiter, P.siter, P.diter,
+                                                 cur, ccur, nxt, cnxt, listD, cnt + 2);
+                TRY(cudaGetLastError());
+                if (it == P.graph_siter) {
+                    k_refine_cap<<<B, T, 0, st>>>(rs, nxt, cnxt, P.diter, listD, cnt + 2);
+                    TRY(cudaGetLastError());
+                    break;
+                }
+                GbtrsArgs ca = sa;
+                ca.fwd_done = false; ca.yin = nullptr; ca.b = r; ca.b_stride = N;
+                ca.accumulate = true; ca.sys_list = nxt; ca.nlist = nsys; ca.d_count = cnxt;
+                TRY(launch_gbtrs(ca, st));
+                std::swap(cur, nxt); std::swap(ccur, cnxt);
+            }
+            iters = P.graph_siter + 1;
+        } else {
+            for (;;) {
+                ra.sys_list = cur; ra.nlist = ncur; ra.d_count = ccur;
+                ra.status = rs.status; ra.status_want = ST_SINGLE;
+                tm.begin("residual_f64", st);
+                count_launch(2);
+                TRY(launch_residual(ra, st));
+                tm.end(st);
+                TRY(cudaMemsetAsync(cnxt, 0, sizeof(int), st));
+                k_refine_decide<<<B, T, 0, st>>>(rs, 0, rnorm, xnorm, P.aiter, P.siter, P.diter,
+                                                 cur, ccur, nxt, cnxt, listD, cnt + 2);
+                TRY(cudaGetLastError());
+                TRY(sync_count(cnxt, hcnt, st));
+                ++iters;
+                if (*hcnt == 0 || iters > P.siter + 1) break;
+                ncur = *hcnt;
+                GbtrsArgs ca = sa;
+                ca.fwd_done = false; ca.yin = nullptr; ca.b = r; ca.b_stride = N;
+                ca.accumulate = true; ca.sys_list = nxt; ca.nlist = ncur; ca.d_count = cnxt;
+                tm.begin("solve_c64", st);
+                count_launch(1);
+                TRY(launch_gbtrs(ca, st));
+                tm.end(st);
+                std::swap(cur, nxt); std::swap(ccur, cnxt);
+            }
         }
     }
     out.single_iters = iters;
 
     // ---- complex128 fallback, in chunks of nslot64 factor slots ------------
-    TRY(sync_count(cnt + 2, hcnt, st));
-    const int nd = *hcnt;
-    out.n_double = nd;
     int d_iters = 0;
-    for (int base = 0; base < nd; base += P.nslot64) {
-        const int chunk = std::min(P.nslot64, nd - base);
-        int *clist = listD + base;
-        TRY(cudaMemcpyAsync(cnt + 4, &chunk, sizeof(int), cudaMemcpyHostToDevice, st));
+    auto fallback_chunk = [&](int *clist, int chunk_host, int iters_max, bool host_loop) -> int {
         GbtrfArgs da;
         da.prec = 'Z'; da.g = P.g; da.nsys = nsys; da.model = P.model; da.src = P.src;
         da.ms = P.ms; da.fac = fac64; da.fac_stride = P.g.fac_elems(); da.ipiv = ipiv64;
-        da.info = info64; da.sys_list = clist; da.nlist = chunk; da.d_count = cnt + 4;
+        da.info = info64; da.sys_list = clist; da.nlist = chunk_host; da.d_count = cnt + 4;
         da.slot_mode = true;
         tm.begin("factor_c128_fallback", st);
         count_launch(2);
         TRY(launch_gbtrf(da, st));
         tm.end(st);
         TRY(cudaMemsetAsync(cnt + 5, 0, sizeof(int), st));
-        k_refine_enter_double<<<(chunk + T - 1) / T, T, 0, st>>>(rs, clist, cnt + 4, info64, 0,
-                                                                 listD2, cnt + 5);
+        k_refine_enter_double<<<(chunk_host + T - 1) / T, T, 0, st>>>(rs, clist, cnt + 4, info64, 0,
+                                                                      listD2, cnt + 5);
         TRY(cudaGetLastError());
-        TRY(sync_count(cnt + 5, hcnt, st));
-        int active = *hcnt, it = 0;
-        while (active > 0 && it <= P.diter + 1) {
+        int active = 1, it = 0;
+        if (host_loop) {
+            TRY(sync_count(cnt + 5, hcnt, st));
+            active = *hcnt;
+        }
+        while (active > 0 && it < iters_max) {
             GbtrsArgs sa;
             sa.prec = 'Z'; sa.trans = P.trans; sa.g = P.g; sa.nsys = nsys; sa.fac = fac64;
             sa.fac_stride = P.g.fac_elems(); sa.ipiv = ipiv64; sa.b = r; sa.b_stride = N;
             sa.x = P.x; sa.x_stride = P.x_stride; sa.accumulate = true;
-            sa.sys_list = clist; sa.nlist = chunk; sa.d_count = cnt + 4; sa.slot_mode = true;
+            sa.sys_list = clist; sa.nlist = chunk_host; sa.d_count = cnt + 4; sa.slot_mode = true;
             sa.status = rs.status; sa.status_want = ST_DOUBLE;
             tm.begin("solve_c128_fallback", st);
             count_launch(3);
             TRY(launch_gbtrs(sa, st));
             tm.end(st);
-            ra.sys_list = clist; ra.nlist = chunk; ra.d_count = cnt + 4;
+            ra.sys_list = clist; ra.nlist = chunk_host; ra.d_count = cnt + 4;
             ra.status = rs.status; ra.status_want = ST_DOUBLE;
             TRY(launch_residual(ra, st));
             TRY(cudaMemsetAsync(cnt + 7, 0, sizeof(int), st));
-            k_refine_decide<<<(chunk + T - 1) / T, T, 0, st>>>(rs, 1, rnorm, xnorm, P.aiter,
-                                                              P.siter, P.diter, clist, cnt + 4,
-                                                              listD2, cnt + 7, listD2, cnt + 8);
+            k_refine_decide<<<(chunk_host + T - 1) / T, T, 0, st>>>(rs, 1, rnorm, xnorm, P.aiter,
+                                                                   P.siter, P.diter, clist, cnt + 4,
+                                                                   listD2, cnt + 7, listD2, cnt + 8);
             TRY(cudaGetLastError());
-            TRY(sync_count(cnt + 7, hcnt, st));
-            active = *hcnt;
+            if (host_loop) {
+                TRY(sync_count(cnt + 7, hcnt, st));
+                active = *hcnt;
+            }
             ++it;
         }
         d_iters = std::max(d_iters, it);
+        return 0;
+    };
+    out.d_unserved = cnt + 9;
+    if (P.graph) {
+        // capturable: one chunk of at most nslot64 systems, fixed iterations
+        count_launch(1);
+        k_chunk_count<<<1, 1, 0, st>>>(cnt + 2, P.nslot64, cnt + 4, cnt + 9);
+        TRY(cudaGetLastError());
+        if (P.diter >= 0) {
+            int rc = fallback_chunk(listD, P.nslot64, imax(P.graph_diter, 1), false);
+            if (rc) return rc;
+        }
+        out.n_double = -1;       // on the device: cnt[2]
+    } else {
+        TRY(cudaMemsetAsync(cnt + 9, 0, sizeof(int), st));
+        TRY(sync_count(cnt + 2, hcnt, st));
+        const int nd = *hcnt;
+        out.n_double = nd;
+        for (int base = 0; base < nd; base += P.nslot64) {
+            const int chunk = std::min(P.nslot64, nd - base);
+            TRY(cudaMemcpyAsync(cnt + 4, &chunk, sizeof(int), cudaMemcpyHostToDevice, st));
+            int rc = fallback_chunk(listD + base, chunk, P.diter + 2, true);
+            if (rc) return rc;
+        }
     }
     out.double_iters = d_iters;
     count_launch(1);

@@ -5,6 +5,11 @@
 
 namespace sgb {
 
+// cudaFuncSetAttribute(MaxDynamicSharedMemorySize) once per (kernel, device,
+// size): later launches (including those recorded into a CUDA graph) make no
+// driver call for it.
+cudaError_t smem_attr(const void *kernel, size_t bytes);
+
 struct GbtrfArgs {
     char prec = 'Z';             // 'Z' complex128 factor, 'C' complex64
     FactorGeom g{};

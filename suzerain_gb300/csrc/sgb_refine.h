@@ -31,6 +31,17 @@ struct RefineProblem {
     int nslot64 = 1;             // complex128 factor slots for the fallback
     int *host_count = nullptr;   // pinned host int for list counts
     struct PhaseTimer *timer = nullptr;   // optional per-phase event timing
+    // Capturable form (no host synchronization, no host-to-device copies):
+    // the complex64 loop runs exactly graph_siter correction solves whose
+    // grids are bounded by device counts (systems still refining then leave
+    // as if siter were exhausted; graph_siter = siter + 1 is the reference's
+    // own bound), and the complex128 fallback runs one chunk of at most
+    // nslot64 systems for graph_diter iterations (diter + 2 is the
+    // reference's bound); systems beyond the chunk are counted in
+    // RefineOutputs::d_unserved (device int) and keep status "needs
+    // complex128".
+    bool graph = false;
+    int graph_siter = 0, graph_diter = 0;
 };
 
 struct RefineOutputs {
@@ -42,6 +53,7 @@ struct RefineOutputs {
     void *fac32 = nullptr, *fac64 = nullptr;     // row-panel factors (slot 0 first)
     int *ipiv32 = nullptr, *ipiv64 = nullptr;
     int single_iters = 0, double_iters = 0, n_double = 0;
+    int *d_unserved = nullptr;   // capturable form: fallback systems beyond the chunk
 };
 
 size_t refine_workspace_bytes(const RefineProblem &P);

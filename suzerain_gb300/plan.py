@@ -75,6 +75,24 @@ class Plan:
                                      C.byref(sp), _ptr(stream))
         nat.check(rc, "sgb_plan_substep")
 
+    def substep_capturable(self, method: str, phi_exp: float, phi_imp: float, u_in, u_out,
+                           spec: RefineSpec | None = None, stream=0) -> None:
+        """substep without host synchronization or allocation, so that it can
+        be recorded into a CUDA graph (run substep once with the same method
+        first).  See sgb_plan_substep_capturable for the refinement caps."""
+        sp = (spec or RefineSpec()).ctypes()
+        rc = self.L.sgb_plan_substep_capturable(self.handle, method.encode(), phi_exp,
+                                                phi_imp, _ptr(u_in), _ptr(u_out),
+                                                C.byref(sp), _ptr(stream))
+        nat.check(rc, "sgb_plan_substep_capturable")
+
+    def unserved(self) -> int:
+        """Fallback systems of the last capturable 'M' substep that did not
+        fit its complex128 chunk (0 when none; synchronizes)."""
+        n = C.c_int()
+        nat.check(self.L.sgb_plan_unserved(self.handle, C.byref(n)), "sgb_plan_unserved")
+        return n.value
+
     def substep_host(self, method: str, phi_exp: float, phi_imp: float,
                      u_in: np.ndarray, u_out: np.ndarray,
                      spec: RefineSpec | None = None, stream=0) -> None:

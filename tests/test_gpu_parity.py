@@ -647,3 +647,86 @@ def test_tuner_records_a_supported_shape(lib, torch_cuda):
         assert tune.get_shape("C", n, kl, ku) == best
     finally:
         tune.set_shape("C", n, kl, ku, *saved)
+
+
+def _three_substeps(plan_fn, phis, du, spec):
+    """SMR91 substeps 0, 1, 2 in sequence through plan_fn(phi_e, phi_i, u_in, u_out)."""
+    import torch
+    a = du
+    outs = []
+    for phi_e, phi_i in phis:
+        b = torch.empty_like(a)
+        plan_fn(phi_e, phi_i, a, b)
+        outs.append(b)
+        a = b
+    return outs
+
+
+def test_plan_three_substeps_in_a_cuda_graph(lib, torch_cuda):
+    """Three SMR91 substeps recorded into one CUDA graph give the same bits
+    as the ordinary host-driven substeps (the capped refinement makes the
+    same decisions when every system converges within the cap)."""
+    torch = torch_cuda
+    from suzerain_gb300 import plan as P, synth
+    c, cs, kx, kz, u = config0()
+    spec = P.RefineSpec(aiter=5, siter=25, diter=5, tolsc=145.0)
+    dt_beta = c.phi
+    phis = [synth.smr91_phis(dt_beta * synth.SMR91_BETA[i] / synth.SMR91_BETA[0], substep=i)
+            for i in range(3)]
+    pl = P.Plan(cs, kx, kz)
+    du = dev(torch, u)
+    ref = _three_substeps(lambda pe, pi, a, b: pl.substep("M", pe, pi, a, b, spec), phis, du, spec)
+    torch.cuda.synchronize()
+    ref = [r.cpu().numpy() for r in ref]
+    # capture
+    static_in = du.clone()
+    g = torch.cuda.CUDAGraph()
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        pl.substep("M", phis[0][0], phis[0][1], static_in, torch.empty_like(du), spec, stream=s.cuda_stream)
+    torch.cuda.current_stream().wait_stream(s)
+    torch.cuda.synchronize()
+    bufs = [torch.empty_like(du) for _ in range(3)]
+    with torch.cuda.graph(g):
+        st = torch.cuda.current_stream().cuda_stream
+        a = static_in
+        for (pe, pi), b in zip(phis, bufs):
+            pl.substep_capturable("M", pe, pi, a, b, spec, stream=st)
+            a = b
+    static_in.copy_(du)
+    g.replay()
+    torch.cuda.synchronize()
+    for k in range(3):
+        assert np.array_equal(bufs[k].cpu().numpy(), ref[k]), k
+    assert pl.unserved() == 0
+    # a second replay from the same input reproduces the result
+    g.replay()
+    torch.cuda.synchronize()
+    assert np.array_equal(bufs[2].cpu().numpy(), ref[2])
+
+
+def test_plan_capturable_fallback_matches_host_driven(lib, oracle, torch_cuda):
+    """The stress mask (walls on momentum only) sends many systems to the
+    complex128 fallback: the capturable form, with enough fallback slots,
+    reaches the same backward error bar and the same fallback set."""
+    torch = torch_cuda
+    from suzerain_gb300 import plan as P, synth
+    c = synth.Config(**{**synth.CONFIGS[0].__dict__, "dirichlet_mask": synth.DIRICHLET_MOMENTUM})
+    cs, kx, kz, u = c.batch()
+    synth.zero_dirichlet_rows(cs, u)
+    phi_e, phi_i = synth.smr91_phis(c.phi)
+    spec = P.RefineSpec(aiter=5, siter=3, diter=5, tolsc=145.0)
+    pl = P.Plan(cs, kx, kz, max_double_slots=len(kx))
+    du = dev(torch, u)
+    a = torch.zeros_like(du)
+    b = torch.zeros_like(du)
+    pl.substep("M", phi_e, phi_i, du, a, spec)
+    rep_a = pl.report()
+    pl.substep_capturable("M", phi_e, phi_i, du, b, spec)
+    torch.cuda.synchronize()
+    rep_b = pl.report()
+    assert pl.unserved() == 0
+    assert list(rep_a["fact"]) == list(rep_b["fact"])
+    assert np.array_equal(a.cpu().numpy(), b.cpu().numpy())
+    assert pl.backward_error().max() <= 1e-12
