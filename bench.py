@@ -320,6 +320,128 @@ def run_ours(args):
     return 0
 
 
+def run_config3(args) -> int:
+    """Configuration 3: 64 cases of uneven S, Ny, k and wavenumber grid,
+    every case resident (one plan each), factor shapes tuned per geometry,
+    one step = the three SMR91 substeps of every case recorded into one CUDA
+    graph over 8 streams and replayed.  value = system solves per second
+    (each system solved once per substep)."""
+    import torch
+    rank, local, world = dist_env()
+    if world > 1 and rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    from suzerain_gb300 import build as B
+    B.build()
+    from suzerain_gb300 import _native as nat, multicase, plan as P, synth
+    L = nat.load()
+    if L.sgb_device_ok() != 0:
+        raise RuntimeError(nat.last_error())
+    cfgs = synth.config3_cases(args.cases)
+    mc = multicase.MultiCase(cfgs, nstreams=8, max_double_slots=128)
+    tuned = mc.tune("C", nsys=512, reps=1)
+    spec = P.RefineSpec(**SPEC)
+    mc.capture("M", spec)
+    for _ in range(args.warmup):
+        mc.replay()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    sampler = ClockSampler(local)
+    sampler.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        mc.replay()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    ms = e0.elapsed_time(e1)
+    nsys = mc.nsys
+    solves = nsys * mc.nsubsteps * args.steps
+    berr = mc.backward_error()
+    line = {
+        "metric": "system solves/s at rel-resid <=1e-12 (mixed c64 LU + FP64 refinement)",
+        "value": solves / (ms / 1e3), "unit": "systems/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c64 factor + f64 refinement",
+        "data": "synthetic (seeded generator of the reference's shapes)",
+        "config": {"workload": f"config 3: {len(cfgs)} cases, S in {{5,7}}, k in {{6,8}}, "
+                               f"Ny in 32..256, {nsys} systems, {len(mc.geometries())} geometries; "
+                               f"step = 3 SMR91 substeps of every case, one CUDA graph over "
+                               f"8 streams",
+                   "l2": "inputs larger than L2"},
+        "rel_resid_max": float(berr.max()),
+        "unserved": mc.unserved(),
+        "gpu_launches": int(mc.graph_kernels) * args.steps,
+        "tuned_shapes": {f"{k[0]} N={k[1]} KL={k[2]}": list(v) for k, v in tuned.items()},
+        "clocks": clocks,
+        "e2e": None,
+        "device_bytes": mc.device_bytes(),
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_config4(args) -> int:
+    """Configuration 4: a Poisson stream of substep-solve requests with case
+    shapes drawn as in configuration 3 and lifetimes of 3..30 substeps,
+    served by the continuous-batching loop under a 120 GB HBM budget.  The
+    capacity (system solves/s with every request present at t = 0) is
+    measured first; then the arrival rate sweeps 10..90 % of it.  Reports
+    p50/p99 per-substep latency and throughput per level, mixed and plain
+    complex128.  Requests per level are bounded (--requests) so the run ends
+    in minutes; the full 10,000-request levels are --requests 10000."""
+    import torch
+    rank, local, world = dist_env()
+    if world > 1 and rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    from suzerain_gb300 import build as B
+    B.build()
+    from suzerain_gb300 import _native as nat, plan as P, serve, synth
+    L = nat.load()
+    if L.sgb_device_ok() != 0:
+        raise RuntimeError(nat.last_error())
+    spec = P.RefineSpec(**SPEC)
+    pool = synth.config3_cases(64, seed=synth.SEED_BASE + 4)
+    mean_sys = sum(c.nsys for c in pool) / len(pool)
+    out = {}
+    for method, nreq in (("M", args.requests), ("Z", max(4, args.requests // 5))):
+        srv = serve.Server(budget_bytes=120e9, method=method, spec=spec, nstreams=8)
+        # warm-up (kernel attributes, first-touch) and capacity
+        srv.run(serve.poisson_trace(4, 1e9, seed=99, configs=pool, life=(3, 3)))
+        tr = serve.poisson_trace(nreq, 1e9, seed=100, configs=pool)
+        srv.prebuild(tr)
+        cap = srv.run(tr)
+        cap_sps = cap["throughput"]
+        levels = []
+        for lvl in (0.1, 0.3, 0.5, 0.7, 0.9):
+            rate = lvl * cap_sps / (mean_sys * 16.5)      # cases/s
+            tr = serve.poisson_trace(nreq, rate, seed=int(lvl * 1000), configs=pool)
+            srv.prebuild(tr)
+            st = srv.run(tr)
+            levels.append({"load": lvl, "rate_cases_per_s": rate, **st})
+        out[method] = {"capacity_system_solves_per_s": cap_sps, "levels": levels}
+    best = out["M"]["levels"][-1]
+    line = {
+        "metric": "system solves/s under Poisson load (serving), p50/p99 per-substep latency",
+        "value": best["throughput"], "unit": "systems/s", "n_gpus": 1,
+        "steps": best["substeps"], "warmup": 1, "ms_per_step": best["p50_ms"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "c64 factor + f64 refinement",
+        "data": "synthetic (seeded generator of the reference's shapes)",
+        "config": {"workload": f"config 4: Poisson requests, case shapes of config 3, "
+                               f"lifetimes 3..30 substeps, 120 GB budget, {args.requests} "
+                               f"requests per level (mixed), {max(4, args.requests // 5)} "
+                               f"(complex128)"},
+        "p50_ms": best["p50_ms"], "p99_ms": best["p99_ms"],
+        "serving": out,
+        "e2e": None,
+    }
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -334,11 +456,18 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=4096)
     ap.add_argument("--ref-sample", type=int, default=4096)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cases", type=int, default=64, help="configuration 3: number of cases")
+    ap.add_argument("--requests", type=int, default=40,
+                    help="configuration 4: requests per load level (mixed)")
     ap.add_argument("--nsys", type=int, default=0,
                     help="use only the first NSYS systems of the batch (profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.config == 3:
+        return run_config3(args)
+    if args.config == 4:
+        return run_config4(args)
     return run_ours(args)
 
 

@@ -351,6 +351,11 @@ sgb_plan *sgb_plan_create(const sgb_case *host_case, int nsys,
                           const double *kx, const double *kz,
                           int max_double_slots);
 int sgb_plan_destroy(sgb_plan *p);
+/** Device bytes the plan will hold after its first substep of method
+ *  ('M', 'Z', or 0 for both), computed without allocating: admission
+ *  control against a memory budget. */
+size_t sgb_plan_estimate_bytes(const sgb_case *host_case, int nsys, int max_double_slots,
+                               char method);
 /** Device bytes the plan holds. */
 size_t sgb_plan_device_bytes(const sgb_plan *p);
 
@@ -368,7 +373,8 @@ int sgb_plan_substep(sgb_plan *p, char method, double phi_exp, double phi_imp,
 /** sgb_plan_substep in a form that can be recorded into a CUDA graph: no
  *  host synchronization, allocation or host-to-device copy.  Call
  *  sgb_plan_substep once with the same method first (it allocates the
- *  workspace).  Method 'M' runs min(siter + 1, 4) complex64 correction solves
+ *  workspace; sgb_plan_prepare does the allocation alone).  Method 'M' runs
+ *  min(siter + 1, 4) complex64 correction solves
  *  whose grids are bounded by device-side counts (exactly the reference's
  *  bound when siter <= 3; with a larger siter, systems still refining after
  *  four solves move to the complex128 fallback as if siter were exhausted),
@@ -380,6 +386,9 @@ int sgb_plan_substep_capturable(sgb_plan *plan, char method, double phi_exp,
                                 double phi_imp, const void *u_in, void *u_out,
                                 const sgb_refine_spec *spec, void *stream);
 int sgb_plan_unserved(sgb_plan *plan, int *count);
+/** Allocate what the first substep of method ('M', 'Z', or 0 for both)
+ *  would, so that every substep can then take the capturable form. */
+int sgb_plan_prepare(sgb_plan *plan, char method);
 
 /** Same, from and to host memory (copies inside the call). */
 int sgb_plan_substep_host(sgb_plan *p, char method, double phi_exp,

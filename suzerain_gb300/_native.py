@@ -132,6 +132,8 @@ _SIGS = {
     "sgb_plan_substep_capturable": (_i, [_p, C.c_char, _d, _d, _p, _p,
                                          C.POINTER(RefineSpec), _p]),
     "sgb_plan_unserved": (_i, [_p, _p]),
+    "sgb_plan_prepare": (_i, [_p, C.c_char]),
+    "sgb_plan_estimate_bytes": (C.c_size_t, [_p, _i, _i, C.c_char]),
     "sgb_plan_report": (_i, [_p, _p, _p, _p, _p, _p, _p]),
     "sgb_plan_backward_error": (_i, [_p, _p, _p]),
     "sgb_plan_set_timing": (_i, [_p, _i]),

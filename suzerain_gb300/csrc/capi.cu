@@ -453,6 +453,58 @@ extern "C" int sgb_plan_destroy(sgb_plan *p)
 
 extern "C" size_t sgb_plan_device_bytes(const sgb_plan *p) { return p ? p->dev_bytes : 0; }
 
+// Device bytes a plan holds once it has run the given method ('M', 'Z' or 0
+// for both): the allocations of sgb_plan_create plus those of the first
+// substep, so that a caller can admit work against a memory budget before
+// creating the plan.  Each allocation is rounded up to 256 bytes.
+extern "C" size_t sgb_plan_estimate_bytes(const sgb_case *c, int nsys, int max_double_slots,
+                                          char method)
+{
+    if (!c || nsys < 1 || c->S < 1 || c->n < 2) return 0;
+    auto up = [](size_t b) { return (b + 255) & ~size_t(255); };
+    const int N = c->S * c->n, KL = c->S * (c->kl + 1) - 1, KU = c->S * (c->ku + 1) - 1;
+    const size_t nb = (size_t) c->ld * c->n, SS = (size_t) c->S * c->S;
+    FactorGeom g{N, KL, KU};
+    size_t b = up(3 * nb * sizeof(double)) + up(nb * sizeof(float4)) + up(4 * SS * sizeof(double))
+             + 2 * up(nsys * sizeof(double)) + up(18 * sizeof(double))
+             + 2 * up((size_t) nsys * N * sizeof(double2));
+    method = (char) toupper(method);
+    if (method == 'Z' || method == 0)
+        b += up((size_t) nsys * g.fac_elems() * sizeof(double2)) + up((size_t) nsys * N * sizeof(int))
+           + up(nsys * sizeof(int)) + up((size_t) nsys * N * sizeof(double2));
+    if (method == 'M' || method == 0) {
+        RefineProblem P;
+        P.nsys = nsys; P.g = g;
+        P.nslot64 = std::max(1, std::min(nsys, max_double_slots > 0 ? max_double_slots : nsys));
+        b += up(refine_workspace_bytes(P));
+    }
+    return b;
+}
+
+static int plan_alloc_z(sgb_plan *p)
+{
+    const int nsys = p->nsys, N = p->N;
+    FactorGeom g{N, p->KL, p->KU};
+    int rc = p->dalloc(&p->fac64, (size_t) nsys * g.fac_elems() * sizeof(double2), "cudaMalloc(fac64)");
+    rc |= p->dalloc((void **) &p->ipiv64, (size_t) nsys * N * sizeof(int), "cudaMalloc(ipiv64)");
+    rc |= p->dalloc((void **) &p->info64, (size_t) nsys * sizeof(int), "cudaMalloc(info64)");
+    rc |= p->dalloc((void **) &p->y64, (size_t) nsys * N * sizeof(double2), "cudaMalloc(y64)");
+    return rc;
+}
+
+// The refinement workspace depends only on (nsys, geometry, fallback slots).
+static int plan_alloc_m(sgb_plan *p)
+{
+    RefineProblem P;
+    P.nsys = p->nsys; P.g = {p->N, p->KL, p->KU}; P.nslot64 = p->nslot64;
+    const size_t need = refine_workspace_bytes(P);
+    if (need <= p->rws_bytes) return 0;
+    int rc = p->dalloc(&p->rws, need, "cudaMalloc(refine workspace)");
+    if (rc) return rc;
+    p->rws_bytes = need;
+    return 0;
+}
+
 // capturable: no host synchronization, no allocation, no host-to-device copy
 // (the refinement runs its capped, device-counted form), so the call can be
 // recorded into a CUDA graph after one ordinary call of the same method.
@@ -485,10 +537,7 @@ static int plan_substep(sgb_plan *p, char method, double phi_exp, double phi_imp
         if (!p->fac64 && capturable)
             return fail("sgb_plan_substep_capturable: run sgb_plan_substep with method 'Z' first");
         if (!p->fac64) {
-            int rc = p->dalloc(&p->fac64, (size_t) nsys * g.fac_elems() * sizeof(double2), "cudaMalloc(fac64)");
-            rc |= p->dalloc((void **) &p->ipiv64, (size_t) nsys * N * sizeof(int), "cudaMalloc(ipiv64)");
-            rc |= p->dalloc((void **) &p->info64, (size_t) nsys * sizeof(int), "cudaMalloc(info64)");
-            rc |= p->dalloc((void **) &p->y64, (size_t) nsys * N * sizeof(double2), "cudaMalloc(y64)");
+            int rc = plan_alloc_z(p);
             if (rc) return rc;
         }
         GbtrfArgs fa;
@@ -524,11 +573,11 @@ static int plan_substep(sgb_plan *p, char method, double phi_exp, double phi_imp
         }
         const size_t need = refine_workspace_bytes(P);
         if (need > p->rws_bytes && capturable)
-            return fail("sgb_plan_substep_capturable: run sgb_plan_substep with method 'M' first");
+            return fail("sgb_plan_substep_capturable: run sgb_plan_substep or sgb_plan_prepare "
+                        "with method 'M' first");
         if (need > p->rws_bytes) {
-            int rc = p->dalloc(&p->rws, need, "cudaMalloc(refine workspace)");
+            int rc = plan_alloc_m(p);
             if (rc) return rc;
-            p->rws_bytes = need;
         }
         int rc = refine_batched(P, p->rws, p->rws_bytes, p->last, st);
         if (rc) return sgb_set_error((cudaError_t) rc, "refine_batched", __FILE__, __LINE__);
@@ -588,6 +637,21 @@ extern "C" int sgb_plan_substep_capturable(sgb_plan *p, char method, double phi_
     std::lock_guard<std::mutex> lk(p->mu);
     return plan_substep(p, (char) toupper(method), phi_exp, phi_imp, u_in, u_out, spec,
                         (cudaStream_t) stream, true);
+}
+
+extern "C" int sgb_plan_prepare(sgb_plan *p, char method)
+{
+    if (!p) return fail("sgb_plan_prepare: null plan");
+    std::lock_guard<std::mutex> lk(p->mu);
+    method = (char) toupper(method);
+    if (method != 'M' && method != 'Z' && method != 0)
+        return fail("sgb_plan_prepare: method must be 'M', 'Z' or 0");
+    if ((method == 'Z' || method == 0) && !p->fac64) {
+        int rc = plan_alloc_z(p);
+        if (rc) return rc;
+    }
+    if (method == 'M' || method == 0) return plan_alloc_m(p);
+    return 0;
 }
 
 extern "C" int sgb_plan_unserved(sgb_plan *p, int *count)

@@ -67,6 +67,16 @@ class Plan:
     def device_bytes(self) -> int:
         return int(self.L.sgb_plan_device_bytes(self.handle))
 
+    @staticmethod
+    def estimate_bytes(case: SynthCase, nsys: int, max_double_slots: int = 0,
+                       method: str = "M") -> int:
+        """Device bytes a plan of this case holds after its first substep of
+        `method` (without creating it)."""
+        L = nat.load()
+        cs = case.ctypes_case()
+        return int(L.sgb_plan_estimate_bytes(C.byref(cs), int(nsys), int(max_double_slots),
+                                             method.encode()))
+
     def substep(self, method: str, phi_exp: float, phi_imp: float, u_in, u_out,
                 spec: RefineSpec | None = None, stream=0) -> None:
         sp = (spec or RefineSpec()).ctypes()
@@ -85,6 +95,11 @@ class Plan:
                                                 phi_imp, _ptr(u_in), _ptr(u_out),
                                                 C.byref(sp), _ptr(stream))
         nat.check(rc, "sgb_plan_substep_capturable")
+
+    def prepare(self, method: str = "M") -> None:
+        """Allocate what the first substep of `method` would (then every
+        substep may take the capturable form)."""
+        nat.check(self.L.sgb_plan_prepare(self.handle, method.encode()), "sgb_plan_prepare")
 
     def unserved(self) -> int:
         """Fallback systems of the last capturable 'M' substep that did not

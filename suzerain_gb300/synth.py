@@ -17,7 +17,7 @@ from . import _native as nat
 
 SEED_BASE = 0x5A2E0000
 DIRICHLET_MOMENTUM = 0b01110   # momentum equations 1..3 only (near-singular stress case)
-DIRICHLET_ALL = 0b11111        # every second-order equation gets its two wall rows
+DIRICHLET_ALL = 0xFFFFFFFF     # every equation (any S) gets its two wall rows
 
 
 @dataclass
@@ -191,3 +191,24 @@ def smr91_phis(dt_beta: float, substep: int = 0, explicit: bool = True):
     explicit=False returns phi_explicit = 0 (solve-only step)."""
     dt = dt_beta / SMR91_BETA[substep]
     return (dt * SMR91_ALPHA[substep] if explicit else 0.0), -dt_beta
+
+
+# Configuration 3: 64 independent cases of uneven size.  Ny uniform on
+# {32, 48, ..., 256}, spline order k on {6, 8}, S on {5, 7} (S = 7: the perfect
+# gas plus two species with the same block generator), (Nx, Nz) on
+# {(32, 32), (64, 48), (128, 96)}, all drawn from one seeded generator.
+CONFIG3_NY = tuple(range(32, 257, 16))
+CONFIG3_GRIDS = ((32, 32), (64, 48), (128, 96))
+
+
+def config3_cases(ncases: int = 64, seed: int = SEED_BASE + 3) -> list[Config]:
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(ncases):
+        Ny = int(rng.choice(CONFIG3_NY))
+        k = int(rng.choice((6, 8)))
+        S = int(rng.choice((5, 7)))
+        Nx, Nz = CONFIG3_GRIDS[int(rng.integers(len(CONFIG3_GRIDS)))]
+        out.append(Config(f"config3-case{i}", S, Ny, k, Nx, Nz, FOURPI, FOURPI / 3, 1e-3,
+                          seed=seed * 1000 + i))
+    return out

@@ -730,3 +730,66 @@ def test_plan_capturable_fallback_matches_host_driven(lib, oracle, torch_cuda):
     assert list(rep_a["fact"]) == list(rep_b["fact"])
     assert np.array_equal(a.cpu().numpy(), b.cpu().numpy())
     assert pl.backward_error().max() <= 1e-12
+
+
+def test_multicase_graph_matches_eager(lib, torch_cuda):
+    """Cases of uneven S, Ny, k and grid, spread over streams and recorded
+    into one CUDA graph per step, give the same bits as the host-driven step;
+    each case's result does not depend on the other cases."""
+    torch = torch_cuda
+    from suzerain_gb300 import multicase, plan as P, synth
+    cfgs = [synth.Config("a", 5, 48, 6, 8, 8, synth.FOURPI, synth.FOURPI / 3, 1e-3, seed=11),
+            synth.Config("b", 7, 64, 8, 8, 6, synth.FOURPI, synth.FOURPI / 3, 1e-3, seed=12),
+            synth.Config("c", 5, 96, 8, 16, 8, synth.FOURPI, synth.FOURPI / 3, 1e-3, seed=13)]
+    # siter = 3: the capturable form's complex64 bound (siter + 1 solves) is
+    # then the reference's own, so graph and host-driven runs agree bit for bit
+    spec = P.RefineSpec(aiter=5, siter=3, diter=5, tolsc=145.0)
+    mc = multicase.MultiCase(cfgs, nstreams=2)
+    mc.step_eager("M", spec)
+    torch.cuda.synchronize()
+    eager = [mc.result(i).cpu().numpy() for i in range(len(cfgs))]
+    assert mc.backward_error().max() <= 1e-12
+    mc.capture("M", spec)
+    mc.reset()
+    mc.replay()
+    torch.cuda.synchronize()
+    for i in range(len(cfgs)):
+        assert np.array_equal(mc.result(i).cpu().numpy(), eager[i]), i
+    assert mc.unserved() == 0
+    # the same case alone
+    solo = multicase.MultiCase(cfgs[1:2], nstreams=1)
+    solo.step_eager("M", spec)
+    torch.cuda.synchronize()
+    assert np.array_equal(solo.result(0).cpu().numpy(), eager[1])
+    # the production spec (siter = 25, capped at four solves in the graph)
+    # still meets the backward error bar
+    mc2 = multicase.MultiCase(cfgs, nstreams=2)
+    mc2.capture("M", P.RefineSpec(aiter=5, siter=25, diter=5, tolsc=145.0))
+    mc2.replay()
+    torch.cuda.synchronize()
+    assert mc2.backward_error().max() <= 1e-12 and mc2.unserved() == 0
+
+
+def test_serving_result_same_alone_and_in_the_mix(lib, torch_cuda):
+    """Continuous batching: requests that arrive while others run are
+    admitted under the memory budget and overlap on the device; each
+    request's final state is the same bits alone and in the mix."""
+    torch = torch_cuda
+    from suzerain_gb300 import serve, synth, plan as P
+    pool = [synth.Config("s0", 5, 48, 6, 8, 8, synth.FOURPI, synth.FOURPI / 3, 1e-3, seed=21),
+            synth.Config("s1", 7, 32, 8, 8, 6, synth.FOURPI, synth.FOURPI / 3, 1e-3, seed=22),
+            synth.Config("s2", 5, 64, 8, 16, 8, synth.FOURPI, synth.FOURPI / 3, 1e-3, seed=23)]
+    trace = serve.poisson_trace(8, rate=200.0, seed=5, configs=pool, life=(3, 6))
+    srv = serve.Server(budget_bytes=2e9, nstreams=4, keep_results=True)
+    stats = srv.run(trace)
+    assert stats["substeps"] == sum(r.nsubsteps for r in trace)
+    assert stats["p99_ms"] >= stats["p50_ms"] > 0
+    for r in trace[:3]:
+        alone = serve.Server(budget_bytes=2e9, nstreams=1, keep_results=True)
+        alone.run([serve.Request(r.rid, r.config, r.nsubsteps, 0.0)])
+        assert np.array_equal(alone.results[r.rid], srv.results[r.rid]), r.rid
+    # a budget that fits one case at a time still serves everything
+    one = P.Plan.estimate_bytes(pool[2].case(), pool[2].nsys, 128, "M") + 2 * pool[2].nsys * 320 * 16
+    tight = serve.Server(budget_bytes=one * 1.01, nstreams=2)
+    st2 = tight.run(serve.poisson_trace(4, rate=500.0, seed=6, configs=pool, life=(3, 3)))
+    assert st2["substeps"] == 12 and st2["peak_resident_cases"] >= 1
