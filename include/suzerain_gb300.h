@@ -222,6 +222,25 @@ int suzerain_diffwave_apply(const int dxcnt, const int dzcnt,
                             const int Nz, const int dNz, const int dkbz,
                             const int dkez);
 
+/** Solver specification (suzerain/specification_zgbsv.hpp:44-140): the
+ *  method and the zcgbsvx refinement parameters.  Defaults (empty string):
+ *  zcgbsvx, equil = reuse = false, aiter = 1, siter = -1, diter = 5,
+ *  tolsc = 0 (suzerain/specification_zgbsv.cpp:46-54). */
+enum { SGB_METHOD_ZGBSV = 1, SGB_METHOD_ZGBSVX = 2, SGB_METHOD_ZCGBSVX = 3 };
+typedef struct sgb_solver_spec {
+    int method, equil, reuse, aiter, siter, diter;
+    double tolsc;
+} sgb_solver_spec;
+void sgb_solver_spec_default(sgb_solver_spec *s);
+/** Parse "zgbsv" | "zgbsvx[,equil=B]" | "zcgbsvx[,reuse=B][,aiter=I][,siter=I]
+ *  [,diter=I][,tolsc=D]" (options in any order, each once; keywords
+ *  case-insensitive; whitespace anywhere between tokens), the grammar of
+ *  suzerain/specification_zgbsv.cpp:56-104.  Returns 0, or -1 with the
+ *  reference's message ("... invalid beginning with '...'") in err. */
+int sgb_solver_spec_parse(const char *spec, sgb_solver_spec *out, char *err, size_t errlen);
+/** The reference's canonical string (suzerain/specification_zgbsv.cpp:128-155). */
+int sgb_solver_spec_format(const sgb_solver_spec *s, char *buf, size_t len);
+
 /* ======================================================================== */
 /* 2. Batched device API                                                    */
 /* ======================================================================== */

@@ -133,6 +133,9 @@ _SIGS = {
                                          C.POINTER(RefineSpec), _p]),
     "sgb_plan_unserved": (_i, [_p, _p]),
     "sgb_plan_prepare": (_i, [_p, C.c_char]),
+    "sgb_solver_spec_default": (None, [_p]),
+    "sgb_solver_spec_parse": (_i, [C.c_char_p, _p, _p, C.c_size_t]),
+    "sgb_solver_spec_format": (_i, [_p, _p, C.c_size_t]),
     "sgb_plan_estimate_bytes": (C.c_size_t, [_p, _i, _i, C.c_char]),
     "sgb_plan_report": (_i, [_p, _p, _p, _p, _p, _p, _p]),
     "sgb_plan_backward_error": (_i, [_p, _p, _p]),

@@ -35,8 +35,52 @@ class RefineSpec:
         return nat.RefineSpec(self.aiter, self.siter, self.diter, self.tolsc)
 
     @classmethod
-    def from_spec(cls, spec) -> "RefineSpec":
-        return cls(spec.aiter(), spec.siter(), spec.diter(), spec.tolsc())
+    def from_string(cls, text: str) -> "RefineSpec":
+        """From a reference solver specification string (its zcgbsvx fields;
+        see SolverSpec)."""
+        s = SolverSpec(text)
+        return cls(s.aiter, s.siter, s.diter, s.tolsc)
+
+
+class _SpecStruct(C.Structure):
+    _fields_ = [("method", C.c_int), ("equil", C.c_int), ("reuse", C.c_int),
+                ("aiter", C.c_int), ("siter", C.c_int), ("diter", C.c_int),
+                ("tolsc", C.c_double)]
+
+
+class SolverSpec:
+    """suzerain::specification_zgbsv: parse a specification string with the
+    reference's grammar and defaults; str() gives its canonical form."""
+    METHODS = {1: "zgbsv", 2: "zgbsvx", 3: "zcgbsvx"}
+
+    def __init__(self, text: str = ""):
+        L = nat.load()
+        self._s = _SpecStruct()
+        err = C.create_string_buffer(512)
+        if L.sgb_solver_spec_parse(text.encode(), C.byref(self._s), err, len(err)) != 0:
+            raise ValueError(err.value.decode())
+
+    def __getattr__(self, name):
+        if name in ("equil", "reuse"):
+            return bool(getattr(self._s, name))
+        if name in ("aiter", "siter", "diter", "tolsc"):
+            return getattr(self._s, name)
+        if name == "method":
+            return self.METHODS.get(self._s.method, "UNKNOWN")
+        raise AttributeError(name)
+
+    def __str__(self) -> str:
+        buf = C.create_string_buffer(256)
+        nat.check(nat.load().sgb_solver_spec_format(C.byref(self._s), buf, len(buf)),
+                  "sgb_solver_spec_format")
+        return buf.value.decode()
+
+    def __eq__(self, other) -> bool:
+        return isinstance(other, SolverSpec) and bytes(self._s) == bytes(other._s)
+
+    def in_place(self) -> bool:
+        """zgbsv factors in place (packf storage); the others do not."""
+        return self.method == "zgbsv"
 
 
 class Plan:

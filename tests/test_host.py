@@ -142,3 +142,35 @@ def test_synth_deterministic_and_config_geometry(native):
     off = cs.a.reshape(5, 5)[~np.eye(5, dtype=bool)]
     assert (np.abs(off) <= 0.1).all()
     assert native.suzerain_inorder_wavenumber(24, 13) == -11
+
+
+def test_solver_spec_grammar_matches_reference_cases(native):
+    """The cases of the reference's tests/test_specification_zgbsv.cpp."""
+    from suzerain_gb300.plan import SolverSpec, RefineSpec
+    d = SolverSpec()
+    assert str(d) != "UNKNOWN" and d.method == "zcgbsvx"
+    assert (d.aiter, d.siter, d.diter, d.tolsc, d.reuse) == (1, -1, 5, 0.0, False)
+    e = SolverSpec(" ")
+    assert str(e) not in ("", "UNKNOWN") and e == d
+    z = SolverSpec("zgbsv")
+    assert z.method == "zgbsv" and str(z) == "zgbsv" and z.in_place()
+    x = SolverSpec("zgbsvx")
+    assert x.method == "zgbsvx" and str(x) == "zgbsvx,equil=false"
+    X = SolverSpec("ZGBSVX,EQUIL=TRUE")
+    assert X.method == "zgbsvx" and str(X) == "zgbsvx,equil=true"
+    c = SolverSpec("zcgbsvx")
+    assert c.method == "zcgbsvx" and str(c) != "zcgbsvx"
+    text = "zcgbsvx,reuse=true,aiter=2,siter=3,diter=4,tolsc=5"
+    r = SolverSpec(text)
+    assert (r.reuse, r.aiter, r.siter, r.diter, r.tolsc) == (True, 2, 3, 4, 5.0)
+    assert str(r) == text
+    a = SolverSpec("zcgbsvx , reuse = true\t\n,\t\nAITER=\t \t2")
+    b = SolverSpec("zcgbsvx,reuse=true,aiter=2")
+    cc = SolverSpec("zcgbsvx,aiter=2,reuse=true")
+    assert a == b and b == cc and a == cc
+    for bad in ("zgbsvq", "zcgbsvx,aiter=2,aiter=3", "zcgbsvx,reuse=maybe", "zgbsv,equil=true",
+                "zcgbsvx,tolsc=", "lu"):
+        with pytest.raises(ValueError, match="invalid beginning with"):
+            SolverSpec(bad)
+    rs = RefineSpec.from_string("zcgbsvx,aiter=5,siter=25,diter=5,tolsc=145")
+    assert (rs.aiter, rs.siter, rs.diter, rs.tolsc) == (5, 25, 5, 145.0)
