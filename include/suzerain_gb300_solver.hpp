@@ -1,0 +1,290 @@
+// Header-only C++ counterpart of suzerain::bsmbsm_solver
+// (suzerain/bsmbsm_solver.hpp:70-330, suzerain/bsmbsm_solver.cpp:58-414) over
+// the C ABI of suzerain_gb300.h: the same protocol (supply_b/B -> optional
+// supplied_PAPT()/apprx() -> solve -> demand_x/X), the same storage roles
+// (LU, PAPT, PB, PX, ipiv; column-major, PAPT in bsmbsm packed band order),
+// the same specification strings and the same error messages.  The solves run
+// on the GPU through the drop-in entry points (suzerain_lapackext_zgbsv,
+// suzerain_lapackext_zcgbsvx); the storage here is host memory, as the
+// reference's Eigen members are.
+//
+// Differences: errors throw std::runtime_error (the reference calls
+// SUZERAIN_ERROR, whose default handler aborts); the zgbsvx method (the
+// equilibrating expert driver) is not provided and build() rejects it.
+#ifndef SUZERAIN_GB300_SOLVER_HPP
+#define SUZERAIN_GB300_SOLVER_HPP
+
+#include <algorithm>
+#include <cctype>
+#include <complex>
+#include <cstdio>
+#include <limits>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "suzerain_gb300.h"
+
+namespace suzerain_gb300 {
+
+/** A solver specification string with the reference's grammar. */
+class specification_zgbsv {
+public:
+    explicit specification_zgbsv(const std::string &text = "")
+    {
+        char err[512];
+        if (sgb_solver_spec_parse(text.c_str(), &s_, err, sizeof err) != 0)
+            throw std::invalid_argument(err);
+    }
+    int method() const { return s_.method; }
+    bool equil() const { return s_.equil != 0; }
+    bool reuse() const { return s_.reuse != 0; }
+    int aiter() const { return s_.aiter; }
+    int siter() const { return s_.siter; }
+    int diter() const { return s_.diter; }
+    double tolsc() const { return s_.tolsc; }
+    bool in_place() const { return s_.method == SGB_METHOD_ZGBSV; }
+    const char *mname() const
+    {
+        switch (s_.method) {
+        case SGB_METHOD_ZGBSV: return "suzerain_lapackext_zgbsv";
+        case SGB_METHOD_ZGBSVX: return "suzerain_lapack_zgbsvx";
+        case SGB_METHOD_ZCGBSVX: return "suzerain_lapackext_zcgbsvx";
+        default: return "UNKNOWN";
+        }
+    }
+    operator std::string() const
+    {
+        char buf[256];
+        sgb_solver_spec_format(&s_, buf, sizeof buf);
+        return buf;
+    }
+
+private:
+    sgb_solver_spec s_;
+};
+
+class bsmbsm_solver {
+public:
+    using complex_double = std::complex<double>;
+
+    virtual ~bsmbsm_solver() = default;
+
+    /** zgbsv or zcgbsvx per the specification (nrhs right hand sides). */
+    static std::unique_ptr<bsmbsm_solver> build(const suzerain_bsmbsm &A,
+                                                const specification_zgbsv &spec, int nrhs);
+
+    const suzerain_bsmbsm A;
+    const specification_zgbsv spec;
+
+    // Storage (column-major).  PAPT is the packed band P A P^T with leading
+    // dimension ld_PAPT() (KL + LD for the in-place zgbsv, LD otherwise);
+    // callers fill it (e.g. with suzerain_bsmbsm_zpackc/zpackf) and call
+    // supplied_PAPT().
+    std::vector<complex_double> LU, PB;
+    std::vector<int> ipiv;
+    complex_double *PAPT() { return PAPT_; }
+    int ld_PAPT() const { return ld_PAPT_; }
+    complex_double *PX() { return PX_; }
+    int nrhs() const { return nrhs_; }
+
+    /** PB(:, j) = P b */
+    int supply_b(const complex_double *b, int j, int incb = 1)
+    {
+        check_col(j);
+        return suzerain_bsmbsm_zaPxpby('N', A.S, A.n, complex_double(1), b, incb,
+                                       complex_double(0), PB.data() + (size_t) j * A.N, 1);
+    }
+    int supply_B(const complex_double *B, int ldB, int incB = 1)
+    {
+        int info = 0;
+        for (int j = 0; !info && j < nrhs_; ++j) info = supply_b(B + (size_t) j * ldB, j, incB);
+        return info;
+    }
+    int supply_B(const complex_double *B) { return supply_B(B, A.N, 1); }
+
+    char fact() const { return fact_; }
+    char default_fact() const { return spec.equil() ? 'E' : 'N'; }
+    bool apprx() const { return apprx_ != 0; }
+
+    /** PAPT was (re)written: refactor on the next solve, or, when the
+     *  specification allows reuse, keep the factor as an approximation. */
+    virtual bsmbsm_solver &supplied_PAPT()
+    {
+        if (spec.reuse()) apprx_ = fact_ != default_fact();
+        else fact_ = default_fact();
+        return *this;
+    }
+    /** Whether a reused factor is still acceptable; returns the old flag. */
+    bool apprx(bool acceptable)
+    {
+        const bool old = apprx_ != 0;
+        if (spec.reuse()) {
+            apprx_ = (apprx_ && acceptable) ? 1 : 0;
+            if (!apprx_) fact_ = default_fact();
+        }
+        return old;
+    }
+
+    int solve(char trans, int nrhs)
+    {
+        if (nrhs == 0) return 0;
+        if (nrhs < 1 || nrhs > nrhs_) throw std::invalid_argument("Invalid nrhs supplied to solve()");
+        const int info = solve_hook(trans, nrhs);
+        if (info == 0) return 0;
+        char buf[256];
+        if (info < 0)
+            std::snprintf(buf, sizeof buf, "%s reported error in argument %d", spec.mname(), -info);
+        else if (info <= A.N)
+            std::snprintf(buf, sizeof buf,
+                          "%s reported singularity in PAP^T row %d corresponding to A row %d"
+                          " for state scalar %d",
+                          spec.mname(), info - 1, suzerain_bsmbsm_q(A.S, A.n, info - 1),
+                          suzerain_bsmbsm_q(A.S, A.n, info - 1) / A.n);
+        else
+            std::snprintf(buf, sizeof buf, "%s reported unknown error %d", spec.mname(), info);
+        throw std::runtime_error(buf);
+    }
+    int solve(char trans) { return solve(trans, nrhs_); }
+
+    /** x = P^T PX(:, j) */
+    int demand_x(complex_double *x, int j, int incx = 1) const
+    {
+        check_col(j);
+        return suzerain_bsmbsm_zaPxpby('T', A.S, A.n, complex_double(1),
+                                       PX_ + (size_t) j * A.N, 1, complex_double(0), x, incx);
+    }
+    int demand_X(complex_double *X, int ldX, int incX = 1) const
+    {
+        int info = 0;
+        for (int j = 0; !info && j < nrhs_; ++j) info = demand_x(X + (size_t) j * ldX, j, incX);
+        return info;
+    }
+    int demand_X(complex_double *X) const { return demand_X(X, A.N, 1); }
+
+    virtual std::vector<std::string> summarize_statistics() const
+    {
+        return {"Employed bsmbsm_solver per specification " + std::string(spec)};
+    }
+
+protected:
+    bsmbsm_solver(const suzerain_bsmbsm &a, const specification_zgbsv &s, int nrhs)
+        : A(a), spec(s), PB((size_t) a.N * nrhs), ipiv(a.N), nrhs_(nrhs),
+          fact_(s.equil() ? 'E' : 'N'), apprx_(0)
+    {
+        if (nrhs < 1) throw std::invalid_argument("nrhs must be positive");
+    }
+    virtual int solve_hook(char trans, int nrhs) = 0;
+    void check_col(int j) const
+    {
+        if (j < 0 || j >= nrhs_) throw std::out_of_range("right hand side column");
+    }
+
+    complex_double *PAPT_ = nullptr, *PX_ = nullptr;
+    int ld_PAPT_ = 0;
+    int nrhs_;
+    char fact_;
+    int apprx_;
+};
+
+/** Plain complex128 band LU, in place: LU is (KL + LD) x N, PAPT aliases its
+ *  rows KL.., PX aliases PB (suzerain/bsmbsm_solver.cpp:155-182). */
+class bsmbsm_solver_zgbsv : public bsmbsm_solver {
+public:
+    bsmbsm_solver_zgbsv(const suzerain_bsmbsm &a, const specification_zgbsv &s, int nrhs)
+        : bsmbsm_solver(a, s, nrhs)
+    {
+        if (!s.in_place()) throw std::invalid_argument("Invalid method in bsmbsm_solver_zgbsv");
+        LU.assign((size_t) (a.KL + a.LD) * a.N,
+                  complex_double(std::numeric_limits<double>::quiet_NaN()));
+        ld_PAPT_ = a.KL + a.LD;
+        PAPT_ = LU.data() + a.KL;
+        PX_ = PB.data();
+    }
+
+protected:
+    int solve_hook(char trans, int nrhs) override
+    {
+        return suzerain_lapackext_zgbsv(&fact_, trans, A.N, A.KL, A.KU, nrhs, LU.data(),
+                                        A.KL + A.LD, ipiv.data(), PB.data(), A.N);
+    }
+};
+
+/** Complex64 factor + complex128 refinement, out of place: PAPT is LD x N,
+ *  LU (2KL + KU + 1) x N holds the factor (suzerain/bsmbsm_solver.cpp:293-414).
+ *  Every right hand side runs the driver with the specification's siter,
+ *  diter, tolsc and records them with fact, apprx, afrob and res. */
+class bsmbsm_solver_zcgbsvx : public bsmbsm_solver {
+public:
+    struct stat { char fact; int apprx; double afrob; int siter, diter; double tolsc, res; };
+    std::vector<stat> stats;
+
+    bsmbsm_solver_zcgbsvx(const suzerain_bsmbsm &a, const specification_zgbsv &s, int nrhs)
+        : bsmbsm_solver(a, s, nrhs), papt_((size_t) a.LD * a.N), px_((size_t) a.N * nrhs), r_(a.N)
+    {
+        if (s.method() != SGB_METHOD_ZCGBSVX)
+            throw std::invalid_argument("Invalid method in bsmbsm_solver_zcgbsvx");
+        LU.assign((size_t) (2 * a.KL + a.KU + 1) * a.N, complex_double(0));
+        ld_PAPT_ = a.LD;
+        PAPT_ = papt_.data();
+        PX_ = px_.data();
+    }
+    bsmbsm_solver &supplied_PAPT() override
+    {
+        afrob_ = -1;
+        return bsmbsm_solver::supplied_PAPT();
+    }
+    std::vector<std::string> summarize_statistics() const override
+    {
+        auto out = bsmbsm_solver::summarize_statistics();
+        if (!stats.empty()) {
+            int s = 0, d = 0;
+            double t = 0;
+            for (const stat &x : stats) { s += x.siter; d += x.diter; t = std::max(t, x.tolsc); }
+            char buf[256];
+            std::snprintf(buf, sizeof buf, "solves %zu, mean siter %.3g, mean diter %.3g, max tolsc %.3g",
+                          stats.size(), (double) s / stats.size(), (double) d / stats.size(), t);
+            out.push_back(buf);
+        }
+        return out;
+    }
+
+protected:
+    int solve_hook(char trans, int nrhs) override
+    {
+        int info = 0;
+        for (int j = 0; !info && j < nrhs; ++j) {
+            int siter = spec.siter(), diter = spec.diter();
+            double tolsc = spec.tolsc(), res = 0;
+            info = suzerain_lapackext_zcgbsvx(&fact_, &apprx_, spec.aiter(), trans, A.N, A.KL, A.KU,
+                                              PAPT_, &afrob_, LU.data(), ipiv.data(),
+                                              PB.data() + (size_t) j * A.N,
+                                              PX_ + (size_t) j * A.N, &siter, &diter, &tolsc,
+                                              r_.data(), &res);
+            stats.push_back({fact_, apprx_, afrob_, siter, diter, tolsc, res});
+        }
+        return info;
+    }
+
+private:
+    std::vector<complex_double> papt_, px_, r_;
+    double afrob_ = -1;
+};
+
+inline std::unique_ptr<bsmbsm_solver> bsmbsm_solver::build(const suzerain_bsmbsm &A,
+                                                           const specification_zgbsv &spec,
+                                                           int nrhs)
+{
+    switch (spec.method()) {
+    case SGB_METHOD_ZGBSV: return std::make_unique<bsmbsm_solver_zgbsv>(A, spec, nrhs);
+    case SGB_METHOD_ZCGBSVX: return std::make_unique<bsmbsm_solver_zcgbsvx>(A, spec, nrhs);
+    default:
+        throw std::invalid_argument(std::string("bsmbsm_solver::build: method not provided: ") +
+                                    std::string(spec));
+    }
+}
+
+}  // namespace suzerain_gb300
+
+#endif  // SUZERAIN_GB300_SOLVER_HPP

@@ -793,3 +793,24 @@ def test_serving_result_same_alone_and_in_the_mix(lib, torch_cuda):
     tight = serve.Server(budget_bytes=one * 1.01, nstreams=2)
     st2 = tight.run(serve.poisson_trace(4, rate=500.0, seed=6, configs=pool, life=(3, 3)))
     assert st2["substeps"] == 12 and st2["peak_resident_cases"] >= 1
+
+
+def test_cpp_solver_shim_runs(lib, tmp_path):
+    """The header-only C++ bsmbsm_solver counterpart, linked against the
+    library, packs S x S banded blocks, solves with the zgbsv and zcgbsvx
+    specifications on the GPU and meets A x = b (dense check)."""
+    import shutil
+    import subprocess
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("no g++")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    libdir = os.path.join(root, "suzerain_gb300", "_lib")
+    exe = str(tmp_path / "shim")
+    r = subprocess.run([gxx, "-std=c++17", "-O1", "-I", os.path.join(root, "include"),
+                        os.path.join(root, "tests", "solver_shim_check.cpp"), "-L", libdir,
+                        "-lsuzerain_gb300", "-Wl,-rpath," + libdir, "-o", exe],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0 and "OK" in r.stdout, r.stdout + r.stderr

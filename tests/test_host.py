@@ -174,3 +174,19 @@ def test_solver_spec_grammar_matches_reference_cases(native):
             SolverSpec(bad)
     rs = RefineSpec.from_string("zcgbsvx,aiter=5,siter=25,diter=5,tolsc=145")
     assert (rs.aiter, rs.siter, rs.diter, rs.tolsc) == (5, 25, 5, 145.0)
+
+
+def test_cpp_solver_shim_compiles(tmp_path):
+    """The header-only C++ solver shim compiles against the C ABI header
+    (C++17, warnings as errors)."""
+    import shutil
+    import subprocess
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("no g++")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([gxx, "-std=c++17", "-Wall", "-Wextra", "-Werror", "-fsyntax-only",
+                        "-I", os.path.join(root, "include"),
+                        os.path.join(root, "tests", "solver_shim_check.cpp")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
