@@ -276,11 +276,12 @@ int sgb_gbtrf_batched_ex(char prec, int nsys, int N, int KL, int KU,
                          void *fac, int *ipiv, int *info, int variant, int nb,
                          int nw, void *stream);
 
-/** Diagnostics: the blocked factor with cycle counters.  cycles_dev (6
+/** Diagnostics: the blocked factor with cycle counters.  cycles_dev (10
  *  device uint64, accumulated) receives the clock cycles the first warp of
  *  every system spent in initial load, panel, interchanges+U12, GEMM, U
- *  output, retire/load (waits at the phase barriers included); nw < 0
- *  selects the lookahead form with -nw warps. */
+ *  output, retire/load (waits at the phase barriers included), then inside
+ *  the panel: pivot search, reciprocal + scale + L store, rank-1 update and
+ *  loop; nw < 0 selects the lookahead form with -nw warps. */
 int sgb_gbtrf_phase_cycles(char prec, int nsys, int N, int KL, int KU,
                            const void *ab, int ldab, long long ab_stride,
                            void *fac, int *ipiv, int *info, int nb, int nw,

@@ -53,13 +53,13 @@ void gbtrf_blk_set_choice(char prec, const FactorGeom &g, int nb, int nw)
 
 void gbtrf_blk_choice(char prec, const FactorGeom &g, int &nb, int &nw)
 {
-    if (nb > 0 && nw > 0) return;
+    if (nb > 0 && nw != 0) return;          // nw < 0: the lookahead form, given
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         auto it = g_tune.find(std::make_tuple(prec, g.N, g.KL, g.KU));
         if (it != g_tune.end()) {
             if (nb <= 0) nb = it->second.first;
-            if (nw <= 0) nw = it->second.second;
+            if (nw == 0) nw = it->second.second;
             return;
         }
     }
@@ -67,7 +67,7 @@ void gbtrf_blk_choice(char prec, const FactorGeom &g, int &nb, int &nw)
     // narrow panels and two warps, complex128 (FP64-throughput bound) with
     // narrow panels and one warp.
     if (nb <= 0) nb = 4;
-    if (nw <= 0) nw = g.KL > 56 ? 4 : (prec == 'C' || g.KL > 52) ? 2 : 1;
+    if (nw == 0) nw = g.KL > 56 ? 4 : (prec == 'C' || g.KL > 52) ? 2 : 1;
 }
 
 cudaError_t launch_gbtrf_blk(const GbtrfArgs &a, int nb, int nw, cudaStream_t st)

@@ -161,10 +161,18 @@ __device__ __forceinline__ void panel_factor(cplx_t<R> *__restrict__ win, int P,
                                              int *__restrict__ pvoff, int *__restrict__ shv,
                                              int j0, int nbk, int N, int KL, int KU,
                                              cplx_t<R> *__restrict__ fl, int *__restrict__ pv,
-                                             cplx_t<R> *__restrict__ ys, int lane)
+                                             cplx_t<R> *__restrict__ ys, int lane,
+                                             unsigned long long *__restrict__ prof = nullptr)
 {
     using T2 = cplx_t<R>;
     const T2 zero = mk<R>(R(0), R(0));
+    // optional sub-phase cycle counters (diagnostics): pivot search,
+    // reciprocal + scale + L store, rank-1 update of the panel columns
+    unsigned long long sp[3] = {0, 0, 0};
+    long long smark = prof ? clock64() : 0;
+    auto stick = [&](int ph) {
+        if (prof) { const long long t = clock64(); sp[ph] += (unsigned long long) (t - smark); smark = t; }
+    };
     auto rsl = [&](int i) { int t = rb + i; return t >= WR ? t - WR : t; };
     auto csl = [&](int c) { int t = cb + c; return t >= WC ? t - WC : t; };
     int ju = shv[0], inf = shv[1];
@@ -186,9 +194,11 @@ __device__ __forceinline__ void panel_factor(cplx_t<R> *__restrict__ win, int P,
         const int km = imin(KL, N - 1 - jj);
         // IZAMAX over rows k..k+km: the largest key, then the
         // smallest row holding it
+        stick(2);
         const int ip = warp_argmax_rows<R, RS>(v, k, km, lane);
         const int bt = ip - k, lp = ip & 31, qp = ip >> 5;
         const T2 piv = shfl_c<R>(pick<R, RS, NB>(v, qp, k), lp);
+        stick(0);
         if (lane == 0) pv[jj] = jj + bt + 1;
         if (cnz<R>(piv)) {
             ju = imax(ju, imin(jj + KU + bt, N - 1));
@@ -233,6 +243,7 @@ __device__ __forceinline__ void panel_factor(cplx_t<R> *__restrict__ win, int P,
                     if (i > k && i <= k + km) rv[q] = cfnma(v[q][k], yj, rv[q]);
                 }
             }
+            stick(1);
             // rank-1 update of the remaining panel columns
 #pragma unroll
             for (int c = k + 1; c < NB; ++c) {
@@ -273,6 +284,8 @@ __device__ __forceinline__ void panel_factor(cplx_t<R> *__restrict__ win, int P,
         }
     }
     if (lane == 0) { shv[0] = ju; shv[1] = inf; }
+    if (prof && lane == 0)
+        for (int ph = 0; ph < 3; ++ph) atomicAdd(prof + 6 + ph, sp[ph]);
 }
 
 // Rows r0 .. r0+nr-1 of A (rows outside 0..N-1 read as zero) at columns
@@ -486,7 +499,7 @@ k_gbtrf_cta(FactorGeom g, int nsys, PackedSource src, ModelSource ms,
         // nbk panel columns (row k of step k is row k of slot 0, on lane k).
         if (warp == 0) {
             panel_factor<R, NB, RS, FWD>(win, P, WR, WC, rb, cb, WR, rs, pvoff, shv, j0, nbk, N, KL,
-                                         KU, fl, pv, FWD ? y + s * y_stride : nullptr, lane);
+                                         KU, fl, pv, FWD ? y + s * y_stride : nullptr, lane, prof);
         } else if constexpr (STAGE) {
             // the next nbk rows of A, at the next window's columns
             if (more) {

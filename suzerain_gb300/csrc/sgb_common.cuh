@@ -52,18 +52,35 @@ SGB_HD double2 cfma(double2 a, double2 b, double2 c)
 SGB_HD float2  cconj(float2 a)  { return make_float2(a.x, -a.y); }
 SGB_HD double2 cconj(double2 a) { return make_double2(a.x, -a.y); }
 
-// 1 / z by Smith's method (range-safe for |re| >> |im| and vice versa).
-template <typename R> SGB_HD cplx_t<R> crcp(cplx_t<R> z)
+// 1 / z by the textbook formula conj(z) / |z|^2 after an exact power-of-two
+// scaling of z (D. M. Priest, "Efficient scaling for complex division", ACM
+// TOMS 30(4), 2004): with s = 2^(-e), e the binary exponent of max(|re|,|im|),
+// zs = s z has max(|re|,|im|) in [1, 2), so |zs|^2 in [1, 8) neither
+// overflows nor underflows, and 1/z = s conj(zs) / |zs|^2 with one
+// correctly rounded reciprocal.  The scale is built from the exponent field
+// (clamped so that it stays a normal number); zero, infinite and NaN inputs
+// give infinite or NaN results, as a division would.
+__device__ __forceinline__ float2 crcp_impl(float2 z)
 {
-    const R a = z.x, b = z.y;
-    if ((a < 0 ? -a : a) >= (b < 0 ? -b : b)) {
-        const R r = b / a, d = a + b * r;
-        return mk<R>(R(1) / d, -r / d);
-    } else {
-        const R r = a / b, d = a * r + b;
-        return mk<R>(r / d, R(-1) / d);
-    }
+    const float m = fmaxf(fabsf(z.x), fabsf(z.y));
+    int e = (int) ((__float_as_uint(m) >> 23) & 0xffu);      // biased exponent
+    e = e > 253 ? 253 : e;
+    const float sc = __uint_as_float((unsigned) (254 - e) << 23);   // 2^(127 - e)
+    const float a = z.x * sc, b = z.y * sc;                         // exact
+    const float inv = __frcp_rn(fmaf(a, a, b * b));
+    return make_float2(a * inv * sc, -b * inv * sc);
 }
+__device__ __forceinline__ double2 crcp_impl(double2 z)
+{
+    const double m = fmax(fabs(z.x), fabs(z.y));
+    long long e = (long long) ((__double_as_longlong(m) >> 52) & 0x7ff);
+    e = e > 2045 ? 2045 : e;
+    const double sc = __longlong_as_double((2046ll - e) << 52);     // 2^(1023 - e)
+    const double a = z.x * sc, b = z.y * sc;
+    const double inv = __drcp_rn(fma(a, a, b * b));
+    return make_double2(a * inv * sc, -b * inv * sc);
+}
+template <typename R> __device__ __forceinline__ cplx_t<R> crcp(cplx_t<R> z) { return crcp_impl(z); }
 
 // LAPACK's IZAMAX metric |re| + |im|.
 template <typename R> SGB_HD R cabs1(cplx_t<R> z)
