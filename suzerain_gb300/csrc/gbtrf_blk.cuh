@@ -521,27 +521,41 @@ k_gbtrf_cta(FactorGeom g, int nsys, PackedSource src, ModelSource ms,
         const int ntr = ce - nbk + 1;
 
         // ---------------- 2. interchanges and U12, one column per thread ---
-        for (int c = nbk + tid; c <= ce; c += NT) {
-            const int cc = csl(c);
-            for (int k = 0; k < nbk; ++k) {
-                const int bt = pvoff[k];
-                if (bt) {
-                    T2 &a = win[rsl(k) * P + cc], &b = win[rsl(k + bt) * P + cc];
-                    const T2 t = a; a = b; b = t;
-                }
-            }
-            T2 u[NB];
+        // The panel's interchange offsets, row offsets and L11 are read once
+        // into registers; per column the interchanges are applied in order,
+        // the nbk entries loaded together and U12 solved in registers (the
+        // same multiply-adds in the same order as a column-by-column sweep).
+        // Trailing columns exist only when column j0 + nbk exists, so then
+        // the panel is full (nbk == NB): phases 2 and 3 need no nbk guards.
+        if (ntr > 0) {
+            int bts[NB], ro[NB];
+            T2 l11[NB][NB];
 #pragma unroll
             for (int k = 0; k < NB; ++k) {
-                if (k < nbk) {
-                    const int ro = rsl(k) * P;
-                    T2 v = win[ro + cc];
+                bts[k] = pvoff[k];
+                ro[k] = rsl(k) * P;
 #pragma unroll
-                    for (int m = 0; m < NB; ++m)
-                        if (m < k) v = cfnma(win[ro + csl(m)], u[m], v);
-                    u[k] = v;
-                    win[ro + cc] = v;
+                for (int m = 0; m < NB; ++m)
+                    l11[k][m] = m < k ? win[ro[k] + csl(m)] : zero;
+            }
+            for (int c = nbk + tid; c <= ce; c += NT) {
+                const int cc = csl(c);
+#pragma unroll
+                for (int k = 0; k < NB; ++k) {
+                    if (bts[k]) {
+                        T2 &a = win[ro[k] + cc], &b = win[rsl(k + bts[k]) * P + cc];
+                        const T2 t = a; a = b; b = t;
+                    }
                 }
+                T2 u[NB];
+#pragma unroll
+                for (int k = 0; k < NB; ++k) u[k] = win[ro[k] + cc];
+#pragma unroll
+                for (int k = 1; k < NB; ++k)
+#pragma unroll
+                    for (int m = 0; m < k; ++m) u[k] = cfnma(l11[k][m], u[m], u[k]);
+#pragma unroll
+                for (int k = 0; k < NB; ++k) win[ro[k] + cc] = u[k];
             }
         }
         __syncthreads();
@@ -572,20 +586,18 @@ k_gbtrf_cta(FactorGeom g, int nsys, PackedSource src, ModelSource ms,
                     for (int u = 0; u < TC; ++u)
                         acc[t][u] = win[roff[t] + coff[u]];
 #pragma unroll
-                for (int m = 0; m < NB; ++m) {
-                    if (m < nbk) {
-                        const int cm = csl(m), rm = rsl(m) * P;
-                        T2 l[MAXTR], uu[TC];
+                for (int m = 0; m < NB; ++m) {       // nbk == NB here
+                    const int cm = csl(m), rm = rsl(m) * P;
+                    T2 l[MAXTR], uu[TC];
 #pragma unroll
-                        for (int t = 0; t < MAXTR; ++t) l[t] = win[roff[t] + cm];
+                    for (int t = 0; t < MAXTR; ++t) l[t] = win[roff[t] + cm];
 #pragma unroll
-                        for (int u = 0; u < TC; ++u) uu[u] = win[rm + coff[u]];
+                    for (int u = 0; u < TC; ++u) uu[u] = win[rm + coff[u]];
 #pragma unroll
-                        for (int t = 0; t < MAXTR; ++t)
+                    for (int t = 0; t < MAXTR; ++t)
 #pragma unroll
-                            for (int u = 0; u < TC; ++u)
-                                acc[t][u] = cfnma(l[t], uu[u], acc[t][u]);
-                    }
+                        for (int u = 0; u < TC; ++u)
+                            acc[t][u] = cfnma(l[t], uu[u], acc[t][u]);
                 }
 #pragma unroll
                 for (int t = 0; t < MAXTR; ++t)
