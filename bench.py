@@ -36,6 +36,26 @@ UNIT = "systems/s"
 SPEC = dict(aiter=5, siter=25, diter=5, tolsc=145.0)
 
 
+def rank_config(cfg, rank: int, world: int):
+    """Weak scaling over replicas: rank r solves its own wavenumber block of
+    the same shape (the configuration's seed offset by the rank); no data
+    crosses ranks."""
+    from suzerain_gb300 import synth
+    if world <= 1:
+        return cfg
+    return synth.Config(**{**cfg.__dict__, "seed": cfg.seed + 1000 * rank})
+
+
+def max_over_ranks(ms: float, world: int, device) -> float:
+    """The slowest rank's time (the job's time) when world > 1."""
+    if world <= 1:
+        return ms
+    import torch
+    t = torch.tensor([ms], device=device, dtype=torch.float64)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
 def dist_env():
     return (int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)),
             int(os.environ.get("WORLD_SIZE", 1)))
@@ -180,8 +200,7 @@ def run_ours(args):
     if L.sgb_device_ok() != 0:
         raise RuntimeError(nat.last_error())
     cfg = synth.CONFIGS[args.config]
-    if world > 1:   # weak scaling: each rank its own wavenumber block (seed)
-        cfg = synth.Config(**{**cfg.__dict__, "seed": cfg.seed + 1000 * rank})
+    cfg = rank_config(cfg, rank, world)
     cs, kx, kz, u = cfg.batch()
     if args.nsys:          # first nsys systems of the same batch (profiling runs)
         kx, kz, u = kx[:args.nsys], kz[:args.nsys], u[:args.nsys]
@@ -217,11 +236,7 @@ def run_ours(args):
     barrier()
     launches = L.sgb_launch_count() - l0
     clocks = sampler.stop()
-    ms = e0.elapsed_time(e1)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(e0.elapsed_time(e1), world, "cuda")
     value = nsys * world * args.steps / (ms / 1e3)
 
     # ---- accuracy of the last step (untimed) ------------------------------
