@@ -54,6 +54,18 @@ int suzerain_bsmbsm_q(int S, int n, int i);
 /** q^{-1}(i) = q with S and n exchanged; suzerain/bsmbsm.h:182-186. */
 int suzerain_bsmbsm_qinv(int S, int n, int i);
 
+/** Same layout as gsl_permutation (size, then the index array). */
+typedef struct sgb_permutation {
+    size_t size;
+    size_t *data;
+} sgb_permutation;
+/** q as a permutation of S n indices; suzerain/bsmbsm.h:294,
+ *  suzerain/bsmbsm.c:109-124.  Both blocks come from malloc, so
+ *  gsl_permutation_free (or sgb_permutation_free) releases the result;
+ *  NULL for S <= 0, n <= 0 or on allocation failure. */
+sgb_permutation *suzerain_bsmbsm_permutation(int S, int n);
+void sgb_permutation_free(sgb_permutation *p);
+
 /** y <- alpha P x + beta y ('N') or alpha P^T x + beta y ('T');
  *  suzerain/bsmbsm.h:208-257, suzerain/bsmbsm_aPxpby_complex.def:36-329.
  *  Returns 0, or the positive BLAS argument position of a bad argument
@@ -79,9 +91,20 @@ int suzerain_bsmbsm_zaPxpby(char trans, int S, int n,
  *  block's positions outside B's band; suzerain/bsmbsm.h:338-381,
  *  suzerain/bsmbsm_pack.def:36-122.  Returns 0 or the positive argument
  *  position (511 when b aliases papt). */
+int suzerain_bsmbsm_spack(int S, int n, int ihat, int jhat, int kl, int ku,
+                          const float alpha, const float *b, int ldb,
+                          int KL, int KU, float *papt, int ldpapt);
 int suzerain_bsmbsm_dpack(int S, int n, int ihat, int jhat, int kl, int ku,
                           const double alpha, const double *b, int ldb,
                           int KL, int KU, double *papt, int ldpapt);
+int suzerain_bsmbsm_cpack(int S, int n, int ihat, int jhat, int kl, int ku,
+                          const sgb_complex_float alpha,
+                          const sgb_complex_float *b, int ldb, int KL, int KU,
+                          sgb_complex_float *papt, int ldpapt);
+int suzerain_bsmbsm_cspack(int S, int n, int ihat, int jhat, int kl, int ku,
+                           const sgb_complex_float alpha, const float *b,
+                           int ldb, int KL, int KU, sgb_complex_float *papt,
+                           int ldpapt);
 int suzerain_bsmbsm_zpack(int S, int n, int ihat, int jhat, int kl, int ku,
                           const sgb_complex_double alpha,
                           const sgb_complex_double *b, int ldb, int KL, int KU,
@@ -105,6 +128,26 @@ int suzerain_bsmbsm_zdpackc(const suzerain_bsmbsm *A, int ihat, int jhat,
 int suzerain_bsmbsm_zdpackf(const suzerain_bsmbsm *A, int ihat, int jhat,
                             const sgb_complex_double alpha, const double *b,
                             sgb_complex_double *papt);
+int suzerain_bsmbsm_spackc(const suzerain_bsmbsm *A, int ihat, int jhat,
+                           const float alpha, const float *b, float *papt);
+int suzerain_bsmbsm_spackf(const suzerain_bsmbsm *A, int ihat, int jhat,
+                           const float alpha, const float *b, float *papt);
+int suzerain_bsmbsm_dpackc(const suzerain_bsmbsm *A, int ihat, int jhat,
+                           const double alpha, const double *b, double *papt);
+int suzerain_bsmbsm_dpackf(const suzerain_bsmbsm *A, int ihat, int jhat,
+                           const double alpha, const double *b, double *papt);
+int suzerain_bsmbsm_cpackc(const suzerain_bsmbsm *A, int ihat, int jhat,
+                           const sgb_complex_float alpha,
+                           const sgb_complex_float *b, sgb_complex_float *papt);
+int suzerain_bsmbsm_cpackf(const suzerain_bsmbsm *A, int ihat, int jhat,
+                           const sgb_complex_float alpha,
+                           const sgb_complex_float *b, sgb_complex_float *papt);
+int suzerain_bsmbsm_cspackc(const suzerain_bsmbsm *A, int ihat, int jhat,
+                            const sgb_complex_float alpha, const float *b,
+                            sgb_complex_float *papt);
+int suzerain_bsmbsm_cspackf(const suzerain_bsmbsm *A, int ihat, int jhat,
+                            const sgb_complex_float alpha, const float *b,
+                            sgb_complex_float *papt);
 
 /** Partial-pivot band LU, LAPACK zgbtrf/cgbtrf semantics and storage
  *  ((2kl+ku+1) x n, 1-based ipiv, info > 0 at the first zero pivot);
@@ -128,6 +171,24 @@ int suzerain_lapack_cgbtrs(const char trans, const int n, const int kl,
                            const int *ipiv, sgb_complex_float *b,
                            const int ldb);
 
+/** LAPACK's expert driver zgbsvx (equilibration for fact 'E', factor for
+ *  'N'/'E', a given factor for 'F', reciprocal condition number, solve,
+ *  iterative refinement with forward and backward error bounds, unscaling;
+ *  info = n+1 when rcond < eps); suzerain/blas_et_al/lapack.c:548-574 and
+ *  lapack.h:601-626, as called by suzerain/bsmbsm_solver.cpp:252-291.  Same
+ *  23 arguments; work is not used and rwork[0] receives the reciprocal pivot
+ *  growth.  The condition estimate's triangular solves do not rescale
+ *  against overflow (zlatbs with scale < 1). */
+int suzerain_lapack_zgbsvx(const char fact, const char trans, const int n,
+                           const int kl, const int ku, const int nrhs,
+                           sgb_complex_double *ab, const int ldab,
+                           sgb_complex_double *afb, const int ldafb,
+                           int *ipiv, char *equed, double *r, double *c,
+                           sgb_complex_double *b, const int ldb,
+                           sgb_complex_double *x, const int ldx,
+                           double *rcond, double *ferr, double *berr,
+                           sgb_complex_double *work, double *rwork);
+
 /** Factor when *fact == 'N' (then *fact = 'F'), solve;
  *  suzerain/blas_et_al/lapackext.c:127-147. */
 int suzerain_lapackext_zgbsv(char *const fact, const char trans, const int n,
@@ -138,6 +199,16 @@ int suzerain_lapackext_cgbsv(char *const fact, const char trans, const int n,
                              const int kl, const int ku, const int nrhs,
                              sgb_complex_float *ab, const int ldab, int *ipiv,
                              sgb_complex_float *b, const int ldb);
+/** Real forms (suzerain/blas_et_al/lapackext.h:66-95): the complex kernels
+ *  on the band promoted with zero imaginary parts. */
+int suzerain_lapackext_dgbsv(char *const fact, const char trans, const int n,
+                             const int kl, const int ku, const int nrhs,
+                             double *ab, const int ldab, int *ipiv,
+                             double *b, const int ldb);
+int suzerain_lapackext_sgbsv(char *const fact, const char trans, const int n,
+                             const int kl, const int ku, const int nrhs,
+                             float *ab, const int ldab, int *ipiv,
+                             float *b, const int ldb);
 
 /** Complex64 LU with FP64 iterative refinement and complex128 fallback;
  *  suzerain/blas_et_al/lapackext.h:258-299,
@@ -156,6 +227,17 @@ int suzerain_lapackext_zcgbsvx(char *const fact, int *const apprx,
                                sgb_complex_double *const x, int *const siter,
                                int *const diter, double *const tolsc,
                                sgb_complex_double *const r, double *const res);
+/** The real form (same 18 arguments, suzerain/blas_et_al/lapackext.h:258-277):
+ *  zcgbsvx on the promoted band; afb returns the float32 factor at its start
+ *  for fact 'S' (the in-place demotion), the float64 one for 'D'. */
+int suzerain_lapackext_dsgbsvx(char *const fact, int *const apprx,
+                               const int aiter, char trans, const int n,
+                               const int kl, const int ku, double *const ab,
+                               double *const afrob, double *const afb,
+                               int *const ipiv, double *const b,
+                               double *const x, int *const siter,
+                               int *const diter, double *const tolsc,
+                               double *const r, double *const res);
 
 /** y <- alpha op(A) x + beta y for a band A; suzerain/blas_et_al/blas.c:1035-1054
  *  over suzerain/blas_et_al/gbmv.def ('C' takes the 'T' branch unconjugated). */
@@ -308,6 +390,21 @@ int sgb_gbtrs_batched(char prec, char trans, int nsys, int N, int KL, int KU,
 int sgb_gbtrs_batched_ws(char prec, char trans, int nsys, int N, int KL, int KU,
                          const void *fac, const int *ipiv, const void *b,
                          void *x, void *ywork, void *stream);
+
+/** Batched zgbsvx: nsys systems of one geometry, one right-hand side each,
+ *  every pointer on the device (rcond, ferr, berr, rpvgrw may also be host
+ *  memory).  Per system: ab (ld ldab, stride ab_stride; overwritten by the
+ *  equilibrated band), afb (LAPACK gbtrf storage, ld ldafb, stride
+ *  afb_stride; input for fact 'F', output otherwise, may be null unless
+ *  'F'), ipiv / r / c / b / x of n entries, equed / info of one.  Returns 0
+ *  or a negative argument index; per-system results follow zgbsvx. */
+int sgb_zgbsvx_batched(char fact, char trans, int nsys, int n, int kl, int ku,
+                       sgb_complex_double *ab, int ldab, long long ab_stride,
+                       sgb_complex_double *afb, int ldafb, long long afb_stride,
+                       int *ipiv, char *equed, double *r, double *c,
+                       sgb_complex_double *b, sgb_complex_double *x,
+                       double *rcond, double *ferr, double *berr, double *rpvgrw,
+                       int *info, void *stream);
 
 /** Row-panel factor -> LAPACK gbtrf storage ((2KL+KU+1) x N per system). */
 int sgb_factor_to_lapack(char prec, int nsys, int N, int KL, int KU,

@@ -5,12 +5,11 @@
 // (LU, PAPT, PB, PX, ipiv; column-major, PAPT in bsmbsm packed band order),
 // the same specification strings and the same error messages.  The solves run
 // on the GPU through the drop-in entry points (suzerain_lapackext_zgbsv,
-// suzerain_lapackext_zcgbsvx); the storage here is host memory, as the
-// reference's Eigen members are.
+// suzerain_lapack_zgbsvx, suzerain_lapackext_zcgbsvx); the storage here is
+// host memory, as the reference's Eigen members are.
 //
-// Differences: errors throw std::runtime_error (the reference calls
-// SUZERAIN_ERROR, whose default handler aborts); the zgbsvx method (the
-// equilibrating expert driver) is not provided and build() rejects it.
+// Difference: errors throw std::runtime_error (the reference calls
+// SUZERAIN_ERROR, whose default handler aborts).
 #ifndef SUZERAIN_GB300_SOLVER_HPP
 #define SUZERAIN_GB300_SOLVER_HPP
 
@@ -71,7 +70,7 @@ public:
 
     virtual ~bsmbsm_solver() = default;
 
-    /** zgbsv or zcgbsvx per the specification (nrhs right hand sides). */
+    /** zgbsv, zgbsvx or zcgbsvx per the specification (nrhs right hand sides). */
     static std::unique_ptr<bsmbsm_solver> build(const suzerain_bsmbsm &A,
                                                 const specification_zgbsv &spec, int nrhs);
 
@@ -211,6 +210,69 @@ protected:
     }
 };
 
+/** LAPACK's expert driver, out of place: PAPT is LD x N, LU (2KL + KU + 1) x N
+ *  holds the factor; the first solve equilibrates (equil=true) or not and
+ *  factors, later ones reuse the factor with fact 'F' until PAPT is supplied
+ *  again (suzerain/bsmbsm_solver.cpp:184-291).  Every right hand side
+ *  records equed, 1/rcond, ferr and berr. */
+class bsmbsm_solver_zgbsvx : public bsmbsm_solver {
+public:
+    struct stat { char equed; double rcond_inv, ferr, berr; };
+    std::vector<stat> stats;
+
+    bsmbsm_solver_zgbsvx(const suzerain_bsmbsm &a, const specification_zgbsv &s, int nrhs)
+        : bsmbsm_solver(a, s, nrhs), papt_((size_t) a.LD * a.N), px_((size_t) a.N * nrhs),
+          r_(a.N), c_(a.N), rwork_(a.N), ferr_(nrhs), berr_(nrhs), work_((size_t) 2 * a.N)
+    {
+        if (s.method() != SGB_METHOD_ZGBSVX)
+            throw std::invalid_argument("Invalid method in bsmbsm_solver_zgbsvx");
+        LU.assign((size_t) (2 * a.KL + a.KU + 1) * a.N, complex_double(0));
+        ld_PAPT_ = a.LD;
+        PAPT_ = papt_.data();
+        PX_ = px_.data();
+    }
+    char equed() const { return equed_; }
+    double rcond() const { return rcond_; }
+    std::vector<std::string> summarize_statistics() const override
+    {
+        auto out = bsmbsm_solver::summarize_statistics();
+        if (!stats.empty()) {
+            double mr = 0, mf = 0, mb = 0;
+            int eq = 0;
+            for (const stat &x : stats) {
+                mr = std::max(mr, x.rcond_inv); mf = std::max(mf, x.ferr); mb = std::max(mb, x.berr);
+                eq += x.equed != 'N';
+            }
+            char buf[256];
+            std::snprintf(buf, sizeof buf,
+                          "solves %zu, equilibrated %d, max 1/rcond %.3g, max ferr %.3g, max berr %.3g",
+                          stats.size(), eq, mr, mf, mb);
+            out.push_back(buf);
+        }
+        return out;
+    }
+
+protected:
+    int solve_hook(char trans, int nrhs) override
+    {
+        const int info = suzerain_lapack_zgbsvx(fact_, trans, A.N, A.KL, A.KU, nrhs, PAPT_, A.LD,
+                                                LU.data(), 2 * A.KL + A.KU + 1, ipiv.data(), &equed_,
+                                                r_.data(), c_.data(), PB.data(), A.N, PX_, A.N,
+                                                &rcond_, ferr_.data(), berr_.data(), work_.data(),
+                                                rwork_.data());
+        fact_ = 'F';
+        for (int j = 0; j < nrhs; ++j) stats.push_back({equed_, 1 / rcond_, ferr_[j], berr_[j]});
+        return info;
+    }
+
+private:
+    std::vector<complex_double> papt_, px_;
+    std::vector<double> r_, c_, rwork_, ferr_, berr_;
+    std::vector<complex_double> work_;
+    char equed_ = 'N';
+    double rcond_ = 0;
+};
+
 /** Complex64 factor + complex128 refinement, out of place: PAPT is LD x N,
  *  LU (2KL + KU + 1) x N holds the factor (suzerain/bsmbsm_solver.cpp:293-414).
  *  Every right hand side runs the driver with the specification's siter,
@@ -278,6 +340,7 @@ inline std::unique_ptr<bsmbsm_solver> bsmbsm_solver::build(const suzerain_bsmbsm
 {
     switch (spec.method()) {
     case SGB_METHOD_ZGBSV: return std::make_unique<bsmbsm_solver_zgbsv>(A, spec, nrhs);
+    case SGB_METHOD_ZGBSVX: return std::make_unique<bsmbsm_solver_zgbsvx>(A, spec, nrhs);
     case SGB_METHOD_ZCGBSVX: return std::make_unique<bsmbsm_solver_zcgbsvx>(A, spec, nrhs);
     default:
         throw std::invalid_argument(std::string("bsmbsm_solver::build: method not provided: ") +

@@ -19,6 +19,10 @@
  *                           pivot metric, first index wins ties)
  *   zgbtrs / cgbtrs         band solve for 'N', 'T', 'C'
  *   zlangb('F'), dznrm2, dlamch('E')
+ *   zgbsvx                  the expert driver (zgbequ, zlaqgb, zlangb, zgbcon
+ *                           with zlacn2, zgbrfs), called by the reference at
+ *                           suzerain/blas_et_al/lapack.c:548-574 and
+ *                           suzerain/bsmbsm_solver.cpp:252-291
  * A runtime switch (orc_use_openblas) routes gbtrf/gbtrs to SciPy's bundled
  * OpenBLAS instead, so the CPU baseline runs production LAPACK code.
  *
@@ -452,6 +456,398 @@ double orc_zlangb_fro(int n, int kl, int ku, const zc *ab, int ldab)
 }
 
 double orc_dlamch_eps(void) { return DBL_EPSILON * 0.5; }
+
+/* ------------------------------------------------------------------------ */
+/* zgbsvx restatement: the expert driver of reference LAPACK with its        */
+/* helpers, from the published algorithms (0-based indices; ab is the band   */
+/* with A(i,j) at ab[ku+i-j + j*ldab]; afb the gbtrf storage).               */
+/*   ZGBEQU  row scales r_i = 1/max_j |a_ij|_1, then column scales c_j =     */
+/*           1/max_i |a_ij|_1 r_i (|.|_1 = |re|+|im|), clamped to            */
+/*           [safmin, 1/safmin]; info i+1 / n+j+1 at the first zero row/col  */
+/*   ZLAQGB  scale rows when rowcnd < 0.1 or amax outside [small, large],    */
+/*           columns when colcnd < 0.1 (small = safmin/precision)            */
+/*   ZLANGB  '1', 'I', 'M' with the modulus                                  */
+/*   ZGBCON  Higham's estimator (ZLACN2: at most 5 iterations, x = 1/n, the  */
+/*           sign vector x_i/|x_i|, unit vectors at the first max modulus,   */
+/*           the alternating vector (-1)^i (1 + i/(n-1)) with 2 s/(3n))      */
+/*           over the solves with the factor; ZLATBS's overflow rescaling    */
+/*           is not taken (scale stays 1)                                    */
+/*   ZGBRFS  residual, componentwise backward error with nz = min(kl+ku+2,   */
+/*           n+1), safe1 = nz safmin, safe2 = safe1/eps; at most 5           */
+/*           corrections while berr > eps and berr halves; ferr from the     */
+/*           estimator on diag(w) inv(op(A)^H) and inv(op(A)) diag(w)        */
+/* ------------------------------------------------------------------------ */
+static const double kSafmin = DBL_MIN;               /* dlamch('S') */
+static const double kPrec = DBL_EPSILON;             /* dlamch('P') */
+
+static int orc_zgbequ(int n, int kl, int ku, const zc *ab, int ldab, double *r,
+                      double *c, double *rowcnd, double *colcnd, double *amax)
+{
+    const double smlnum = kSafmin, bignum = 1.0 / smlnum;
+    *rowcnd = 1; *colcnd = 1; *amax = 0;
+    for (int i = 0; i < n; ++i) r[i] = 0;
+    for (int j = 0; j < n; ++j)
+        for (int i = imax(0, j - ku); i <= imin(n - 1, j + kl); ++i)
+            r[i] = fmax(r[i], zabs1(ab[ku + i - j + j * ldab]));
+    double mn = bignum, mx = 0;
+    for (int i = 0; i < n; ++i) { mx = fmax(mx, r[i]); mn = fmin(mn, r[i]); }
+    *amax = mx;
+    if (mn == 0) {
+        for (int i = 0; i < n; ++i) if (r[i] == 0) return i + 1;
+    }
+    for (int i = 0; i < n; ++i) r[i] = 1.0 / fmin(fmax(r[i], smlnum), bignum);
+    *rowcnd = fmax(mn, smlnum) / fmin(mx, bignum);
+    for (int j = 0; j < n; ++j) c[j] = 0;
+    for (int j = 0; j < n; ++j)
+        for (int i = imax(0, j - ku); i <= imin(n - 1, j + kl); ++i)
+            c[j] = fmax(c[j], zabs1(ab[ku + i - j + j * ldab]) * r[i]);
+    mn = bignum; mx = 0;
+    for (int j = 0; j < n; ++j) { mn = fmin(mn, c[j]); mx = fmax(mx, c[j]); }
+    if (mn == 0) {
+        for (int j = 0; j < n; ++j) if (c[j] == 0) return n + j + 1;
+    }
+    for (int j = 0; j < n; ++j) c[j] = 1.0 / fmin(fmax(c[j], smlnum), bignum);
+    *colcnd = fmax(mn, smlnum) / fmin(mx, bignum);
+    return 0;
+}
+
+static char orc_zlaqgb(int n, int kl, int ku, zc *ab, int ldab, const double *r,
+                       const double *c, double rowcnd, double colcnd, double amax)
+{
+    const double small = kSafmin / kPrec, large = 1.0 / small;
+    char equed;
+    if (rowcnd >= 0.1 && amax >= small && amax <= large)
+        equed = colcnd >= 0.1 ? 'N' : 'C';
+    else
+        equed = colcnd >= 0.1 ? 'R' : 'B';
+    if (equed == 'N') return equed;
+    for (int j = 0; j < n; ++j)
+        for (int i = imax(0, j - ku); i <= imin(n - 1, j + kl); ++i) {
+            double f = equed == 'C' ? c[j] : (equed == 'R' ? r[i] : c[j] * r[i]);
+            ab[ku + i - j + j * ldab] *= f;
+        }
+    return equed;
+}
+
+static double orc_zlangb(char norm, int n, int kl, int ku, const zc *ab, int ldab)
+{
+    double v = 0;
+    if (norm == 'M') {
+        for (int j = 0; j < n; ++j)
+            for (int i = imax(0, j - ku); i <= imin(n - 1, j + kl); ++i)
+                v = fmax(v, cabs(ab[ku + i - j + j * ldab]));
+    } else if (norm == '1') {
+        for (int j = 0; j < n; ++j) {
+            double s = 0;
+            for (int i = imax(0, j - ku); i <= imin(n - 1, j + kl); ++i)
+                s += cabs(ab[ku + i - j + j * ldab]);
+            v = fmax(v, s);
+        }
+    } else {
+        for (int i = 0; i < n; ++i) {
+            double s = 0;
+            for (int j = imax(0, i - kl); j <= imin(n - 1, i + ku); ++j)
+                s += cabs(ab[ku + i - j + j * ldab]);
+            v = fmax(v, s);
+        }
+    }
+    return v;
+}
+
+static double dzsum1(int n, const zc *x)
+{
+    double s = 0;
+    for (int i = 0; i < n; ++i) s += cabs(x[i]);
+    return s;
+}
+static int izmax1(int n, const zc *x)
+{
+    int k = 0;
+    double best = cabs(x[0]);
+    for (int i = 1; i < n; ++i) if (cabs(x[i]) > best) { best = cabs(x[i]); k = i; }
+    return k;
+}
+static void sign_vec(int n, zc *x)
+{
+    for (int i = 0; i < n; ++i) {
+        const double a = cabs(x[i]);
+        x[i] = a > kSafmin ? creal(x[i]) / a + I * (cimag(x[i]) / a) : 1.0;
+    }
+}
+
+/* ZLACN2 reverse communication; isave[0] = state, [1] = index, [2] = iter */
+static void orc_zlacn2(int n, zc *v, zc *x, double *est, int *kase, int isave[3])
+{
+    if (*kase == 0) {
+        for (int i = 0; i < n; ++i) x[i] = 1.0 / (double) n;
+        *kase = 1; isave[0] = 1;
+        return;
+    }
+    switch (isave[0]) {
+    case 1:
+        if (n == 1) { v[0] = x[0]; *est = cabs(v[0]); *kase = 0; return; }
+        *est = dzsum1(n, x);
+        sign_vec(n, x);
+        *kase = 2; isave[0] = 2;
+        return;
+    case 2:
+        isave[1] = izmax1(n, x);
+        isave[2] = 2;
+        goto unit;
+    case 3: {
+        memcpy(v, x, (size_t) n * sizeof(zc));
+        const double estold = *est;
+        *est = dzsum1(n, v);
+        if (*est <= estold) goto alt;
+        sign_vec(n, x);
+        *kase = 2; isave[0] = 4;
+        return;
+    }
+    case 4: {
+        const int jlast = isave[1];
+        isave[1] = izmax1(n, x);
+        if (cabs(x[jlast]) != cabs(x[isave[1]]) && isave[2] < 5) {
+            isave[2] += 1;
+            goto unit;
+        }
+        goto alt;
+    }
+    case 5: {
+        const double temp = 2.0 * (dzsum1(n, x) / (double) (3 * n));
+        if (temp > *est) { memcpy(v, x, (size_t) n * sizeof(zc)); *est = temp; }
+        *kase = 0;
+        return;
+    }
+    }
+unit:
+    for (int i = 0; i < n; ++i) x[i] = 0;
+    x[isave[1]] = 1;
+    *kase = 1; isave[0] = 3;
+    return;
+alt:
+    for (int i = 0; i < n; ++i)
+        x[i] = ((i & 1) ? -1.0 : 1.0) * (1.0 + (double) i / (double) (n - 1));
+    *kase = 1; isave[0] = 5;
+}
+
+static double orc_zgbcon(char norm, int n, int kl, int ku, const zc *afb, int ldafb,
+                         const int *ipiv, double anorm, zc *work)
+{
+    if (n == 0) return 1;
+    if (anorm == 0) return 0;
+    const int kase1 = norm == '1' ? 1 : 2;
+    zc *x = work, *v = work + n;
+    double ainvnm = 0;
+    int kase = 0, isave[3] = {0, 0, 0};
+    for (;;) {
+        orc_zlacn2(n, v, x, &ainvnm, &kase, isave);
+        if (!kase) break;
+        orc_zgbtrs(kase == kase1 ? 'N' : 'C', n, kl, ku, 1, afb, ldafb, ipiv, x, n);
+    }
+    return ainvnm != 0 ? (1.0 / ainvnm) / anorm : 0;
+}
+
+static void orc_zgbrfs(char trans, int n, int kl, int ku, const zc *ab, int ldab,
+                       const zc *afb, int ldafb, const int *ipiv, const zc *b, zc *x,
+                       double *ferr, double *berr, zc *work, double *rw)
+{
+    const int notran = trans == 'N';
+    const char transn = notran ? 'N' : 'C', transt = notran ? 'C' : 'N';
+    const double nz = imin(kl + ku + 2, n + 1);
+    const double eps = DBL_EPSILON * 0.5, safe1 = nz * kSafmin, safe2 = safe1 / eps;
+    zc *r = work, *ex = work + n, *ev = work + 2 * n;
+    int count = 1;
+    double lstres = 3;
+    for (;;) {
+        for (int i = 0; i < n; ++i) { r[i] = b[i]; rw[i] = zabs1(b[i]); }
+        if (notran) {
+            for (int k = 0; k < n; ++k) {
+                const double xk = zabs1(x[k]);
+                for (int i = imax(0, k - ku); i <= imin(n - 1, k + kl); ++i) {
+                    const zc a = ab[ku + i - k + k * ldab];
+                    r[i] -= a * x[k];
+                    rw[i] += zabs1(a) * xk;
+                }
+            }
+        } else {
+            for (int k = 0; k < n; ++k) {
+                double s = 0;
+                for (int i = imax(0, k - ku); i <= imin(n - 1, k + kl); ++i) {
+                    zc a = ab[ku + i - k + k * ldab];
+                    if (trans == 'C') a = conj(a);
+                    r[k] -= a * x[i];
+                    s += zabs1(a) * zabs1(x[i]);
+                }
+                rw[k] += s;
+            }
+        }
+        double s = 0;
+        for (int i = 0; i < n; ++i)
+            s = fmax(s, rw[i] > safe2 ? zabs1(r[i]) / rw[i] : (zabs1(r[i]) + safe1) / (rw[i] + safe1));
+        *berr = s;
+        if (s > eps && 2 * s <= lstres && count <= 5) {
+            orc_zgbtrs(trans, n, kl, ku, 1, afb, ldafb, ipiv, r, n);
+            for (int i = 0; i < n; ++i) x[i] += r[i];
+            lstres = s;
+            count += 1;
+            continue;
+        }
+        break;
+    }
+    for (int i = 0; i < n; ++i)
+        rw[i] = rw[i] > safe2 ? zabs1(r[i]) + nz * eps * rw[i] : zabs1(r[i]) + nz * eps * rw[i] + safe1;
+    int kase = 0, isave[3] = {0, 0, 0};
+    *ferr = 0;
+    for (;;) {
+        orc_zlacn2(n, ev, ex, ferr, &kase, isave);
+        if (!kase) break;
+        if (kase == 1) {
+            orc_zgbtrs(transt, n, kl, ku, 1, afb, ldafb, ipiv, ex, n);
+            for (int i = 0; i < n; ++i) ex[i] *= rw[i];
+        } else {
+            for (int i = 0; i < n; ++i) ex[i] *= rw[i];
+            orc_zgbtrs(transn, n, kl, ku, 1, afb, ldafb, ipiv, ex, n);
+        }
+    }
+    double xm = 0;
+    for (int i = 0; i < n; ++i) xm = fmax(xm, zabs1(x[i]));
+    if (xm != 0) *ferr /= xm;
+}
+
+/* suzerain_lapack_zgbsvx semantics (fact 'N', 'E', 'F'; nrhs columns);
+ * returns info; *rpvgrw receives what LAPACK leaves in rwork[0]. */
+int orc_zgbsvx(char fact, char trans, int n, int kl, int ku, int nrhs, zc *ab, int ldab,
+               zc *afb, int ldafb, int *ipiv, char *equed, double *r, double *c, zc *b,
+               int ldb, zc *x, int ldx, double *rcond, double *ferr, double *berr,
+               double *rpvgrw)
+{
+    fact = (char) toupper((unsigned char) fact);
+    trans = (char) toupper((unsigned char) trans);
+    const int nofact = fact == 'N', equil = fact == 'E', notran = trans == 'N';
+    int rowequ = 0, colequ = 0;
+    double rowcnd = 1, colcnd = 1, amax = 0;
+    const double smlnum = kSafmin, bignum = 1.0 / smlnum;
+    if (nofact || equil) *equed = 'N';
+    else {
+        *equed = (char) toupper((unsigned char) *equed);
+        rowequ = *equed == 'R' || *equed == 'B';
+        colequ = *equed == 'C' || *equed == 'B';
+    }
+    if (!nofact && !equil && fact != 'F') return -1;
+    if (!notran && trans != 'T' && trans != 'C') return -2;
+    if (n < 0) return -3;
+    if (kl < 0) return -4;
+    if (ku < 0) return -5;
+    if (nrhs < 0) return -6;
+    if (ldab < kl + ku + 1) return -8;
+    if (ldafb < 2 * kl + ku + 1) return -10;
+    if (fact == 'F' && !(rowequ || colequ || *equed == 'N')) return -12;
+    if (rowequ) {
+        double mn = bignum, mx = 0;
+        for (int j = 0; j < n; ++j) { mn = fmin(mn, r[j]); mx = fmax(mx, r[j]); }
+        if (mn <= 0) return -13;
+        rowcnd = n > 0 ? fmax(mn, smlnum) / fmin(mx, bignum) : 1;
+    }
+    if (colequ) {
+        double mn = bignum, mx = 0;
+        for (int j = 0; j < n; ++j) { mn = fmin(mn, c[j]); mx = fmax(mx, c[j]); }
+        if (mn <= 0) return -14;
+        colcnd = n > 0 ? fmax(mn, smlnum) / fmin(mx, bignum) : 1;
+    }
+    if (ldb < imax(1, n)) return -16;
+    if (ldx < imax(1, n)) return -18;
+    if (equil) {
+        if (orc_zgbequ(n, kl, ku, ab, ldab, r, c, &rowcnd, &colcnd, &amax) == 0) {
+            *equed = orc_zlaqgb(n, kl, ku, ab, ldab, r, c, rowcnd, colcnd, amax);
+            rowequ = *equed == 'R' || *equed == 'B';
+            colequ = *equed == 'C' || *equed == 'B';
+        }
+    }
+    for (int j = 0; j < nrhs; ++j)
+        for (int i = 0; i < n; ++i) {
+            if (notran && rowequ) b[i + j * ldb] *= r[i];
+            else if (!notran && colequ) b[i + j * ldb] *= c[i];
+        }
+    const int kv = kl + ku;
+    int info = 0;
+    if (nofact || equil) {
+        for (int j = 0; j < n; ++j) {
+            for (int t = 0; t < ldafb; ++t) afb[t + j * ldafb] = 0;
+            for (int i = imax(0, j - ku); i <= imin(n - 1, j + kl); ++i)
+                afb[kl + ku + i - j + j * ldafb] = ab[ku + i - j + j * ldab];
+        }
+        info = orc_zgbtrf(n, kl, ku, afb, ldafb, ipiv);
+        if (info > 0) {
+            double an = 0, um = 0;
+            for (int j = 0; j < info; ++j)
+                for (int i = imax(0, j - ku); i <= imin(n - 1, j + kl); ++i)
+                    an = fmax(an, cabs(ab[ku + i - j + j * ldab]));
+            for (int j = 0; j < info; ++j)
+                for (int i = imax(0, j - kv); i <= j; ++i)
+                    um = fmax(um, cabs(afb[kv + i - j + j * ldafb]));
+            *rpvgrw = um == 0 ? 1 : an / um;
+            *rcond = 0;
+            return info;
+        }
+    }
+    const char norm = notran ? '1' : 'I';
+    const double anorm = orc_zlangb(norm, n, kl, ku, ab, ldab);
+    double um = 0;
+    for (int j = 0; j < n; ++j)
+        for (int i = imax(0, j - kv); i <= j; ++i)
+            um = fmax(um, cabs(afb[kv + i - j + j * ldafb]));
+    *rpvgrw = um == 0 ? 1 : orc_zlangb('M', n, kl, ku, ab, ldab) / um;
+    zc *work = (zc *) malloc((size_t) 3 * imax(n, 1) * sizeof(zc));
+    double *rw = (double *) malloc((size_t) imax(n, 1) * sizeof(double));
+    *rcond = orc_zgbcon(norm, n, kl, ku, afb, ldafb, ipiv, anorm, work);
+    for (int j = 0; j < nrhs; ++j) {
+        for (int i = 0; i < n; ++i) x[i + j * ldx] = b[i + j * ldb];
+        orc_zgbtrs(trans, n, kl, ku, 1, afb, ldafb, ipiv, x + j * ldx, ldx);
+        orc_zgbrfs(trans, n, kl, ku, ab, ldab, afb, ldafb, ipiv, b + j * ldb, x + j * ldx,
+                   ferr + j, berr + j, work, rw);
+    }
+    free(work);
+    free(rw);
+    for (int j = 0; j < nrhs; ++j) {
+        if (notran && colequ) {
+            for (int i = 0; i < n; ++i) x[i + j * ldx] *= c[i];
+            ferr[j] /= colcnd;
+        } else if (!notran && rowequ) {
+            for (int i = 0; i < n; ++i) x[i + j * ldx] *= r[i];
+            ferr[j] /= rowcnd;
+        }
+    }
+    if (*rcond < DBL_EPSILON * 0.5) info = n + 1;
+    return info;
+}
+
+/* LAPACK's own zgbsvx from SciPy's OpenBLAS, for pinning the restatement;
+ * returns -1000 when the library or the symbol is missing. */
+typedef void (*f_gbsvx)(const char*, const char*, const int*, const int*, const int*,
+                        const int*, void*, const int*, void*, const int*, int*, char*,
+                        double*, double*, void*, const int*, void*, const int*, double*,
+                        double*, double*, void*, double*, int*, size_t, size_t, size_t);
+int orc_openblas_zgbsvx(const char *path, char fact, char trans, int n, int kl, int ku,
+                        int nrhs, zc *ab, int ldab, zc *afb, int ldafb, int *ipiv,
+                        char *equed, double *r, double *c, zc *b, int ldb, zc *x, int ldx,
+                        double *rcond, double *ferr, double *berr, double *rpvgrw)
+{
+    void *h = path ? dlopen(path, RTLD_NOW | RTLD_LOCAL) : NULL;
+    if (!h) return -1000;
+    f_gbsvx f = (f_gbsvx) dlsym(h, "scipy_zgbsvx_");
+    void (*set_threads)(int) = (void (*)(int)) dlsym(h, "scipy_openblas_set_num_threads");
+    if (!f) return -1000;
+    if (set_threads) set_threads(1);
+    zc *work = (zc *) malloc((size_t) 2 * imax(n, 1) * sizeof(zc));
+    double *rwork = (double *) malloc((size_t) imax(n, 1) * sizeof(double));
+    int info = 0;
+    f(&fact, &trans, &n, &kl, &ku, &nrhs, ab, &ldab, afb, &ldafb, ipiv, equed, r, c, b, &ldb,
+      x, &ldx, rcond, ferr, berr, work, rwork, &info, 1, 1, 1);
+    *rpvgrw = rwork[0];
+    free(work);
+    free(rwork);
+    return info;
+}
 
 /* ------------------------------------------------------------------------ */
 /* zcgbsvx restatement (suzerain/blas_et_al/dsgbsvx.def:70-313)             */

@@ -97,6 +97,10 @@ def lib():
         L.orc_zcgbsvx.argtypes = [_p, _p, _i, C.c_char, _i, _i, _i, _p, _p,
                                   _p, _p, _p, _p, _p, _p, _p, _p, _p]
         L.orc_use_openblas.argtypes = [_cp]
+        gbsvx_args = [C.c_char, C.c_char, _i, _i, _i, _i, _p, _i, _p, _i, _p,
+                      _p, _p, _p, _p, _i, _p, _i, _p, _p, _p, _p]
+        L.orc_zgbsvx.argtypes = gbsvx_args
+        L.orc_openblas_zgbsvx.argtypes = [_cp] + gbsvx_args
         L.orc_assemble_packed.argtypes = [_i, _i, _i, _i, _p, _p, _p, _i, _p,
                                           _p, _p, _p, _p, _i, _i]
         L.orc_block_coefs.argtypes = [_i, _p, _p, _p, _p, _d, _d, _d, _p, _p,
@@ -232,6 +236,47 @@ def zcgbsvx(ab, n, kl, ku, b, trans="N", aiter=5, siter=25, diter=5,
     return dict(info=info, fact=fact.raw.decode(), x=x, r=r, siter=si.value,
                 diter=di.value, tolsc=ts.value, res=res.value,
                 afrob=afrob.value)
+
+
+def zgbsvx(ab, n, kl, ku, b, trans="N", fact="E", afb=None, ipiv=None,
+           equed="N", r=None, c=None, ldab=None, openblas=False):
+    """Restated LAPACK zgbsvx (or, with openblas=True, SciPy's OpenBLAS
+    zgbsvx itself) on copies of the inputs.  ab: band with rows 0..kl+ku
+    (ldab rows, column-major flat); b: n x nrhs (or n).  For fact 'F' pass
+    the afb (ldafb = 2kl+ku+1), ipiv, equed, r, c of an earlier call.
+    Returns a dict with every output."""
+    ldab = ldab or kl + ku + 1
+    ldafb = 2 * kl + ku + 1
+    ab = np.array(ab, dtype=np.complex128).reshape(-1).copy()
+    bb = np.array(b, dtype=np.complex128)
+    nrhs = 1 if bb.ndim == 1 else bb.shape[1]
+    bb = np.asfortranarray(bb.reshape(n, nrhs)).copy(order="F")
+    x = np.zeros((n, nrhs), dtype=np.complex128, order="F")
+    afb = (np.zeros(ldafb * n, dtype=np.complex128) if afb is None
+           else np.array(afb, dtype=np.complex128).reshape(-1).copy())
+    ipiv = (np.zeros(n, dtype=np.int32) if ipiv is None
+            else np.array(ipiv, dtype=np.int32).copy())
+    r = np.zeros(n) if r is None else np.array(r, dtype=np.float64).copy()
+    c = np.zeros(n) if c is None else np.array(c, dtype=np.float64).copy()
+    eq = C.create_string_buffer(equed.encode(), 1)
+    rcond, rpv = C.c_double(0), C.c_double(0)
+    ferr = np.zeros(nrhs)
+    berr = np.zeros(nrhs)
+    args = [fact.encode(), trans.encode(), n, kl, ku, nrhs, _ptr(ab), ldab,
+            _ptr(afb), ldafb, _ptr(ipiv), C.addressof(eq), _ptr(r), _ptr(c),
+            _ptr(bb), n, _ptr(x), n, C.addressof(rcond), _ptr(ferr),
+            _ptr(berr), C.addressof(rpv)]
+    if openblas:
+        path = openblas_path()
+        info = lib().orc_openblas_zgbsvx(path.encode() if path else None,
+                                         *args)
+        if info == -1000:
+            return None
+    else:
+        info = lib().orc_zgbsvx(*args)
+    return dict(info=info, x=x, ab=ab, afb=afb, ipiv=ipiv,
+                equed=eq.raw.decode(), r=r, c=c, b=bb, rcond=rcond.value,
+                ferr=ferr, berr=berr, rpvgrw=rpv.value)
 
 
 def assemble_packed(S, n, kl, ku, M, D1, D2, ld, cM, cD1, cD2, dirichlet,

@@ -29,6 +29,11 @@ class Bsmbsm(C.Structure):
                                        "KU", "LD")]
 
 
+class Permutation(C.Structure):
+    """Layout of gsl_permutation."""
+    _fields_ = [("size", C.c_size_t), ("data", C.POINTER(C.c_size_t))]
+
+
 class Case(C.Structure):
     _fields_ = [("S", _i), ("n", _i), ("kl", _i), ("ku", _i), ("ld", _i),
                 ("M", _p), ("D1", _p), ("D2", _p), ("a", _p), ("b", _p),
@@ -68,6 +73,19 @@ _SIGS = {
     "suzerain_bsmbsm_dpack": (_i, [_i] * 6 + [_d, _p, _i, _i, _i, _p, _i]),
     "suzerain_bsmbsm_zpack": (_i, [_i] * 6 + [ZC, _p, _i, _i, _i, _p, _i]),
     "suzerain_bsmbsm_zdpack": (_i, [_i] * 6 + [ZC, _p, _i, _i, _i, _p, _i]),
+    "suzerain_bsmbsm_spack": (_i, [_i] * 6 + [C.c_float, _p, _i, _i, _i, _p, _i]),
+    "suzerain_bsmbsm_cpack": (_i, [_i] * 6 + [CC, _p, _i, _i, _i, _p, _i]),
+    "suzerain_bsmbsm_cspack": (_i, [_i] * 6 + [CC, _p, _i, _i, _i, _p, _i]),
+    "suzerain_bsmbsm_spackc": (_i, [_p, _i, _i, C.c_float, _p, _p]),
+    "suzerain_bsmbsm_spackf": (_i, [_p, _i, _i, C.c_float, _p, _p]),
+    "suzerain_bsmbsm_dpackc": (_i, [_p, _i, _i, _d, _p, _p]),
+    "suzerain_bsmbsm_dpackf": (_i, [_p, _i, _i, _d, _p, _p]),
+    "suzerain_bsmbsm_cpackc": (_i, [_p, _i, _i, CC, _p, _p]),
+    "suzerain_bsmbsm_cpackf": (_i, [_p, _i, _i, CC, _p, _p]),
+    "suzerain_bsmbsm_cspackc": (_i, [_p, _i, _i, CC, _p, _p]),
+    "suzerain_bsmbsm_cspackf": (_i, [_p, _i, _i, CC, _p, _p]),
+    "suzerain_bsmbsm_permutation": (C.POINTER(Permutation), [_i, _i]),
+    "sgb_permutation_free": (None, [C.POINTER(Permutation)]),
     "suzerain_bsmbsm_zpackc": (_i, [_p, _i, _i, ZC, _p, _p]),
     "suzerain_bsmbsm_zpackf": (_i, [_p, _i, _i, ZC, _p, _p]),
     "suzerain_bsmbsm_zdpackc": (_i, [_p, _i, _i, ZC, _p, _p]),
@@ -82,6 +100,19 @@ _SIGS = {
                                       _p, _p, _i]),
     "suzerain_lapackext_cgbsv": (_i, [_p, C.c_char, _i, _i, _i, _i, _p, _i,
                                       _p, _p, _i]),
+    "suzerain_lapackext_dgbsv": (_i, [_p, C.c_char, _i, _i, _i, _i, _p, _i,
+                                      _p, _p, _i]),
+    "suzerain_lapackext_sgbsv": (_i, [_p, C.c_char, _i, _i, _i, _i, _p, _i,
+                                      _p, _p, _i]),
+    "suzerain_lapackext_dsgbsvx": (_i, [_p, _p, _i, C.c_char, _i, _i, _i, _p,
+                                        _p, _p, _p, _p, _p, _p, _p, _p, _p,
+                                        _p]),
+    "suzerain_lapack_zgbsvx": (_i, [C.c_char, C.c_char, _i, _i, _i, _i, _p, _i,
+                                    _p, _i, _p, _p, _p, _p, _p, _i, _p, _i,
+                                    _p, _p, _p, _p, _p]),
+    "sgb_zgbsvx_batched": (_i, [C.c_char, C.c_char, _i, _i, _i, _i, _p, _i,
+                                _ll, _p, _i, _ll, _p, _p, _p, _p, _p, _p, _p,
+                                _p, _p, _p, _p, _p]),
     "suzerain_lapackext_zcgbsvx": (_i, [_p, _p, _i, C.c_char, _i, _i, _i, _p,
                                         _p, _p, _p, _p, _p, _p, _p, _p, _p,
                                         _p]),

@@ -37,14 +37,23 @@ def _stale() -> bool:
     if not os.path.exists(LIB):
         return True
     t = os.path.getmtime(LIB)
-    deps = sources() + glob.glob(os.path.join(CSRC, "*.h")) + \
-        glob.glob(os.path.join(CSRC, "*.cuh")) + \
-        [os.path.join(ROOT, "include", "suzerain_gb300.h"), __file__]
+    deps = sources() + _headers()
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def _compile(src: str, nvcc: str, debug: bool) -> str:
-    obj = os.path.join(OBJ_DIR, os.path.basename(src) + ".o")
+def _headers() -> list[str]:
+    return glob.glob(os.path.join(CSRC, "*.h")) + \
+        glob.glob(os.path.join(CSRC, "*.cuh")) + \
+        [os.path.join(ROOT, "include", "suzerain_gb300.h"), __file__]
+
+
+def _compile(src: str, nvcc: str, debug: bool, force: bool = False) -> str:
+    obj = os.path.join(OBJ_DIR, os.path.basename(src) + (".dbg.o" if debug else ".o"))
+    if not force and os.path.exists(obj):
+        # an object newer than its source and every header is current
+        t = os.path.getmtime(obj)
+        if all(os.path.getmtime(d) < t for d in [src] + _headers()):
+            return obj
     inc = ["-I", os.path.join(ROOT, "include"), "-I", CSRC]
     if src.endswith(".cu"):
         cmd = [nvcc, "-std=c++17", *ARCH, "-O3", "-lineinfo", "-Xcompiler",
@@ -71,7 +80,7 @@ def build(force: bool = False, debug: bool = False, verbose: bool = False
     os.makedirs(OBJ_DIR, exist_ok=True)
     srcs = sources()
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
-        objs = list(ex.map(lambda s: _compile(s, nvcc, debug), srcs))
+        objs = list(ex.map(lambda s: _compile(s, nvcc, debug, force), srcs))
     tmp = LIB + ".tmp"
     cmd = [nvcc, *ARCH, "-shared", "-cudart=static", "-o", tmp, *objs,
            "-lpthread"]

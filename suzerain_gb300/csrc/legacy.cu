@@ -9,6 +9,7 @@
 
 #include <algorithm>
 #include <cctype>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -160,6 +161,15 @@ __device__ __forceinline__ TT pack_val(TT alpha, TS b);
 template <> __device__ __forceinline__ double pack_val(double a, double b) { return a * b; }
 template <> __device__ __forceinline__ double2 pack_val(double2 a, double2 b) { return cx_mul(a, b); }
 template <> __device__ __forceinline__ double2 pack_val(double2 a, double b) { return make_double2(a.x * b, a.y * b); }
+template <> __device__ __forceinline__ float pack_val(float a, float b) { return a * b; }
+template <> __device__ __forceinline__ float2 pack_val(float2 a, float2 b) { return cx_mul(a, b); }
+template <> __device__ __forceinline__ float2 pack_val(float2 a, float b) { return make_float2(a.x * b, a.y * b); }
+
+// alpha == 0 in every component: B is not read
+static bool all_zero(float a) { return a == 0; }
+static bool all_zero(double a) { return a == 0; }
+static bool all_zero(const sgb_complex_float &a) { return a.real() == 0 && a.imag() == 0; }
+static bool all_zero(const sgb_complex_double &a) { return a.real() == 0 && a.imag() == 0; }
 
 template <typename TS, typename TT>
 __global__ void k_pack(int S, int n, int ihat, int jhat, int kl, int ku, TT alpha, bool azero,
@@ -200,9 +210,7 @@ static int pack_impl(int S, int n, int ihat, int jhat, int kl, int ku, UT alpha,
     if (n == 0 || S == 0) return 0;
     TT a;
     std::memcpy(&a, &alpha, sizeof a);
-    double comps[2] = {0, 0};       // alpha == 0 in every component: B unread
-    std::memcpy(comps, &alpha, sizeof alpha);
-    const bool azero = comps[0] == 0 && (sizeof alpha == sizeof(double) || comps[1] == 0);
+    const bool azero = all_zero(alpha);
     const int N = S * n;
     Stage sb(azero ? nullptr : b, azero ? 0 : (size_t) ldb * n * sizeof(US), true);
     // Positions written: column Cj, offsets 0..KL+KU -> extent (N-1)*ldpapt + KL+KU+1.
@@ -228,6 +236,36 @@ extern "C" int suzerain_bsmbsm_zdpack(int S, int n, int ihat, int jhat, int kl, 
                                       const sgb_complex_double alpha, const double *b, int ldb,
                                       int KL, int KU, sgb_complex_double *papt, int ldpapt)
 { return pack_impl<double, double2>(S, n, ihat, jhat, kl, ku, alpha, b, ldb, KL, KU, papt, ldpapt); }
+
+extern "C" int suzerain_bsmbsm_spack(int S, int n, int ihat, int jhat, int kl, int ku,
+                                     const float alpha, const float *b, int ldb, int KL, int KU,
+                                     float *papt, int ldpapt)
+{ return pack_impl<float, float>(S, n, ihat, jhat, kl, ku, alpha, b, ldb, KL, KU, papt, ldpapt); }
+extern "C" int suzerain_bsmbsm_cpack(int S, int n, int ihat, int jhat, int kl, int ku,
+                                     const sgb_complex_float alpha, const sgb_complex_float *b,
+                                     int ldb, int KL, int KU, sgb_complex_float *papt, int ldpapt)
+{ return pack_impl<float2, float2>(S, n, ihat, jhat, kl, ku, alpha, b, ldb, KL, KU, papt, ldpapt); }
+extern "C" int suzerain_bsmbsm_cspack(int S, int n, int ihat, int jhat, int kl, int ku,
+                                      const sgb_complex_float alpha, const float *b, int ldb,
+                                      int KL, int KU, sgb_complex_float *papt, int ldpapt)
+{ return pack_impl<float, float2>(S, n, ihat, jhat, kl, ku, alpha, b, ldb, KL, KU, papt, ldpapt); }
+
+// packc (LD x N target) and packf (papt + KL, leading dimension LD + KL) for
+// the s, d, c and cs variants; z and zd follow below.
+#define SGB_PACKCF(P, TA, TB, TP)                                                          \
+    extern "C" int suzerain_bsmbsm_##P##packc(const suzerain_bsmbsm *A, int ihat, int jhat,  \
+                                              const TA alpha, const TB *b, TP *papt)        \
+    { return suzerain_bsmbsm_##P##pack(A->S, A->n, ihat, jhat, A->kl, A->ku, alpha, b, A->ld, \
+                                       A->KL, A->KU, papt, A->LD); }                        \
+    extern "C" int suzerain_bsmbsm_##P##packf(const suzerain_bsmbsm *A, int ihat, int jhat,  \
+                                              const TA alpha, const TB *b, TP *papt)        \
+    { return suzerain_bsmbsm_##P##pack(A->S, A->n, ihat, jhat, A->kl, A->ku, alpha, b, A->ld, \
+                                       A->KL, A->KU, papt + A->KL, A->LD + A->KL); }
+SGB_PACKCF(s, float, float, float)
+SGB_PACKCF(d, double, double, double)
+SGB_PACKCF(c, sgb_complex_float, sgb_complex_float, sgb_complex_float)
+SGB_PACKCF(cs, sgb_complex_float, float, sgb_complex_float)
+#undef SGB_PACKCF
 
 extern "C" int suzerain_bsmbsm_zpackc(const suzerain_bsmbsm *A, int ihat, int jhat,
                                       const sgb_complex_double alpha, const sgb_complex_double *b,
@@ -472,6 +510,308 @@ extern "C" int suzerain_lapackext_cgbsv(char *const fact, const char trans, cons
         *fact = 'F';
     }
     if (!info) info = suzerain_lapack_cgbtrs(trans, n, kl, ku, nrhs, ab, ldab, ipiv, b, ldb);
+    return info;
+}
+
+// ---------------------------------------------------------------------------
+// Real drop-ins through the complex kernels: the band and right-hand sides
+// are promoted with zero imaginary parts, which stay zero through every
+// operation of the factor and solves (pivot metric |re| + |im| = |re|), and
+// the real parts come back.
+// ---------------------------------------------------------------------------
+template <typename R, typename C2>
+__global__ void k_promote_real(long long n, const R *__restrict__ a, C2 *__restrict__ z)
+{
+    const long long i = (long long) blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) { C2 v; v.x = a[i]; v.y = 0; z[i] = v; }
+}
+template <typename R, typename C2>
+__global__ void k_real_part(long long n, const C2 *__restrict__ z, R *__restrict__ a)
+{
+    const long long i = (long long) blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] = z[i].x;
+}
+
+template <typename R, typename C2, typename CU>
+static int gbsv_real(char *fact, char trans, int n, int kl, int ku, int nrhs, R *ab, int ldab,
+                     int *ipiv, R *b, int ldb,
+                     int (*zsolve)(char *, char, int, int, int, int, CU *, int, int *, CU *, int))
+{
+    // invalid arguments and empty problems: the complex driver answers
+    if (n <= 0 || nrhs < 0 || kl < 0 || ku < 0 || ldab < 2 * kl + ku + 1 || ldb < n)
+        return zsolve(fact, trans, n, kl, ku, nrhs, nullptr, ldab, ipiv, nullptr, ldb);
+    const long long na = (long long) ldab * n, nb = (long long) ldb * nrhs;
+    Stage sab(ab, na * sizeof(R), true), sb(b, nb * sizeof(R), true);
+    if (sab.err || sb.err) return err_of(sab.err ? sab.err : sb.err, "gbsv staging");
+    C2 *za = nullptr, *zb = nullptr;
+    cudaError_t e = cudaMalloc(&za, na * sizeof(C2));
+    if (e == cudaSuccess) e = cudaMalloc(&zb, std::max(nb, 1ll) * sizeof(C2));
+    if (e == cudaSuccess) {
+        k_promote_real<R, C2><<<(unsigned) ((na + 255) / 256), 256>>>(na, (const R *) sab.dev, za);
+        if (nb) k_promote_real<R, C2><<<(unsigned) ((nb + 255) / 256), 256>>>(nb, (const R *) sb.dev, zb);
+        e = cudaGetLastError();
+    }
+    int info = 0;
+    if (e == cudaSuccess) {
+        info = zsolve(fact, trans, n, kl, ku, nrhs, (CU *) za, ldab, ipiv, (CU *) zb, ldb);
+        k_real_part<R, C2><<<(unsigned) ((na + 255) / 256), 256>>>(na, za, (R *) sab.dev);
+        if (nb) k_real_part<R, C2><<<(unsigned) ((nb + 255) / 256), 256>>>(nb, zb, (R *) sb.dev);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    }
+    if (za) cudaFree(za);
+    if (zb) cudaFree(zb);
+    if (e == cudaSuccess) e = sab.back();
+    if (e == cudaSuccess) e = sb.back();
+    if (e != cudaSuccess) return err_of(e, "suzerain_lapackext_gbsv (real)");
+    return info;
+}
+
+extern "C" int suzerain_lapackext_dgbsv(char *const fact, const char trans, const int n,
+                                        const int kl, const int ku, const int nrhs, double *ab,
+                                        const int ldab, int *ipiv, double *b, const int ldb)
+{
+    return gbsv_real<double, double2, sgb_complex_double>(fact, trans, n, kl, ku, nrhs, ab, ldab,
+                                                          ipiv, b, ldb, suzerain_lapackext_zgbsv);
+}
+extern "C" int suzerain_lapackext_sgbsv(char *const fact, const char trans, const int n,
+                                        const int kl, const int ku, const int nrhs, float *ab,
+                                        const int ldab, int *ipiv, float *b, const int ldb)
+{
+    return gbsv_real<float, float2, sgb_complex_float>(fact, trans, n, kl, ku, nrhs, ab, ldab,
+                                                       ipiv, b, ldb, suzerain_lapackext_cgbsv);
+}
+
+// float32 factor at the start of a float64 buffer (dsgbsvx's in-place
+// demotion) from the complex64 factor at the start of the complex128 one
+__global__ void k_real_part_f2(long long n, const float2 *__restrict__ z, float *__restrict__ a)
+{
+    const long long i = (long long) blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] = z[i].x;
+}
+
+extern "C" int suzerain_lapackext_dsgbsvx(char *const fact, int *const apprx, const int aiter,
+                                          char trans, const int n, const int kl, const int ku,
+                                          double *const ab, double *const afrob,
+                                          double *const afb, int *const ipiv, double *const b,
+                                          double *const x, int *const siter, int *const diter,
+                                          double *const tolsc, double *const r,
+                                          double *const res)
+{
+    const char f = (char) std::toupper((unsigned char) *fact);
+    const char t = (char) std::toupper((unsigned char) trans);
+    const bool bad = (f != 'N' && f != 'S' && f != 'D') || *apprx < 0 || aiter < 0 ||
+                     (t != 'N' && t != 'T' && t != 'C') || n < 0 || kl < 0 || ku < 0 ||
+                     *tolsc < 0 || (*siter < 0 && *diter < 0);
+    if (bad || n == 0 || kl + 1 > 64 || kl + ku + 1 > 192)
+        return suzerain_lapackext_zcgbsvx(fact, apprx, aiter, trans, n, kl, ku, nullptr, afrob,
+                                          nullptr, ipiv, nullptr, nullptr, siter, diter, tolsc,
+                                          nullptr, res);
+    const long long na = (long long) (kl + ku + 1) * n, nf = (long long) (2 * kl + ku + 1) * n;
+    Stage sab(ab, na * sizeof(double), true), sb(b, n * sizeof(double), true);
+    Stage sx(x, n * sizeof(double), false), sr(r, r ? n * sizeof(double) : 0, false);
+    Stage sf(afb, afb ? nf * sizeof(double) : 0, true);
+    if (sab.err || sb.err || sx.err || sr.err || sf.err) return err_of(cudaErrorMemoryAllocation, "dsgbsvx staging");
+    double2 *za = nullptr, *zb = nullptr, *zx = nullptr, *zr = nullptr, *zf = nullptr;
+    cudaError_t e = cudaMalloc(&za, na * sizeof(double2));
+    if (e == cudaSuccess) e = cudaMalloc(&zb, n * sizeof(double2));
+    if (e == cudaSuccess) e = cudaMalloc(&zx, n * sizeof(double2));
+    if (e == cudaSuccess) e = cudaMalloc(&zr, n * sizeof(double2));
+    if (e == cudaSuccess) e = cudaMalloc(&zf, nf * sizeof(double2));
+    if (e == cudaSuccess) {
+        k_promote_real<double, double2><<<(unsigned) ((na + 255) / 256), 256>>>(na, (const double *) sab.dev, za);
+        k_promote_real<double, double2><<<(unsigned) ((n + 255) / 256), 256>>>(n, (const double *) sb.dev, zb);
+        e = cudaGetLastError();
+    }
+    int info = 0;
+    if (e == cudaSuccess) {
+        info = suzerain_lapackext_zcgbsvx(fact, apprx, aiter, trans, n, kl, ku,
+                                          (sgb_complex_double *) za, afrob,
+                                          (sgb_complex_double *) zf, ipiv,
+                                          (sgb_complex_double *) zb, (sgb_complex_double *) zx,
+                                          siter, diter, tolsc,
+                                          r ? (sgb_complex_double *) zr : nullptr, res);
+        k_real_part<double, double2><<<(unsigned) ((n + 255) / 256), 256>>>(n, zx, (double *) sx.dev);
+        if (r) k_real_part<double, double2><<<(unsigned) ((n + 255) / 256), 256>>>(n, zr, (double *) sr.dev);
+        if (afb && *fact == 'S')
+            k_real_part_f2<<<(unsigned) ((nf + 255) / 256), 256>>>(nf, (const float2 *) zf, (float *) sf.dev);
+        else if (afb && *fact == 'D')
+            k_real_part<double, double2><<<(unsigned) ((nf + 255) / 256), 256>>>(nf, zf, (double *) sf.dev);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    }
+    cudaFree(za); cudaFree(zb); cudaFree(zx); cudaFree(zr); cudaFree(zf);
+    if (e == cudaSuccess) e = sx.back();
+    if (e == cudaSuccess && r) e = sr.back();
+    if (e == cudaSuccess && afb) e = sf.back();
+    if (e != cudaSuccess) return err_of(e, "suzerain_lapackext_dsgbsvx");
+    return info;
+}
+
+// q as a permutation object with gsl_permutation's layout (size, data),
+// both blocks from malloc so that gsl_permutation_free releases it.
+extern "C" sgb_permutation *suzerain_bsmbsm_permutation(int S, int n)
+{
+    if (S <= 0 || n <= 0) return nullptr;
+    const size_t N = (size_t) S * n;
+    sgb_permutation *p = (sgb_permutation *) std::malloc(sizeof(sgb_permutation));
+    if (!p) return nullptr;
+    p->size = N;
+    p->data = (size_t *) std::malloc(N * sizeof(size_t));
+    if (!p->data) { std::free(p); return nullptr; }
+    for (size_t i = 0; i < N; ++i) p->data[i] = (size_t) suzerain_bsmbsm_q(S, n, (int) i);
+    return p;
+}
+extern "C" void sgb_permutation_free(sgb_permutation *p)
+{
+    if (!p) return;
+    std::free(p->data);
+    std::free(p);
+}
+
+// ---------------------------------------------------------------------------
+// zgbsvx (LAPACK's expert driver): the right-hand sides run as systems of the
+// batched driver that share one band (stride 0); each factors the same band
+// into its own slot, so the factor, pivots, scalings and rcond of system 0
+// are those of every right-hand side.
+// ---------------------------------------------------------------------------
+extern "C" int suzerain_lapack_zgbsvx(const char fact_in, const char trans_in, const int n,
+                                      const int kl, const int ku, const int nrhs,
+                                      sgb_complex_double *ab, const int ldab,
+                                      sgb_complex_double *afb, const int ldafb, int *ipiv,
+                                      char *equed, double *r, double *c, sgb_complex_double *b,
+                                      const int ldb, sgb_complex_double *x, const int ldx,
+                                      double *rcond, double *ferr, double *berr,
+                                      sgb_complex_double *work, double *rwork)
+{
+    (void) work;
+    const char fact = (char) std::toupper((unsigned char) fact_in);
+    const char trans = (char) std::toupper((unsigned char) trans_in);
+    // argument checks in ZGBSVX's order (INFO = -i for argument i)
+    if (fact != 'N' && fact != 'E' && fact != 'F') return -1;
+    if (trans != 'N' && trans != 'T' && trans != 'C') return -2;
+    if (n < 0) return -3;
+    if (kl < 0) return -4;
+    if (ku < 0) return -5;
+    if (nrhs < 0) return -6;
+    if (ldab < kl + ku + 1) return -8;
+    if (ldafb < 2 * kl + ku + 1) return -10;
+    if (!equed || !rcond) return -12;
+    Stage se(equed, 1, true);
+    Stage sr(r, (size_t) std::max(n, 1) * sizeof(double), true);
+    Stage sc(c, (size_t) std::max(n, 1) * sizeof(double), true);
+    if (se.err || sr.err || sc.err) return err_of(cudaErrorMemoryAllocation, "zgbsvx staging");
+    char eq = 'N';
+    if (fact == 'F') {
+        cudaError_t e = cudaMemcpy(&eq, se.dev, 1, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return err_of(e, "zgbsvx equed");
+        eq = (char) std::toupper((unsigned char) eq);
+        if (eq != 'N' && eq != 'R' && eq != 'C' && eq != 'B') return -12;
+        std::vector<double> h(n);
+        if ((eq == 'R' || eq == 'B') && n > 0) {
+            e = cudaMemcpy(h.data(), sr.dev, n * sizeof(double), cudaMemcpyDeviceToHost);
+            if (e != cudaSuccess) return err_of(e, "zgbsvx r");
+            if (*std::min_element(h.begin(), h.end()) <= 0) return -13;
+        }
+        if ((eq == 'C' || eq == 'B') && n > 0) {
+            e = cudaMemcpy(h.data(), sc.dev, n * sizeof(double), cudaMemcpyDeviceToHost);
+            if (e != cudaSuccess) return err_of(e, "zgbsvx c");
+            if (*std::min_element(h.begin(), h.end()) <= 0) return -14;
+        }
+    }
+    if (ldb < std::max(1, n)) return -16;
+    if (ldx < std::max(1, n)) return -18;
+    if (n == 0) {
+        if (fact != 'F') { char nn = 'N'; cudaMemcpy(se.dev, &nn, 1, cudaMemcpyHostToDevice); se.back(); }
+        *rcond = 1;
+        for (int j = 0; j < nrhs; ++j) { if (ferr) ferr[j] = 0; if (berr) berr[j] = 0; }
+        if (rwork) rwork[0] = 1;
+        return 0;
+    }
+    if (kl + 1 > 64 || kl + ku + 1 > 192) {
+        sgb_set_error(cudaErrorNotSupported, "suzerain_lapack_zgbsvx: bandwidth beyond KL < 64, KL + KU < 192", __FILE__, __LINE__);
+        return -4;
+    }
+    const int ns = std::max(nrhs, 1);
+    Stage sab(ab, (size_t) ldab * n * sizeof(double2), true);
+    Stage saf(afb, (size_t) ldafb * n * sizeof(double2), fact == 'F');
+    Stage spv(ipiv, (size_t) n * sizeof(int), fact == 'F');
+    Stage sb(nrhs ? b : nullptr, (size_t) ldb * nrhs * sizeof(double2), true);
+    Stage sx(nrhs ? x : nullptr, (size_t) ldx * nrhs * sizeof(double2), true);
+    if (sab.err || saf.err || spv.err || sb.err || sx.err || !saf.dev || !spv.dev)
+        return err_of(sab.err ? sab.err : cudaErrorInvalidValue, "zgbsvx staging");
+    // per-system copies: b, x, ipiv, equed, r, c (replicated for 'F')
+    const size_t vn = (size_t) ns * n;
+    double2 *bz = nullptr, *xz = nullptr;
+    int *pz = nullptr, *iz = nullptr;
+    double *rz = nullptr, *cz = nullptr, *dz = nullptr;
+    char *ez = nullptr;
+    cudaError_t e = cudaMalloc(&bz, vn * sizeof(double2));
+    if (e == cudaSuccess) e = cudaMalloc(&xz, vn * sizeof(double2));
+    if (e == cudaSuccess) e = cudaMalloc(&pz, vn * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&iz, ns * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&rz, vn * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&cz, vn * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&dz, 4 * (size_t) ns * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&ez, ns);
+    if (e == cudaSuccess && nrhs) {
+        e = cudaMemcpy2D(bz, n * sizeof(double2), sb.dev, ldb * sizeof(double2), n * sizeof(double2), nrhs, cudaMemcpyDeviceToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy2D(xz, n * sizeof(double2), sx.dev, ldx * sizeof(double2), n * sizeof(double2), nrhs, cudaMemcpyDeviceToDevice);
+    } else if (e == cudaSuccess) {
+        e = cudaMemset(bz, 0, vn * sizeof(double2));
+    }
+    for (int j = 0; j < ns && e == cudaSuccess; ++j) {
+        if (fact == 'F') e = cudaMemcpy(pz + (size_t) j * n, spv.dev, n * sizeof(int), cudaMemcpyDeviceToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(rz + (size_t) j * n, sr.dev, n * sizeof(double), cudaMemcpyDeviceToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(cz + (size_t) j * n, sc.dev, n * sizeof(double), cudaMemcpyDeviceToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(ez + j, &eq, 1, cudaMemcpyHostToDevice);
+    }
+    int info = 0;
+    if (e == cudaSuccess) {
+        GbsvxArgs A;
+        A.nsys = ns; A.fact = fact; A.trans = trans; A.g = {n, kl, ku};
+        A.ab = (const double2 *) sab.dev; A.ab_out = (double2 *) sab.dev; A.ldab = ldab; A.ab_stride = 0;
+        A.afb = (double2 *) saf.dev; A.ldafb = ldafb; A.afb_stride = 0;
+        A.ipiv = pz; A.equed = ez; A.R = rz; A.C = cz;
+        A.b = bz; A.b_out = bz; A.x = xz;
+        A.rcond = dz; A.ferr = dz + ns; A.berr = dz + 2 * ns; A.rpvgrw = dz + 3 * ns; A.info = iz;
+        int rc = zgbsvx_batched(A, 0);
+        if (rc) { if (pz) cudaFree(pz); cudaFree(bz); cudaFree(xz); cudaFree(iz); cudaFree(rz); cudaFree(cz); cudaFree(dz); cudaFree(ez); return rc; }
+        std::vector<double> hd(4 * (size_t) ns);
+        e = cudaMemcpy(hd.data(), dz, hd.size() * sizeof(double), cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess) e = cudaMemcpy(&info, iz, sizeof(int), cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess) e = cudaMemcpy(&eq, ez, 1, cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess) {
+            *rcond = hd[0];
+            if (rwork) rwork[0] = hd[3 * ns];
+            const bool solved = info == 0 || info == n + 1;
+            for (int j = 0; j < nrhs && solved; ++j) {
+                if (ferr) ferr[j] = hd[ns + j];
+                if (berr) berr[j] = hd[2 * ns + j];
+            }
+            if (nrhs) {
+                e = cudaMemcpy2D(sb.dev, ldb * sizeof(double2), bz, n * sizeof(double2), n * sizeof(double2), nrhs, cudaMemcpyDeviceToDevice);
+                if (e == cudaSuccess && solved)
+                    e = cudaMemcpy2D(sx.dev, ldx * sizeof(double2), xz, n * sizeof(double2), n * sizeof(double2), nrhs, cudaMemcpyDeviceToDevice);
+            }
+        }
+        if (e == cudaSuccess && fact != 'F') {
+            e = cudaMemcpy(spv.dev, pz, n * sizeof(int), cudaMemcpyDeviceToDevice);
+            if (e == cudaSuccess) e = cudaMemcpy(se.dev, &eq, 1, cudaMemcpyHostToDevice);
+            if (e == cudaSuccess && fact == 'E') e = cudaMemcpy(sr.dev, rz, n * sizeof(double), cudaMemcpyDeviceToDevice);
+            if (e == cudaSuccess && fact == 'E') e = cudaMemcpy(sc.dev, cz, n * sizeof(double), cudaMemcpyDeviceToDevice);
+        }
+    }
+    cudaFree(bz); cudaFree(xz); cudaFree(pz); cudaFree(iz); cudaFree(rz); cudaFree(cz); cudaFree(dz); cudaFree(ez);
+    if (e == cudaSuccess) e = sab.back();
+    if (e == cudaSuccess && fact != 'F') e = saf.back();
+    if (e == cudaSuccess && fact != 'F') e = spv.back();
+    if (e == cudaSuccess) e = se.back();
+    if (e == cudaSuccess && fact == 'E') e = sr.back();
+    if (e == cudaSuccess && fact == 'E') e = sc.back();
+    if (e == cudaSuccess) e = sb.back();
+    if (e == cudaSuccess) e = sx.back();
+    if (e != cudaSuccess) return err_of(e, "suzerain_lapack_zgbsvx");
     return info;
 }
 

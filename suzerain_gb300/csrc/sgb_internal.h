@@ -104,4 +104,30 @@ struct ApplyArgs {
 };
 cudaError_t launch_model_apply(const ApplyArgs &a, cudaStream_t st);
 
+// Batched complex128 expert driver (LAPACK zgbsvx semantics, one right-hand
+// side per system).  Device pointers unless noted; per-system strides are
+// in complex elements (b, x: N per system; ipiv, R, C: N per system).
+struct GbsvxArgs {
+    int nsys = 0;
+    char fact = 'N';             // 'N' factor, 'E' equilibrate and factor, 'F' factor given
+    char trans = 'N';
+    FactorGeom g{};
+    const double2 *ab = nullptr; // band rows 0..KL+KU (ld ldab)
+    double2 *ab_out = nullptr;   // equilibrated band written back (may equal ab)
+    int ldab = 0;
+    long long ab_stride = 0;
+    double2 *afb = nullptr;      // LAPACK gbtrf storage: input for 'F', output otherwise (may be null)
+    int ldafb = 0;
+    long long afb_stride = 0;
+    int *ipiv = nullptr;         // input for 'F', output otherwise
+    char *equed = nullptr;       // input for 'F', output otherwise
+    double *R = nullptr, *C = nullptr;   // input for 'F', output for 'E'
+    const double2 *b = nullptr;
+    double2 *b_out = nullptr;    // scaled right-hand side (may equal b)
+    double2 *x = nullptr;
+    double *rcond = nullptr, *ferr = nullptr, *berr = nullptr, *rpvgrw = nullptr;  // host or device
+    int *info = nullptr;         // device
+};
+int zgbsvx_batched(const GbsvxArgs &a, cudaStream_t st);
+
 }  // namespace sgb

@@ -1,7 +1,9 @@
 // Drives include/suzerain_gb300_solver.hpp the way Suzerain's operators
 // drive suzerain::bsmbsm_solver: pack S x S banded blocks into P A P^T,
-// supply b, solve, demand x; checks A x = b against a dense copy of A for
-// both the zgbsv and the zcgbsvx specifications.  Prints "OK ..." on success.
+// supply b, solve, demand x (twice: the second solve reuses the factor);
+// checks A x = b against a dense copy of A for the zgbsv, zgbsvx (with and
+// without equilibration) and zcgbsvx specifications.  Prints "OK ..." on
+// success.
 #include "suzerain_gb300_solver.hpp"
 
 #include <cmath>
@@ -33,7 +35,8 @@ int main()
     std::vector<cd> b(N), x(N);
     for (auto &v : b) v = cd(nd(rng), nd(rng));
     double worst = 0;
-    for (const char *text : {"zgbsv", "zcgbsvx,aiter=5,siter=25,diter=5,tolsc=145"}) {
+    for (const char *text : {"zgbsv", "zgbsvx,equil=true", "zgbsvx",
+                             "zcgbsvx,aiter=5,siter=25,diter=5,tolsc=145"}) {
         suzerain_gb300::specification_zgbsv spec(text);
         auto solver = suzerain_gb300::bsmbsm_solver::build(A, spec, 1);
         for (int i = 0; i < S; ++i)
@@ -44,6 +47,7 @@ int main()
                 if (rc) { std::printf("FAIL pack %d\n", rc); return 1; }
             }
         solver->supplied_PAPT();
+        for (int rep = 0; rep < 2; ++rep) {
         if (solver->supply_b(b.data(), 0)) { std::printf("FAIL supply_b\n"); return 1; }
         solver->solve('N');
         if (solver->demand_x(x.data(), 0)) { std::printf("FAIL demand_x\n"); return 1; }
@@ -64,6 +68,7 @@ int main()
         worst = std::max(worst, berr);
         for (const auto &line : solver->summarize_statistics()) std::printf("# %s\n", line.c_str());
         std::printf("%s berr=%.3e fact=%c\n", std::string(spec).c_str(), berr, solver->fact());
+        }
     }
     if (worst > 1e-13) { std::printf("FAIL berr %.3e\n", worst); return 1; }
     // an invalid specification is rejected with the reference's message

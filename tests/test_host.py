@@ -190,3 +190,14 @@ def test_cpp_solver_shim_compiles(tmp_path):
                         os.path.join(root, "tests", "solver_shim_check.cpp")],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_bsmbsm_permutation_layout(native):
+    """suzerain_bsmbsm_permutation: gsl_permutation layout holding q."""
+    p = native.suzerain_bsmbsm_permutation(5, 12)
+    assert p
+    assert p.contents.size == 60
+    assert [p.contents.data[i] for i in range(60)] == \
+        [native.suzerain_bsmbsm_q(5, 12, i) for i in range(60)]
+    native.sgb_permutation_free(p)
+    assert not native.suzerain_bsmbsm_permutation(0, 12)

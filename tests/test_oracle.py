@@ -272,3 +272,53 @@ def test_gbmv_matches_reference(oracle):
                                   a.ctypes.data, lda, x.ctypes.data, 1,
                                   oracle._z(0.5), y2.ctypes.data, 1)
             assert np.allclose(y1, y2, rtol=1e-13, atol=1e-13)
+
+
+# --------------------------------------------------------------------------
+# zgbsvx: the restatement against LAPACK's own zgbsvx (SciPy's OpenBLAS, the
+# routine suzerain_lapack_zgbsvx forwards to)
+# --------------------------------------------------------------------------
+@pytest.mark.parametrize("trans", ["N", "T", "C"])
+@pytest.mark.parametrize("fact", ["N", "E"])
+@pytest.mark.parametrize("scaled", [False, True])
+def test_zgbsvx_matches_lapack(oracle, trans, fact, scaled):
+    from gbsvx_cases import GEOMS, assert_close, band, rhs
+    if oracle.openblas_path() is None:
+        pytest.skip("SciPy's OpenBLAS not found")
+    for k, (n, kl, ku) in enumerate(GEOMS):
+        ab, _ = band(n, kl, ku, seed=100 + k, scaled=scaled)
+        b = rhs(n, 2, seed=100 + k)
+        got = oracle.zgbsvx(ab, n, kl, ku, b, trans=trans, fact=fact)
+        want = oracle.zgbsvx(ab, n, kl, ku, b, trans=trans, fact=fact, openblas=True)
+        if want is None:
+            pytest.skip("scipy_zgbsvx_ not exported")
+        assert_close(got, want, n, kl, ku, f"{n},{kl},{ku},{trans},{fact}")
+        np.testing.assert_array_equal(got["ipiv"], want["ipiv"])
+
+
+def test_zgbsvx_fact_f_and_singular(oracle):
+    """fact 'F' reuses an earlier call's factor and scalings; a zero column
+    stops at the factor with info = its index, rcond = 0, x untouched."""
+    from gbsvx_cases import assert_close, band, rhs
+    if oracle.openblas_path() is None:
+        pytest.skip("SciPy's OpenBLAS not found")
+    n, kl, ku = 40, 5, 4
+    ab, _ = band(n, kl, ku, seed=7, scaled=True)
+    b = rhs(n, 1, seed=7)
+    first = oracle.zgbsvx(ab, n, kl, ku, b, fact="E")
+    assert first["equed"] == "B"
+    kw = dict(fact="F", afb=first["afb"], ipiv=first["ipiv"], equed=first["equed"],
+              r=first["r"], c=first["c"])
+    b2 = rhs(n, 3, seed=8)
+    for trans in "NTC":
+        got = oracle.zgbsvx(first["ab"], n, kl, ku, b2, trans=trans, **kw)
+        want = oracle.zgbsvx(first["ab"], n, kl, ku, b2, trans=trans, openblas=True, **kw)
+        if want is None:
+            pytest.skip("scipy_zgbsvx_ not exported")
+        assert_close(got, want, n, kl, ku, "F" + trans)
+    ab, _ = band(10, 2, 2, seed=9, singular_col=4)
+    got = oracle.zgbsvx(ab, 10, 2, 2, rhs(10, 1, 9), fact="N")
+    want = oracle.zgbsvx(ab, 10, 2, 2, rhs(10, 1, 9), fact="N", openblas=True)
+    assert got["info"] == want["info"] == 5
+    assert_close(got, want, 10, 2, 2, "singular")
+    assert not got["x"].any()
