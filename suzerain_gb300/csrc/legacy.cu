@@ -696,7 +696,8 @@ extern "C" int suzerain_lapack_zgbsvx(const char fact_in, const char trans_in, c
     if (nrhs < 0) return -6;
     if (ldab < kl + ku + 1) return -8;
     if (ldafb < 2 * kl + ku + 1) return -10;
-    if (!equed || !rcond) return -12;
+    if (!equed) return -12;
+    if (!rcond) return -19;
     Stage se(equed, 1, true);
     Stage sr(r, (size_t) std::max(n, 1) * sizeof(double), true);
     Stage sc(c, (size_t) std::max(n, 1) * sizeof(double), true);
