@@ -406,6 +406,12 @@ int sgb_zgbsvx_batched(char fact, char trans, int nsys, int n, int kl, int ku,
                        double *rcond, double *ferr, double *berr, double *rpvgrw,
                        int *info, void *stream);
 
+/** Records in flight per system of the quad-lane solves (trans 'N' with a
+ *  y workspace): 2, 4, 8 or 16 for the forward and the backward sweep (0
+ *  keeps the current value; defaults 8 and 4).  Returns -1 for other values.
+ *  Process-wide; results do not depend on it. */
+int sgb_gbtrs_set_quad_depth(int fwd, int bwd);
+
 /** Row-panel factor -> LAPACK gbtrf storage ((2KL+KU+1) x N per system). */
 int sgb_factor_to_lapack(char prec, int nsys, int N, int KL, int KU,
                          const void *fac, void *ab, void *stream);
@@ -475,6 +481,10 @@ size_t sgb_plan_estimate_bytes(const sgb_case *host_case, int nsys, int max_doub
                                char method);
 /** Device bytes the plan holds. */
 size_t sgb_plan_device_bytes(const sgb_plan *p);
+/** Plans draw device memory from a stream-ordered pool that keeps freed
+ *  blocks for the next plan; this returns cached blocks beyond keep_bytes
+ *  to the device. */
+int sgb_plan_pool_trim(size_t keep_bytes);
 
 /** One implicit substep for every system of the plan:
  *    y = P (M + phi_exp L) u          (explicit operator, Dirichlet rows 0)

@@ -5,9 +5,10 @@
 // written in the permuted order that aPxpby('N') produces).
 //
 // The model form applies the three real bands once per component and mixes
-// the results with the S x S coefficients: ~(3 S n ld + 3 S^2 n) complex-real
-// multiply-adds instead of the S^2 n ld complex ones of the packed band,
-// which matters on a part whose FP64 pipe is 1/62 of its FP32 pipe.
+// the results with the S x S coefficients (complex for M, real for D1 and
+// D2): ~(3 S n ld + 2 S^2 n) complex-real multiply-adds and S^2 n complex
+// ones instead of the S^2 n ld complex ones of the packed band, which
+// matters on a part whose FP64 pipe is 1/62 of its FP32 pipe.
 #include "sgb_internal.h"
 
 namespace sgb {
@@ -114,14 +115,19 @@ k_model_op(int nsys, ModelSource ms,
     const int S = cs.S, n = cs.n, N = S * n, kl = cs.kl, ku = cs.ku, ld = cs.ld;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     double2 *xs = reinterpret_cast<double2 *>(smem_raw);   // permuted x
-    double2 *cf = xs + N;                                   // 3 S^2 coefficients
+    // S^2 complex M coefficients, then the D1 and D2 ones, which
+    // sgb_block_coefs makes real (a, b scaled by phi): their products with
+    // the complex band sums take two multiply-adds instead of four, the same
+    // values as the complex product with a zero imaginary part
+    double2 *cf = xs + N;
+    double *cd = reinterpret_cast<double *>(cf + S * S);   // 2 S^2 reals
     const double kx = ms.kx[s], kz = ms.kz[s];
     for (int idx = lane; idx < S * S; idx += 32) {
         sgb_coef cM, cD1, cD2;
         sgb_block_coefs(&cs, idx / S, idx % S, ms.phi, kx, kz, &cM, &cD1, &cD2);
         cf[idx] = make_double2(cM.re, cM.im);
-        cf[S * S + idx] = make_double2(cD1.re, cD1.im);
-        cf[2 * S * S + idx] = make_double2(cD2.re, cD2.im);
+        cd[idx] = cD1.re;
+        cd[S * S + idx] = cD2.re;
     }
     double xn = 0;
     for (int i = lane; i < N; i += 32) {
@@ -160,8 +166,11 @@ k_model_op(int nsys, ModelSource ms,
                 for (int f = 0; f < S; ++f) {
                     const int ef = e * S + f;
                     y = cfma(cf[ef], u[f], y);
-                    y = cfma(cf[S * S + ef], v[f], y);
-                    y = cfma(cf[2 * S * S + ef], w[f], y);
+                    const double c1 = cd[ef], c2 = cd[S * S + ef];
+                    y.x = fma(c1, v[f].x, y.x);
+                    y.y = fma(c1, v[f].y, y.y);
+                    y.x = fma(c2, w[f].x, y.x);
+                    y.y = fma(c2, w[f].y, y.y);
                 }
             }
             double2 out;

@@ -329,6 +329,71 @@ extern "C" int sgb_zcgbsvx_batched(int nsys, int N, int KL, int KU, char trans, 
 }
 
 // ---------------------------------------------------------------------------
+// Plan memory: a stream-ordered pool that keeps freed blocks, so that plans
+// created and destroyed in turn (a serving loop admitting and retiring cases)
+// reuse device memory instead of paying cudaMalloc / cudaFree each time.  A
+// plan's blocks return to the pool only after the work it issued completes:
+// its frees are ordered after an event recorded at the end of each of its
+// calls (per stream), or after a device synchronization when the plan was
+// ever recorded into a CUDA graph (a graph may be replayed at any time).
+// ---------------------------------------------------------------------------
+namespace {
+struct PlanPool {
+    std::mutex mu;
+    cudaMemPool_t pool = nullptr;
+    cudaStream_t st = nullptr;
+    int dev = -1;
+    cudaError_t init()
+    {
+        int d = 0;
+        cudaError_t e = cudaGetDevice(&d);
+        if (e != cudaSuccess) return e;
+        if (pool && d == dev) return cudaSuccess;
+        if (pool) return cudaErrorInvalidDevice;     // one device per process
+        cudaMemPoolProps props;
+        std::memset(&props, 0, sizeof props);
+        props.allocType = cudaMemAllocationTypePinned;
+        props.handleTypes = cudaMemHandleTypeNone;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = d;
+        e = cudaMemPoolCreate(&pool, &props);
+        if (e != cudaSuccess) { pool = nullptr; return e; }
+        unsigned long long keep = ~0ull;
+        e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+        if (e != cudaSuccess) return e;
+        dev = d;
+        return cudaSuccess;
+    }
+    cudaError_t alloc(void **p, size_t bytes)
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        cudaError_t e = init();
+        if (e != cudaSuccess) return e;
+        e = cudaMallocFromPoolAsync(p, bytes, pool, st);
+        if (e == cudaErrorMemoryAllocation) {          // give cached blocks back, retry once
+            cudaGetLastError();
+            cudaStreamSynchronize(st);
+            cudaMemPoolTrimTo(pool, 0);
+            e = cudaMallocFromPoolAsync(p, bytes, pool, st);
+        }
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);   // usable from any stream
+        return e;
+    }
+};
+PlanPool g_pool;
+}  // namespace
+
+extern "C" int sgb_plan_pool_trim(size_t keep_bytes)
+{
+    std::lock_guard<std::mutex> lk(g_pool.mu);
+    if (!g_pool.pool) return 0;
+    SGB_CUDA_TRY(cudaStreamSynchronize(g_pool.st));
+    SGB_CUDA_TRY(cudaMemPoolTrimTo(g_pool.pool, keep_bytes));
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
 // Plan: one resident case
 // ---------------------------------------------------------------------------
 struct sgb_plan {
@@ -352,13 +417,33 @@ struct sgb_plan {
     std::vector<void *> allocs;
     std::mutex mu;
 
+    std::vector<std::pair<cudaStream_t, cudaEvent_t>> done;   // end of the last call per stream
+    bool captured = false;                                     // ever recorded into a graph
+
     int dalloc(void **p, size_t bytes, const char *what)
     {
-        cudaError_t e = cudaMalloc(p, bytes);
+        cudaError_t e = g_pool.alloc(p, bytes);
         if (e != cudaSuccess) return sgb_set_error(e, what, __FILE__, __LINE__);
         allocs.push_back(*p);
         dev_bytes += bytes;
         return 0;
+    }
+    // Marks the end of a call's work on stream st (frees wait for it).
+    void note(cudaStream_t st)
+    {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(st, &cs) != cudaSuccess) { cudaGetLastError(); captured = true; return; }
+        if (cs != cudaStreamCaptureStatusNone) { captured = true; return; }
+        for (auto &d : done)
+            if (d.first == st) { cudaEventRecord(d.second, st); return; }
+        cudaEvent_t ev = nullptr;
+        if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) {
+            cudaGetLastError();
+            captured = true;       // fall back to a device synchronization at destroy
+            return;
+        }
+        cudaEventRecord(ev, st);
+        done.push_back({st, ev});
     }
     ModelSource ms(double phi) const
     {
@@ -445,7 +530,13 @@ extern "C" sgb_plan *sgb_plan_create(const sgb_case *hcase, int nsys, const doub
 extern "C" int sgb_plan_destroy(sgb_plan *p)
 {
     if (!p) return 0;
-    for (void *a : p->allocs) cudaFree(a);
+    if (!p->allocs.empty()) {
+        std::lock_guard<std::mutex> lk(g_pool.mu);
+        if (p->captured) cudaDeviceSynchronize();
+        for (auto &d : p->done) cudaStreamWaitEvent(g_pool.st, d.second, 0);
+        for (void *a : p->allocs) cudaFreeAsync(a, g_pool.st);
+    }
+    for (auto &d : p->done) cudaEventDestroy(d.second);
     if (p->hcount) cudaFreeHost(p->hcount);
     delete p;
     return 0;
@@ -625,8 +716,10 @@ extern "C" int sgb_plan_substep(sgb_plan *p, char method, double phi_exp, double
 {
     if (!p || !u_in || !u_out) return fail("sgb_plan_substep: null argument");
     std::lock_guard<std::mutex> lk(p->mu);
-    return plan_substep(p, (char) toupper(method), phi_exp, phi_imp, u_in, u_out, spec,
-                        (cudaStream_t) stream);
+    const int rc = plan_substep(p, (char) toupper(method), phi_exp, phi_imp, u_in, u_out, spec,
+                                (cudaStream_t) stream);
+    p->note((cudaStream_t) stream);
+    return rc;
 }
 
 extern "C" int sgb_plan_substep_capturable(sgb_plan *p, char method, double phi_exp,
@@ -635,8 +728,10 @@ extern "C" int sgb_plan_substep_capturable(sgb_plan *p, char method, double phi_
 {
     if (!p || !u_in || !u_out) return fail("sgb_plan_substep_capturable: null argument");
     std::lock_guard<std::mutex> lk(p->mu);
-    return plan_substep(p, (char) toupper(method), phi_exp, phi_imp, u_in, u_out, spec,
-                        (cudaStream_t) stream, true);
+    const int rc = plan_substep(p, (char) toupper(method), phi_exp, phi_imp, u_in, u_out, spec,
+                                (cudaStream_t) stream, true);
+    p->note((cudaStream_t) stream);
+    return rc;
 }
 
 extern "C" int sgb_plan_prepare(sgb_plan *p, char method)

@@ -228,9 +228,11 @@ __host__ __device__ inline int quad_pow2(int v)
 // warp reading four consecutive elements each fill the banks twice
 __host__ __device__ inline int quad_pad(int e) { return e + ((4 - e % 16) + 16) % 16; }
 
-// Records in flight per system (forward, backward).
-template <typename R> __host__ __device__ constexpr int quad_fdepth() { return 8; }
-template <typename R> __host__ __device__ constexpr int quad_bdepth() { return 4; }
+// Records in flight per system (forward, backward): template parameters of
+// the kernels, chosen at launch from a process-wide setting
+// (sgb_gbtrs_set_quad_depth); 8 and 4 unless set.
+static int g_qdepth[2] = {8, 4};
+static bool quad_depth_ok(int d) { return d == 2 || d == 4 || d == 8 || d == 16; }
 
 // A factor segment of n complex elements starting at element e (from the
 // base pointer `base`) is copied with 16-byte cp.async: complex128 element by
@@ -263,12 +265,11 @@ template <typename R> __host__ __device__ constexpr int quad_span(int n)
     return sizeof(R) == 8 ? n : ((n + 2) & ~1);
 }
 
-template <typename R>
+template <typename R, int PD>
 struct QuadFwdLayout {
     int XW, RL, SE;       // window (pow2 >= KL+2), L record (span), per-system stride
     __host__ __device__ QuadFwdLayout(const FactorGeom &g)
     {
-        constexpr int PD = quad_fdepth<R>();
         constexpr int EB = (int) sizeof(cplx_t<R>);
         XW = quad_pow2(g.KL + 2);
         RL = quad_span<R>(g.KL);
@@ -277,12 +278,11 @@ struct QuadFwdLayout {
         SE = quad_pad((bytes + EB - 1) / EB);
     }
 };
-template <typename R>
+template <typename R, int PD>
 struct QuadBwdLayout {
     int XW, RP, SE;       // mirrored window (2 x (KV+3) ring), record, stride
     __host__ __device__ QuadBwdLayout(const FactorGeom &g)
     {
-        constexpr int PD = quad_bdepth<R>();
         XW = g.UW() + 2;
         RP = quad_span<R>(g.UW()) + 1;      // U row span, then y_j
         RP += RP & 1;
@@ -303,7 +303,7 @@ __device__ __forceinline__ int quad_system(int pos, int nsys, const int *sys_lis
     return s;
 }
 
-template <typename R>
+template <typename R, int PD>
 __global__ void __launch_bounds__(32)
 k_gbtrs_fwd_quad(FactorGeom g, int nsys, const cplx_t<R> *__restrict__ fac, long long fac_stride,
                  const int *__restrict__ ipiv, const double2 *__restrict__ b, long long b_stride,
@@ -312,7 +312,6 @@ k_gbtrs_fwd_quad(FactorGeom g, int nsys, const cplx_t<R> *__restrict__ fac, long
                  int status_want)
 {
     using T2 = cplx_t<R>;
-    constexpr int PD = quad_fdepth<R>();
     const int lane = threadIdx.x, sub = lane >> 2, q = lane & 3;
     const int pos = blockIdx.x * QSYS + sub;
     const int s = quad_system(pos, nsys, sys_list, nlist, d_count, status, status_want);
@@ -320,7 +319,7 @@ k_gbtrs_fwd_quad(FactorGeom g, int nsys, const cplx_t<R> *__restrict__ fac, long
     if (!__any_sync(0xffffffffu, act)) return;
     const long long fi = slot_mode ? (long long) pos : (long long) s;
     const int N = g.N, KL = g.KL;
-    const QuadFwdLayout<R> L(g);
+    const QuadFwdLayout<R, PD> L(g);
     const int m = L.XW - 1;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T2 *xw = reinterpret_cast<T2 *>(smem_raw) + sub * L.SE;
@@ -374,7 +373,7 @@ k_gbtrs_fwd_quad(FactorGeom g, int nsys, const cplx_t<R> *__restrict__ fac, long
     if (act && q == 0) ys[N - 1] = xw[(N - 1) & m];
 }
 
-template <typename R, bool ACCUM>
+template <typename R, bool ACCUM, int PD>
 __global__ void __launch_bounds__(32)
 k_gbtrs_bwd_quad(FactorGeom g, int nsys, const cplx_t<R> *__restrict__ fac, long long fac_stride,
                  cplx_t<R> *__restrict__ yw, double2 *__restrict__ x, long long x_stride,
@@ -382,7 +381,6 @@ k_gbtrs_bwd_quad(FactorGeom g, int nsys, const cplx_t<R> *__restrict__ fac, long
                  bool slot_mode, const int *__restrict__ status, int status_want, int unS, int unn)
 {
     using T2 = cplx_t<R>;
-    constexpr int PD = quad_bdepth<R>();
     const int lane = threadIdx.x, sub = lane >> 2, q = lane & 3;
     const int pos = blockIdx.x * QSYS + sub;
     const int s = quad_system(pos, nsys, sys_list, nlist, d_count, status, status_want);
@@ -390,7 +388,7 @@ k_gbtrs_bwd_quad(FactorGeom g, int nsys, const cplx_t<R> *__restrict__ fac, long
     if (!__any_sync(0xffffffffu, act)) return;
     const long long fi = slot_mode ? (long long) pos : (long long) s;
     const int N = g.N, UW = g.UW(), KV = UW - 1;
-    const QuadBwdLayout<R> L(g);
+    const QuadBwdLayout<R, PD> L(g);
     const int XW = L.XW;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     // x window: ring of XW = KV+3 slots (row r at r mod XW), stored twice so
@@ -467,8 +465,8 @@ k_gbtrs_bwd_quad(FactorGeom g, int nsys, const cplx_t<R> *__restrict__ fac, long
     }
 }
 
-template <typename R>
-static cudaError_t launch_quad(const GbtrsArgs &a, cudaStream_t st)
+template <typename R, int PF, int PB>
+static cudaError_t launch_quad_d(const GbtrsArgs &a, cudaStream_t st)
 {
     const int count = a.sys_list ? a.nlist : a.nsys;
     if (count == 0) return cudaSuccess;
@@ -477,26 +475,69 @@ static cudaError_t launch_quad(const GbtrsArgs &a, cudaStream_t st)
     T2 *yw = reinterpret_cast<T2 *>(a.ywork);
     cudaError_t e;
     if (!a.fwd_done) {
-        const QuadFwdLayout<R> L(a.g);
+        const QuadFwdLayout<R, PF> L(a.g);
         const size_t smem = (size_t) QSYS * L.SE * sizeof(T2);
-        e = smem_attr((const void *) k_gbtrs_fwd_quad<R>, smem);
+        e = smem_attr((const void *) k_gbtrs_fwd_quad<R, PF>, smem);
         if (e != cudaSuccess) return e;
-        k_gbtrs_fwd_quad<R><<<grid, 32, smem, st>>>(a.g, a.nsys, reinterpret_cast<const T2 *>(a.fac),
-                                                     a.fac_stride, a.ipiv, a.b, a.b_stride, yw,
-                                                     a.sys_list, a.nlist, a.d_count, a.slot_mode,
-                                                     a.status, a.status_want);
+        k_gbtrs_fwd_quad<R, PF><<<grid, 32, smem, st>>>(a.g, a.nsys, reinterpret_cast<const T2 *>(a.fac),
+                                                         a.fac_stride, a.ipiv, a.b, a.b_stride, yw,
+                                                         a.sys_list, a.nlist, a.d_count, a.slot_mode,
+                                                         a.status, a.status_want);
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
-    const QuadBwdLayout<R> L(a.g);
+    const QuadBwdLayout<R, PB> L(a.g);
     const size_t smem = (size_t) QSYS * L.SE * sizeof(T2);
-    auto kern = a.accumulate ? k_gbtrs_bwd_quad<R, true> : k_gbtrs_bwd_quad<R, false>;
+    auto kern = a.accumulate ? k_gbtrs_bwd_quad<R, true, PB> : k_gbtrs_bwd_quad<R, false, PB>;
     e = smem_attr((const void *) kern, smem);
     if (e != cudaSuccess) return e;
     kern<<<grid, 32, smem, st>>>(a.g, a.nsys, reinterpret_cast<const T2 *>(a.fac), a.fac_stride, yw,
                                  a.x, a.x_stride, a.sys_list, a.nlist, a.d_count, a.slot_mode,
                                  a.status, a.status_want, a.unpermute_S, a.unpermute_n);
     return cudaGetLastError();
+}
+
+template <typename R, int PF>
+static cudaError_t launch_quad_b(const GbtrsArgs &a, cudaStream_t st)
+{
+    switch (g_qdepth[1]) {
+    case 2: return launch_quad_d<R, PF, 2>(a, st);
+    case 8: return launch_quad_d<R, PF, 8>(a, st);
+    case 16: return launch_quad_d<R, PF, 16>(a, st);
+    default: return launch_quad_d<R, PF, 4>(a, st);
+    }
+}
+
+template <typename R>
+static cudaError_t launch_quad(const GbtrsArgs &a, cudaStream_t st)
+{
+    switch (g_qdepth[0]) {
+    case 2: return launch_quad_b<R, 2>(a, st);
+    case 4: return launch_quad_b<R, 4>(a, st);
+    case 16: return launch_quad_b<R, 16>(a, st);
+    default: return launch_quad_b<R, 8>(a, st);
+    }
+}
+
+template <typename R>
+static size_t quad_fwd_se(const FactorGeom &g)
+{
+    switch (g_qdepth[0]) {
+    case 2: return QuadFwdLayout<R, 2>(g).SE;
+    case 4: return QuadFwdLayout<R, 4>(g).SE;
+    case 16: return QuadFwdLayout<R, 16>(g).SE;
+    default: return QuadFwdLayout<R, 8>(g).SE;
+    }
+}
+template <typename R>
+static size_t quad_bwd_se(const FactorGeom &g)
+{
+    switch (g_qdepth[1]) {
+    case 2: return QuadBwdLayout<R, 2>(g).SE;
+    case 8: return QuadBwdLayout<R, 8>(g).SE;
+    case 16: return QuadBwdLayout<R, 16>(g).SE;
+    default: return QuadBwdLayout<R, 4>(g).SE;
+    }
 }
 
 // The quad path needs a writable y buffer (nsys x N, complex of prec) and,
@@ -506,8 +547,8 @@ static bool quad_ok(const GbtrsArgs &a)
     if (a.trans != 'N' || !a.ywork) return false;
     if (a.fwd_done && a.yin != a.ywork) return false;
     const size_t el = a.prec == 'Z' ? 16 : 8;
-    const size_t fwd = a.prec == 'Z' ? QuadFwdLayout<double>(a.g).SE : QuadFwdLayout<float>(a.g).SE;
-    const size_t bwd = a.prec == 'Z' ? QuadBwdLayout<double>(a.g).SE : QuadBwdLayout<float>(a.g).SE;
+    const size_t fwd = a.prec == 'Z' ? quad_fwd_se<double>(a.g) : quad_fwd_se<float>(a.g);
+    const size_t bwd = a.prec == 'Z' ? quad_bwd_se<double>(a.g) : quad_bwd_se<float>(a.g);
     return (size_t) QSYS * std::max(fwd, bwd) * el <= 227 * 1024;
 }
 
@@ -550,3 +591,13 @@ cudaError_t launch_gbtrs(const GbtrsArgs &a, cudaStream_t st)
 }
 
 }  // namespace sgb
+
+// Tuning knob: records in flight per system of the quad-lane solves
+// (2, 4, 8 or 16; 0 keeps the current value).
+extern "C" int sgb_gbtrs_set_quad_depth(int fwd, int bwd)
+{
+    if ((fwd && !sgb::quad_depth_ok(fwd)) || (bwd && !sgb::quad_depth_ok(bwd))) return -1;
+    if (fwd) sgb::g_qdepth[0] = fwd;
+    if (bwd) sgb::g_qdepth[1] = bwd;
+    return 0;
+}

@@ -197,3 +197,64 @@ class Plan:
                                                  _ptr(stream)),
                   "sgb_plan_backward_error")
         return out
+
+
+class BatchPlan:
+    """One batch of systems of a case split into `parts` resident Plans over
+    consecutive wavenumber ranges, each substep issued on its own CUDA stream
+    (forked from and joined into the caller's stream) in the capturable form,
+    which keeps the host out of the refinement loop: the parts' kernels
+    overlap on the device, the FP64 residual and explicit-operator kernels
+    of one part alongside the complex64 factor of another.  Results are
+    those of one Plan over the whole batch with the capturable substep (each
+    system is solved by the same kernels on the same data)."""
+
+    def __init__(self, case: SynthCase, kx: np.ndarray, kz: np.ndarray,
+                 parts: int = 4, max_double_slots: int = 0, method: str = "M"):
+        import torch
+        self.torch = torch
+        n = int(len(kx))
+        parts = max(1, min(int(parts), n))
+        self.bounds = [int(b) for b in np.linspace(0, n, parts + 1)]
+        self.plans = []
+        for a, b in zip(self.bounds[:-1], self.bounds[1:]):
+            pl = Plan(case, kx[a:b], kz[a:b], max_double_slots=max_double_slots)
+            pl.prepare(method)
+            self.plans.append(pl)
+        self.streams = [torch.cuda.Stream() for _ in self.plans]
+        self.nsys = n
+        self.N = case.N
+
+    def substep(self, method: str, phi_exp: float, phi_imp: float, u_in, u_out,
+                spec: RefineSpec | None = None) -> None:
+        """u_in, u_out: device tensors (nsys x N), rows split by part."""
+        torch = self.torch
+        cur = torch.cuda.current_stream()
+        for s in self.streams:
+            s.wait_stream(cur)
+        for pl, s, a, b in zip(self.plans, self.streams, self.bounds[:-1], self.bounds[1:]):
+            with torch.cuda.stream(s):
+                pl.substep_capturable(method, phi_exp, phi_imp, u_in[a:b], u_out[a:b], spec,
+                                      stream=s.cuda_stream)
+        for s in self.streams:
+            cur.wait_stream(s)
+
+    def report(self) -> dict:
+        reps = [pl.report() for pl in self.plans]
+        out = {k: np.concatenate([r[k] for r in reps]) for k in reps[0] if k != "fact"}
+        out["fact"] = "".join(r["fact"] for r in reps)
+        return out
+
+    def backward_error(self) -> np.ndarray:
+        return np.concatenate([pl.backward_error() for pl in self.plans])
+
+    def unserved(self) -> int:
+        return sum(pl.unserved() for pl in self.plans)
+
+    def device_bytes(self) -> int:
+        return sum(pl.device_bytes() for pl in self.plans)
+
+    def close(self) -> None:
+        for pl in self.plans:
+            pl.close()
+        self.plans = []

@@ -190,6 +190,41 @@ def test_gbtrs_quad_path(lib, oracle, torch_cuda, n, kl, ku, prec):
         assert d <= (1e-9 if prec == "Z" else 1e-2), (s, d)
 
 
+@pytest.mark.parametrize("n,kl,ku", [(7, 0, 3), (240, 34, 34), (97, 48, 48)])
+def test_gbtrs_quad_depth_does_not_change_results(lib, torch_cuda, n, kl, ku):
+    """Every prefetch depth of the quad solves gives the same bits."""
+    torch = torch_cuda
+    rng = np.random.default_rng(5 + n)
+    nsys, ld = 21, kl + ku + 1
+    bands = [rand_band(rng, n, kl, ku)[0] for _ in range(nsys)]
+    b = rng.normal(size=(nsys, n)) + 1j * rng.normal(size=(nsys, n))
+    ab = dev(torch, np.stack(bands))
+    fe = lib.sgb_factor_elems(n, kl, ku)
+    assert lib.sgb_gbtrs_set_quad_depth(3, 0) == -1
+    try:
+        for prec, fdt in (("Z", torch.complex128), ("C", torch.complex64)):
+            fac = torch.zeros(nsys * fe, dtype=fdt, device="cuda")
+            ipiv = torch.zeros(nsys * n, dtype=torch.int32, device="cuda")
+            info = torch.zeros(nsys, dtype=torch.int32, device="cuda")
+            assert lib.sgb_gbtrf_batched(prec.encode(), nsys, n, kl, ku, ab.data_ptr(), ld,
+                                         ld * n, fac.data_ptr(), ipiv.data_ptr(),
+                                         info.data_ptr(), 0) == 0
+            outs = []
+            for f, bk in [(8, 4), (2, 2), (4, 8), (16, 16)]:
+                assert lib.sgb_gbtrs_set_quad_depth(f, bk) == 0
+                x = dev(torch, b)
+                yw = torch.zeros(nsys * n, dtype=fdt, device="cuda")
+                assert lib.sgb_gbtrs_batched_ws(prec.encode(), b"N", nsys, n, kl, ku,
+                                                fac.data_ptr(), ipiv.data_ptr(), x.data_ptr(),
+                                                x.data_ptr(), yw.data_ptr(), 0) == 0
+                torch.cuda.synchronize()
+                outs.append(x.cpu().numpy())
+            for o in outs[1:]:
+                assert np.array_equal(o, outs[0]), prec
+    finally:
+        lib.sgb_gbtrs_set_quad_depth(8, 4)
+
+
 def test_singular_and_nan_systems(lib, oracle, torch_cuda):
     torch = torch_cuda
     n, kl, ku = 30, 2, 3
@@ -440,6 +475,66 @@ def test_plan_result_independent_of_factor_shape(lib, torch_cuda):
     for row in results[1:]:
         for m in range(2):
             assert np.array_equal(row[m], results[0][m])
+
+
+def test_plan_memory_reuse_waits_for_issued_work(lib, torch_cuda):
+    """Plans take device memory from a pool that keeps freed blocks.  A plan
+    destroyed right after issuing a substep on a side stream must not hand
+    its blocks to the next plan before that substep completes: the results
+    equal a synchronised run, and the next plan (same sizes, so it reuses
+    the blocks) computes its own correctly."""
+    torch = torch_cuda
+    from suzerain_gb300 import plan as P
+    c, cs, kx, kz, u = config0()
+    spec = P.RefineSpec(tolsc=145.0)
+    du = dev(torch, u)
+    ref = torch.zeros_like(du)
+    pl = P.Plan(cs, kx, kz)
+    pl.prepare("M")
+    pl.substep_capturable("M", 0.0, -c.phi, du, ref, spec)
+    torch.cuda.synchronize()
+    want = ref.cpu().numpy()
+    pl.close()
+    side = torch.cuda.Stream()
+    outs = []
+    for rep in range(3):
+        out = torch.zeros_like(du)
+        pl = P.Plan(cs, kx, kz)
+        pl.prepare("M")
+        with torch.cuda.stream(side):
+            pl.substep_capturable("M", 0.0, -c.phi, du, out, spec, stream=side.cuda_stream)
+        pl.close()                      # no synchronisation before the destroy
+        outs.append(out)
+    torch.cuda.synchronize()
+    for out in outs:
+        assert np.array_equal(out.cpu().numpy(), want)
+    assert lib.sgb_plan_pool_trim(0) == 0
+
+
+def test_batch_plan_parts_match_one_plan(lib, torch_cuda):
+    """A batch split into resident plans on their own streams gives the same
+    bits as one plan over the batch (capturable substeps both)."""
+    torch = torch_cuda
+    from suzerain_gb300 import plan as P
+    c, cs, kx, kz, u = config0()
+    spec = P.RefineSpec(aiter=5, siter=25, diter=5, tolsc=145.0)
+    du = dev(torch, u)
+    one = P.Plan(cs, kx, kz, max_double_slots=64)
+    one.prepare("M")
+    want = torch.zeros_like(du)
+    one.substep_capturable("M", 0.0, -c.phi, du, want, spec)
+    torch.cuda.synchronize()
+    one.close()
+    bp = P.BatchPlan(cs, kx, kz, parts=3, max_double_slots=22)
+    got = torch.zeros_like(du)
+    bp.substep("M", 0.0, -c.phi, du, got, spec)
+    torch.cuda.synchronize()
+    assert np.array_equal(got.cpu().numpy(), want.cpu().numpy())
+    assert bp.unserved() == 0
+    rep = bp.report()
+    assert (rep["info"] == 0).all() and len(rep["fact"]) == len(kx)
+    assert bp.backward_error().max() <= 1e-12
+    bp.close()
 
 
 def test_plan_host_entry_matches_device_entry(lib, torch_cuda):
