@@ -408,7 +408,7 @@ int sgb_zgbsvx_batched(char fact, char trans, int nsys, int n, int kl, int ku,
 
 /** Records in flight per system of the quad-lane solves (trans 'N' with a
  *  y workspace): 2, 4, 8 or 16 for the forward and the backward sweep (0
- *  keeps the current value; defaults 8 and 4).  Returns -1 for other values.
+ *  keeps the current value; defaults 2 and 2).  Returns -1 for other values.
  *  Process-wide; results do not depend on it. */
 int sgb_gbtrs_set_quad_depth(int fwd, int bwd);
 

@@ -230,8 +230,11 @@ __host__ __device__ inline int quad_pad(int e) { return e + ((4 - e % 16) + 16) 
 
 // Records in flight per system (forward, backward): template parameters of
 // the kernels, chosen at launch from a process-wide setting
-// (sgb_gbtrs_set_quad_depth); 8 and 4 unless set.
-static int g_qdepth[2] = {8, 4};
+// (sgb_gbtrs_set_quad_depth); 2 and 2 unless set.  Shared memory bounds the
+// warps per SM, and on the GB300 more resident warps with two records each
+// beat fewer warps with deeper rings (N = 960, KL = KU = 34, complex64:
+// forward + backward 4.6 ms at depth 2, 6.3 ms at 8 / 4, 8.6 ms at 16 / 8).
+static int g_qdepth[2] = {2, 2};
 static bool quad_depth_ok(int d) { return d == 2 || d == 4 || d == 8 || d == 16; }
 
 // A factor segment of n complex elements starting at element e (from the
@@ -501,10 +504,10 @@ template <typename R, int PF>
 static cudaError_t launch_quad_b(const GbtrsArgs &a, cudaStream_t st)
 {
     switch (g_qdepth[1]) {
-    case 2: return launch_quad_d<R, PF, 2>(a, st);
+    case 4: return launch_quad_d<R, PF, 4>(a, st);
     case 8: return launch_quad_d<R, PF, 8>(a, st);
     case 16: return launch_quad_d<R, PF, 16>(a, st);
-    default: return launch_quad_d<R, PF, 4>(a, st);
+    default: return launch_quad_d<R, PF, 2>(a, st);
     }
 }
 
@@ -512,10 +515,10 @@ template <typename R>
 static cudaError_t launch_quad(const GbtrsArgs &a, cudaStream_t st)
 {
     switch (g_qdepth[0]) {
-    case 2: return launch_quad_b<R, 2>(a, st);
     case 4: return launch_quad_b<R, 4>(a, st);
+    case 8: return launch_quad_b<R, 8>(a, st);
     case 16: return launch_quad_b<R, 16>(a, st);
-    default: return launch_quad_b<R, 8>(a, st);
+    default: return launch_quad_b<R, 2>(a, st);
     }
 }
 
@@ -523,20 +526,20 @@ template <typename R>
 static size_t quad_fwd_se(const FactorGeom &g)
 {
     switch (g_qdepth[0]) {
-    case 2: return QuadFwdLayout<R, 2>(g).SE;
     case 4: return QuadFwdLayout<R, 4>(g).SE;
+    case 8: return QuadFwdLayout<R, 8>(g).SE;
     case 16: return QuadFwdLayout<R, 16>(g).SE;
-    default: return QuadFwdLayout<R, 8>(g).SE;
+    default: return QuadFwdLayout<R, 2>(g).SE;
     }
 }
 template <typename R>
 static size_t quad_bwd_se(const FactorGeom &g)
 {
     switch (g_qdepth[1]) {
-    case 2: return QuadBwdLayout<R, 2>(g).SE;
+    case 4: return QuadBwdLayout<R, 4>(g).SE;
     case 8: return QuadBwdLayout<R, 8>(g).SE;
     case 16: return QuadBwdLayout<R, 16>(g).SE;
-    default: return QuadBwdLayout<R, 4>(g).SE;
+    default: return QuadBwdLayout<R, 2>(g).SE;
     }
 }
 
