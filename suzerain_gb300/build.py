@@ -1,6 +1,6 @@
 """Build libsuzerain_gb300.so in-tree: nvcc for sm_103a, one -gencode.
 
-Translation units compile in parallel, then link with the static CUDA
+Translation units compile in parallel (one worker per host core), then link with the static CUDA
 runtime, so the library carries no dependency on torch's runtime copy.
 """
 from __future__ import annotations
@@ -33,6 +33,28 @@ def sources() -> list[str]:
                   glob.glob(os.path.join(CSRC, "*.cpp")))
 
 
+# gbtrf_blk_inst.cu is compiled once per (precision, panel width, warp
+# family): each object holds 8 of the 192 blocked-factor kernels.
+BLK_INST = "gbtrf_blk_inst.cu"
+BLK_VARIANTS = [(p, nb, fam) for nb in (16, 8, 4) for p in ("z", "c")
+                for fam in (0, 1, 2, 4)]
+
+
+def jobs() -> list[tuple[str, str, list[str]]]:
+    """(source, object stem, extra flags) per object, the heaviest first."""
+    out = []
+    for src in sources():
+        if os.path.basename(src) == BLK_INST:
+            for p, nb, fam in BLK_VARIANTS:
+                r = "double" if p == "z" else "float"
+                out.append((src, f"gbtrf_blk_{p}{nb}_f{fam}",
+                            [f"-DSGB_BLK_R={r}", f"-DSGB_BLK_NB={nb}",
+                             f"-DSGB_BLK_FAM={fam}"]))
+        else:
+            out.append((src, os.path.basename(src), []))
+    return out
+
+
 def _stale() -> bool:
     if not os.path.exists(LIB):
         return True
@@ -47,8 +69,10 @@ def _headers() -> list[str]:
         [os.path.join(ROOT, "include", "suzerain_gb300.h"), __file__]
 
 
-def _compile(src: str, nvcc: str, debug: bool, force: bool = False) -> str:
-    obj = os.path.join(OBJ_DIR, os.path.basename(src) + (".dbg.o" if debug else ".o"))
+def _compile(job: tuple[str, str, list[str]], nvcc: str, debug: bool,
+             force: bool = False) -> str:
+    src, stem, defs = job
+    obj = os.path.join(OBJ_DIR, stem + (".dbg.o" if debug else ".o"))
     if not force and os.path.exists(obj):
         # an object newer than its source and every header is current
         t = os.path.getmtime(obj)
@@ -58,7 +82,7 @@ def _compile(src: str, nvcc: str, debug: bool, force: bool = False) -> str:
     if src.endswith(".cu"):
         cmd = [nvcc, "-std=c++17", *ARCH, "-O3", "-lineinfo", "-Xcompiler",
                "-fPIC,-ffp-contract=off", "--expt-relaxed-constexpr", *inc,
-               "-c", src, "-o", obj]
+               *defs, "-c", src, "-o", obj]
         if debug:
             cmd.insert(1, "-DSGB_DEBUG_BOUNDS")
     else:
@@ -78,9 +102,10 @@ def build(force: bool = False, debug: bool = False, verbose: bool = False
         return LIB
     nvcc = _nvcc()
     os.makedirs(OBJ_DIR, exist_ok=True)
-    srcs = sources()
-    with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
-        objs = list(ex.map(lambda s: _compile(s, nvcc, debug, force), srcs))
+    js = jobs()
+    workers = max(1, min(len(js), os.cpu_count() or 8))
+    with cf.ThreadPoolExecutor(max_workers=workers) as ex:
+        objs = list(ex.map(lambda j: _compile(j, nvcc, debug, force), js))
     tmp = LIB + ".tmp"
     cmd = [nvcc, *ARCH, "-shared", "-cudart=static", "-o", tmp, *objs,
            "-lpthread"]

@@ -1,7 +1,7 @@
 // Blocked batched band LU: shared-memory size, supported shapes, the default
 // shape choice and the dispatch over (precision, panel width NB, warps per
-// system NW).  The kernel template is in gbtrf_blk.cuh;
-// gbtrf_blk_{z,c}{4,8,16}.cu instantiate it.
+// system NW).  The kernel template is in gbtrf_blk.cuh; gbtrf_blk_inst.cu,
+// compiled once per (precision, NB, warp family), instantiates it.
 #include "gbtrf_blk.cuh"
 
 #include <mutex>
@@ -70,16 +70,27 @@ void gbtrf_blk_choice(char prec, const FactorGeom &g, int &nb, int &nw)
     if (nw == 0) nw = g.KL > 56 ? 4 : (prec == 'C' || g.KL > 52) ? 2 : 1;
 }
 
+namespace {
+template <typename R, int NB>
+cudaError_t launch_nb(const GbtrfArgs &a, int nw, cudaStream_t st)
+{
+    if (a.variant == 2 && nw > 1) return launch_blk_fam<R, NB, 0>(a, nw, st);
+    if (nw == 1) return launch_blk_fam<R, NB, 1>(a, nw, st);
+    if (nw == 2) return launch_blk_fam<R, NB, 2>(a, nw, st);
+    return launch_blk_fam<R, NB, 4>(a, nw, st);
+}
+}  // namespace
+
 cudaError_t launch_gbtrf_blk(const GbtrfArgs &a, int nb, int nw, cudaStream_t st)
 {
     if (a.prec == 'Z') {
-        if (nb == 4) return launch_blk_z4(a, nw, st);
-        if (nb == 16) return launch_blk_z16(a, nw, st);
-        return launch_blk_z8(a, nw, st);
+        if (nb == 4) return launch_nb<double, 4>(a, nw, st);
+        if (nb == 16) return launch_nb<double, 16>(a, nw, st);
+        return launch_nb<double, 8>(a, nw, st);
     }
-    if (nb == 4) return launch_blk_c4(a, nw, st);
-    if (nb == 16) return launch_blk_c16(a, nw, st);
-    return launch_blk_c8(a, nw, st);
+    if (nb == 4) return launch_nb<float, 4>(a, nw, st);
+    if (nb == 16) return launch_nb<float, 16>(a, nw, st);
+    return launch_nb<float, 8>(a, nw, st);
 }
 
 }  // namespace sgb

@@ -955,32 +955,13 @@ cudaError_t launch_cta_r(const GbtrfArgs &a, cudaStream_t st)
                : launch_cta_one<R, NB, NW, MAXTR, LA, false, false>(a, st);
 }
 
-// The phased kernel: KL <= (4 NW) MAXTR rows of the trailing update per
-// thread.  The lookahead kernel (variant 2, NW = 2 or 4) loops its worker
-// update over row passes.
-template <typename R, int NB>
-cudaError_t launch_cta_nw(const GbtrfArgs &a, int nw, cudaStream_t st)
-{
-    const int KL = a.g.KL;
-    if (a.variant == 2 && nw > 1)
-        return nw == 2 ? launch_cta_r<R, NB, 2, 1, true>(a, st) : launch_cta_r<R, NB, 4, 1, true>(a, st);
-    if (nw == 1) return KL <= 36 ? launch_cta_r<R, NB, 1, 9, false>(a, st) : launch_cta_r<R, NB, 1, 13, false>(a, st);
-    if (nw == 2) return KL <= 40 ? launch_cta_r<R, NB, 2, 5, false>(a, st) : launch_cta_r<R, NB, 2, 7, false>(a, st);
-    return KL <= 48 ? launch_cta_r<R, NB, 4, 3, false>(a, st) : launch_cta_r<R, NB, 4, 4, false>(a, st);
-}
-
-// One translation unit per (precision, NB) instantiates the kernels.
-#define SGB_BLK_INSTANTIATE(R, NB, NAME)                                          \
-    cudaError_t NAME(const GbtrfArgs &a, int nw, cudaStream_t st)                 \
-    {                                                                             \
-        return launch_cta_nw<R, NB>(a, nw, st);                                   \
-    }
-
-cudaError_t launch_blk_z4(const GbtrfArgs &, int, cudaStream_t);
-cudaError_t launch_blk_z8(const GbtrfArgs &, int, cudaStream_t);
-cudaError_t launch_blk_z16(const GbtrfArgs &, int, cudaStream_t);
-cudaError_t launch_blk_c4(const GbtrfArgs &, int, cudaStream_t);
-cudaError_t launch_blk_c8(const GbtrfArgs &, int, cudaStream_t);
-cudaError_t launch_blk_c16(const GbtrfArgs &, int, cudaStream_t);
+// The kernels of one (precision R, panel width NB, warp family FAM) are
+// instantiated by one translation unit, gbtrf_blk_inst.cu compiled once per
+// triple, so the build compiles them in parallel.  FAM 0 is the lookahead
+// kernel (variant 2, nw = 2 or 4, which loops its worker update over row
+// passes); FAM 1, 2, 4 the phased kernel with that many warps, KL <= (4 FAM)
+// MAXTR rows of the trailing update per thread.
+template <typename R, int NB, int FAM>
+cudaError_t launch_blk_fam(const GbtrfArgs &a, int nw, cudaStream_t st);
 
 }  // namespace sgb

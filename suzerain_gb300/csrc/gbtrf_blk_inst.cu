@@ -1,0 +1,32 @@
+// Blocked band LU kernels of one (precision, panel width, warp family).
+// The build compiles this file once per triple with -DSGB_BLK_R=float|double
+// -DSGB_BLK_NB=4|8|16 -DSGB_BLK_FAM=0|1|2|4 (24 objects, compiled in
+// parallel); without those definitions it instantiates nothing.
+#include "gbtrf_blk.cuh"
+
+namespace sgb {
+
+template <typename R, int NB, int FAM>
+cudaError_t launch_blk_fam(const GbtrfArgs &a, int nw, cudaStream_t st)
+{
+    const int KL = a.g.KL;
+    if constexpr (FAM == 0)
+        return nw == 2 ? launch_cta_r<R, NB, 2, 1, true>(a, st)
+                       : launch_cta_r<R, NB, 4, 1, true>(a, st);
+    else if constexpr (FAM == 1)
+        return KL <= 36 ? launch_cta_r<R, NB, 1, 9, false>(a, st)
+                        : launch_cta_r<R, NB, 1, 13, false>(a, st);
+    else if constexpr (FAM == 2)
+        return KL <= 40 ? launch_cta_r<R, NB, 2, 5, false>(a, st)
+                        : launch_cta_r<R, NB, 2, 7, false>(a, st);
+    else
+        return KL <= 48 ? launch_cta_r<R, NB, 4, 3, false>(a, st)
+                        : launch_cta_r<R, NB, 4, 4, false>(a, st);
+}
+
+#if defined(SGB_BLK_R) && defined(SGB_BLK_NB) && defined(SGB_BLK_FAM)
+template cudaError_t launch_blk_fam<SGB_BLK_R, SGB_BLK_NB, SGB_BLK_FAM>(
+    const GbtrfArgs &, int, cudaStream_t);
+#endif
+
+}  // namespace sgb
