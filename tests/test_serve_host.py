@@ -1,0 +1,190 @@
+"""Host logic of the continuous-batching request loop (serve.Server.run),
+without a GPU: streams, events, device buffers and plans are fakes that
+model what the loop relies on (work on one stream runs in issue order; an
+event completes when the work recorded before it on its stream has run; a
+plan's substep advances the case's state), so that admission in arrival
+order, the HBM budget, overlap of resident cases, the alternating state
+buffers, plan release and latency accounting are checked on CPU.  The GPU
+counterpart (test_serving_result_same_alone_and_in_the_mix) checks that
+each case's result is the same alone and in the mix."""
+import dataclasses
+import sys
+import time
+import types
+
+import numpy as np
+import pytest
+
+from suzerain_gb300 import serve
+
+
+class _Arr(np.ndarray):
+    def cuda(self):
+        return self.copy()
+
+    def cpu(self):
+        return self
+
+    def numpy(self):
+        return np.asarray(self)
+
+
+class _Device:
+    def __init__(self):
+        self.streams = {}
+        self.log = []            # (rid, substep, start, end) per issued substep
+
+
+class _Stream:
+    def __init__(self, dev):
+        self.cuda_stream = len(dev.streams) + 1
+        self.busy_until = 0.0
+        dev.streams[self.cuda_stream] = self
+
+
+class _Event:
+    def __init__(self, enable_timing=False):
+        self.t = None
+
+    def record(self, stream=None):
+        now = time.perf_counter()
+        self.t = max(now, stream.busy_until) if stream is not None else now
+
+    def query(self):
+        return time.perf_counter() >= self.t
+
+    def elapsed_time(self, other):
+        return (other.t - self.t) * 1e3
+
+
+def _fake_torch(dev):
+    class _StreamCtx:
+        def __init__(self, st):
+            self.st = st
+
+        def __enter__(self):
+            return self.st
+
+        def __exit__(self, *a):
+            return False
+
+    cuda = types.SimpleNamespace(Stream=lambda: _Stream(dev), Event=_Event,
+                                 synchronize=lambda: None, stream=_StreamCtx)
+    return types.SimpleNamespace(cuda=cuda,
+                                 from_numpy=lambda a: np.asarray(a).view(_Arr),
+                                 empty_like=lambda a: np.empty_like(a).view(_Arr))
+
+
+@dataclasses.dataclass
+class _Case:
+    rid: int
+    nsys: int
+    bytes: int
+    dur: float
+    phi: float = 1e-3
+
+    def batch(self):
+        cs = {"rid": self.rid, "bytes": self.bytes, "dur": self.dur}
+        u = np.full((self.nsys, 4), float(self.rid), dtype=np.complex128)
+        return cs, np.zeros(self.nsys), np.zeros(self.nsys), u
+
+
+def _fake_plan(dev, created, closed):
+    class Plan:
+        def __init__(self, cs, kx, kz, max_double_slots=0):
+            self.cs, self.nsys, self.k = cs, len(kx), 0
+            created.append(cs["rid"])
+
+        @staticmethod
+        def estimate_bytes(cs, nsys, slots, method):
+            return cs["bytes"]
+
+        def prepare(self, method):
+            pass
+
+        def substep_capturable(self, method, pe, pi, a, b, spec, stream=0):
+            st = dev.streams[stream]
+            start = max(time.perf_counter(), st.busy_until)
+            st.busy_until = start + self.cs["dur"]
+            b[...] = a + 1
+            dev.log.append((self.cs["rid"], self.k, start, st.busy_until))
+            self.k += 1
+
+        def close(self):
+            closed.append(self.cs["rid"])
+
+    return Plan
+
+
+@pytest.fixture
+def fake(monkeypatch):
+    dev = _Device()
+    created, closed = [], []
+    monkeypatch.setitem(sys.modules, "torch", _fake_torch(dev))
+    monkeypatch.setattr(serve.P, "Plan", _fake_plan(dev, created, closed))
+    monkeypatch.setattr(serve.synth, "zero_dirichlet_rows", lambda cs, u: u)
+    return types.SimpleNamespace(dev=dev, created=created, closed=closed)
+
+
+def _trace(arrivals, lives, nbytes, dur, nsys=8):
+    return [serve.Request(i, _Case(i, nsys, nbytes, dur), n, t)
+            for i, (t, n) in enumerate(zip(arrivals, lives))]
+
+
+def _need(srv, req):
+    return srv._prepare(req)[-1]
+
+
+def test_admission_in_arrival_order_within_budget_with_overlap(fake):
+    arrivals = [0.0, 0.004, 0.008, 0.012, 0.03, 0.031, 0.05, 0.06]
+    lives = [3, 4, 5, 3, 4, 3, 5, 3]
+    trace = _trace(arrivals, lives, 30_000_000, 0.01)
+    trace = trace[3:] + trace[:3]                  # the loop sorts by arrival
+    srv = serve.Server(budget_bytes=100e6, nstreams=4, keep_results=True)
+    need = _need(srv, trace[0])
+    st = srv.run(trace)
+
+    assert st["substeps"] == st["issued"] == sum(lives)
+    assert st["system_solves"] == 8 * sum(lives)
+    assert fake.created == sorted(fake.created) == list(range(8))
+    assert sorted(fake.closed) == list(range(8))
+    assert st["peak_resident_bytes"] <= 100e6
+    assert st["peak_resident_bytes"] // need == 3   # three 30 MB cases fit
+    assert st["peak_resident_cases"] >= 2
+    for rid, n in enumerate(lives):                   # state advanced once per substep,
+        np.testing.assert_array_equal(srv.results[rid], rid + n)   # buffers alternate
+    # substeps of one case run one after another; different cases overlap
+    spans = {}
+    for rid, k, t0, t1 in fake.dev.log:
+        spans.setdefault(rid, []).append((k, t0, t1))
+    for rid, s in spans.items():
+        assert [k for k, _, _ in s] == list(range(lives[rid]))
+        assert all(b[1] >= a[2] - 1e-9 for a, b in zip(s, s[1:]))
+    first = {rid: s[0][1] for rid, s in spans.items()}
+    last = {rid: s[-1][2] for rid, s in spans.items()}
+    assert any(first[j] < last[i] for i in spans for j in spans if j > i)
+    assert st["p50_ms"] >= 0.9 * 10.0
+
+
+def test_budget_of_one_case_serialises_cases_and_counts_their_wait(fake):
+    trace = _trace([0.0, 0.0, 0.0], [3, 3, 3], 60_000_000, 0.01)
+    srv = serve.Server(budget_bytes=100e6, nstreams=3)
+    st = srv.run(trace)
+    assert st["substeps"] == 9 and st["peak_resident_cases"] == 1
+    spans = {}
+    for rid, k, t0, t1 in fake.dev.log:
+        spans.setdefault(rid, []).append((t0, t1))
+    assert spans[1][0][0] >= spans[0][-1][1] - 1e-9
+    assert spans[2][0][0] >= spans[1][-1][1] - 1e-9
+    # the third case's first substep waited for six others: its latency
+    # counts from arrival, so the p99 is well above one substep
+    assert st["p99_ms"] >= 50.0
+    assert st["queue_p99_ms"] >= 40.0
+
+
+def test_case_larger_than_the_budget_runs_alone(fake):
+    trace = _trace([0.0, 0.001], [2, 2], 150_000_000, 0.005)
+    srv = serve.Server(budget_bytes=100e6, nstreams=2)
+    st = srv.run(trace)
+    assert st["substeps"] == 4 and st["peak_resident_cases"] == 1
+    assert fake.closed == [0, 1]
