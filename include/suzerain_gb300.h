@@ -391,6 +391,18 @@ int sgb_gbtrs_batched_ws(char prec, char trans, int nsys, int N, int KL, int KU,
                          const void *fac, const int *ipiv, const void *b,
                          void *x, void *ywork, void *stream);
 
+/** One row-panel factor (fac, ipiv of one system) solved for nrhs
+ *  right-hand sides in one launch: column r of b (complex128, leading
+ *  dimension ldb >= N) gives column r of x (ldx >= N); x may equal b when
+ *  ldx == ldb.  ywork (nrhs x N complex of prec, or NULL) enables the
+ *  four-lanes-per-system sweeps for trans 'N'.  Replaces the per-column
+ *  zgbtrs loop of a bsmbsm_solver with nrhs > 1 and a reused factor
+ *  (suzerain/bsmbsm_solver.cpp:80-102, :155-182; the wavenumber-independent
+ *  operator of apps/perfect/operator_hybrid_isothermal.cpp:691-760). */
+int sgb_gbtrs_shared(char prec, char trans, int nrhs, int N, int KL, int KU,
+                     const void *fac, const int *ipiv, const void *b, long long ldb,
+                     void *x, long long ldx, void *ywork, void *stream);
+
 /** Batched zgbsvx: nsys systems of one geometry, one right-hand side each,
  *  every pointer on the device (rcond, ferr, berr, rpvgrw may also be host
  *  memory).  Per system: ab (ld ldab, stride ab_stride; overwritten by the

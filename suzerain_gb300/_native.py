@@ -146,6 +146,8 @@ _SIGS = {
                                _p, _p]),
     "sgb_gbtrs_batched_ws": (_i, [C.c_char, C.c_char, _i, _i, _i, _i, _p, _p, _p,
                                   _p, _p, _p]),
+    "sgb_gbtrs_shared": (_i, [C.c_char, C.c_char, _i, _i, _i, _i, _p, _p, _p, _ll,
+                              _p, _ll, _p, _p]),
     "sgb_factor_to_lapack": (_i, [C.c_char, _i, _i, _i, _i, _p, _p, _p]),
     "sgb_zcgbsvx_batched": (_i, [_i, _i, _i, _i, C.c_char, _p, _i, _ll, _p,
                                  _p, C.POINTER(RefineSpec),

@@ -194,6 +194,29 @@ extern "C" int sgb_gbtrs_batched_ws(char prec, char trans, int nsys, int N, int 
     return 0;
 }
 
+// One factor, many right-hand sides: the wavenumber-independent operator
+// factored once and solved for every wavenumber's right-hand side
+// (apps/perfect/operator_hybrid_isothermal.cpp:691-760, bsmbsm_solver with
+// nrhs > 1 and a reused factor, suzerain/bsmbsm_solver.cpp:80-102).
+extern "C" int sgb_gbtrs_shared(char prec, char trans, int nrhs, int N, int KL, int KU,
+                                const void *fac, const int *ipiv, const void *b, long long ldb,
+                                void *x, long long ldx, void *ywork, void *stream)
+{
+    trans = (char) toupper(trans);
+    if (prec != 'Z' && prec != 'C') return fail("sgb_gbtrs_shared: prec must be 'Z' or 'C'");
+    if (trans != 'N' && trans != 'T' && trans != 'C') return fail("sgb_gbtrs_shared: bad trans");
+    if (!geom_ok(N, KL, KU) || nrhs < 0) return fail("sgb_gbtrs_shared: bad geometry");
+    if (ldb < N || ldx < N) return fail("sgb_gbtrs_shared: ldb and ldx must be >= N");
+    GbtrsArgs a;
+    a.prec = prec; a.trans = trans; a.g = {N, KL, KU}; a.nsys = nrhs; a.fac = fac;
+    a.fac_stride = 0; a.ipiv = ipiv;
+    a.b = reinterpret_cast<const double2 *>(b); a.b_stride = ldb;
+    a.x = reinterpret_cast<double2 *>(x); a.x_stride = ldx;
+    a.ywork = ywork;
+    SGB_CUDA_TRY(launch_gbtrs(a, (cudaStream_t) stream));
+    return 0;
+}
+
 template <typename T2>
 __global__ void k_factor_to_lapack(int nsys, FactorGeom g, const T2 *__restrict__ fac,
                                    T2 *__restrict__ ab)

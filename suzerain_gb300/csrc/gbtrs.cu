@@ -77,7 +77,7 @@ k_gbtrs(FactorGeom g, int nsys, const cplx_t<R> *__restrict__ fac,
     int *rp = reinterpret_cast<int *>(rl + PD * KL);   // PD pivots
     const T2 *fu = fac + fi * fac_stride;
     const T2 *fl = fu + (long long) N * UW;
-    const int *pv = ipiv + fi * N;
+    const int *pv = ipiv + (fac_stride ? fi * N : 0);   // stride 0: one shared factor
     const bool cj = (TRANS == 2);
 
     // ring fillers: step t's data into slot t % PD (empty groups past the end)
@@ -330,7 +330,7 @@ k_gbtrs_fwd_quad(FactorGeom g, int nsys, const cplx_t<R> *__restrict__ fac, long
     double2 *rb = reinterpret_cast<double2 *>(rl + PD * L.RL);   // PD entering b
     int *rp = reinterpret_cast<int *>(rb + PD);                  // PD pivots
     const long long lbase = fi * fac_stride + (long long) N * g.UW();
-    const int *pv = act ? ipiv + fi * N : nullptr;
+    const int *pv = act ? ipiv + (fac_stride ? fi * N : 0) : nullptr;
     const double2 *bs = act ? b + s * b_stride : nullptr;
     T2 *ys = act ? yw + (long long) s * N : nullptr;
 

@@ -427,6 +427,28 @@ extern "C" int suzerain_lapack_cgbtrf(const int m, const int n, const int kl, co
                                       sgb_complex_float *ab, const int ldab, int *ipiv)
 { return gbtrf_legacy<float>(m, n, kl, ku, ab, ldab, ipiv); }
 
+// complex64 columns (leading dimension ld) <-> packed complex128, element t
+// = column t / n, row t % n.
+__global__ void k_widen_cols(int n, int nrhs, const float2 *__restrict__ src, long long ld,
+                             double2 *__restrict__ dst)
+{
+    const long long t = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+    if (t >= (long long) n * nrhs) return;
+    const long long r = t / n, i = t - r * n;
+    const float2 v = src[r * ld + i];
+    dst[t] = make_double2(v.x, v.y);
+}
+
+__global__ void k_narrow_cols(int n, int nrhs, const double2 *__restrict__ src,
+                              float2 *__restrict__ dst, long long ld)
+{
+    const long long t = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+    if (t >= (long long) n * nrhs) return;
+    const long long r = t / n, i = t - r * n;
+    const double2 v = src[t];
+    dst[r * ld + i] = make_float2((float) v.x, (float) v.y);
+}
+
 template <typename R>
 static int gbtrs_legacy(char trans, int n, int kl, int ku, int nrhs, const void *ab, int ldab,
                         const int *ipiv, void *b, int ldb)
@@ -452,26 +474,33 @@ static int gbtrs_legacy(char trans, int n, int kl, int ku, int nrhs, const void 
     if (sab.err || spv.err || sb.err) return err_of(cudaErrorMemoryAllocation, "gbtrs staging");
     k_lapack_to_rowpanel<T2><<<n, 128>>>(g, (const T2 *) sab.dev, ldab, (T2 *) g_pool.fac);
     cudaError_t e = cudaGetLastError();
-    // Solves run in FP64 storage; stage each right-hand side.
-    double2 *bz = nullptr;
-    if (e == cudaSuccess) e = cudaMalloc(&bz, (size_t) n * sizeof(double2));
-    for (int r = 0; r < nrhs && e == cudaSuccess; ++r) {
-        T2 *col = (T2 *) sb.dev + (size_t) r * ldb;
-        std::vector<T2> h(n);
-        std::vector<double2> hz(n);
-        e = cudaMemcpy(h.data(), col, n * sizeof(T2), cudaMemcpyDeviceToHost);
-        for (int i = 0; i < n; ++i) hz[i] = make_double2(h[i].x, h[i].y);
-        if (e == cudaSuccess) e = cudaMemcpy(bz, hz.data(), n * sizeof(double2), cudaMemcpyHostToDevice);
-        GbtrsArgs a;
-        a.prec = sizeof(R) == 8 ? 'Z' : 'C'; a.trans = trans; a.g = g; a.nsys = 1;
-        a.fac = g_pool.fac; a.fac_stride = g.fac_elems(); a.ipiv = (const int *) spv.dev;
+    // Every right-hand side in one launch over the one factor (stride 0:
+    // shared factor and pivots).  The solve reads and writes FP64, so
+    // complex64 columns are widened on the device and rounded back after.
+    GbtrsArgs a;
+    a.prec = sizeof(R) == 8 ? 'Z' : 'C'; a.trans = trans; a.g = g; a.nsys = nrhs;
+    a.fac = g_pool.fac; a.fac_stride = 0; a.ipiv = (const int *) spv.dev;
+    if constexpr (sizeof(R) == 8) {
+        a.b = (const double2 *) sb.dev; a.b_stride = ldb;
+        a.x = (double2 *) sb.dev; a.x_stride = ldb;
+        if (e == cudaSuccess) e = launch_gbtrs(a, 0);
+    } else {
+        const long long tot = (long long) n * nrhs;
+        const unsigned nblk = (unsigned) ((tot + 255) / 256);
+        double2 *bz = nullptr;
+        if (e == cudaSuccess) e = cudaMalloc(&bz, (size_t) tot * sizeof(double2));
+        if (e == cudaSuccess) {
+            k_widen_cols<<<nblk, 256>>>(n, nrhs, (const float2 *) sb.dev, ldb, bz);
+            e = cudaGetLastError();
+        }
         a.b = bz; a.b_stride = n; a.x = bz; a.x_stride = n;
         if (e == cudaSuccess) e = launch_gbtrs(a, 0);
-        if (e == cudaSuccess) e = cudaMemcpy(hz.data(), bz, n * sizeof(double2), cudaMemcpyDeviceToHost);
-        for (int i = 0; i < n; ++i) { h[i].x = (decltype(h[i].x)) hz[i].x; h[i].y = (decltype(h[i].y)) hz[i].y; }
-        if (e == cudaSuccess) e = cudaMemcpy(col, h.data(), n * sizeof(T2), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) {
+            k_narrow_cols<<<nblk, 256>>>(n, nrhs, bz, (float2 *) sb.dev, ldb);
+            e = cudaGetLastError();
+        }
+        if (bz) cudaFree(bz);
     }
-    if (bz) cudaFree(bz);
     if (e == cudaSuccess) e = sb.back();
     return err_of(e, "suzerain_lapack_gbtrs");
 }

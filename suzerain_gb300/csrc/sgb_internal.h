@@ -50,7 +50,7 @@ struct GbtrsArgs {
     FactorGeom g{};
     int nsys = 0;
     const void *fac = nullptr;
-    long long fac_stride = 0;
+    long long fac_stride = 0;    // 0: every system solves with one factor and its pivots
     const int *ipiv = nullptr;
     bool fwd_done = false;       // input already forward-eliminated (trans N only)
     const double2 *b = nullptr;  // FP64 input when !yin

@@ -148,6 +148,60 @@ def test_gbtrs_batched(lib, oracle, torch_cuda, n, kl, ku, trans, prec):
         assert berr <= (1e-14 if prec == "Z" else 1e-5), berr
 
 
+@pytest.mark.parametrize("n,kl,ku", [(40, 3, 5), (240, 34, 34), (97, 48, 48)])
+@pytest.mark.parametrize("trans", ["N", "T", "C"])
+@pytest.mark.parametrize("prec", ["Z", "C"])
+def test_gbtrs_shared_factor_many_rhs(lib, oracle, torch_cuda, n, kl, ku, trans, prec):
+    """One factor, nrhs right-hand sides with padded leading dimensions:
+    bit-identical to the batched solve over copies of the factor (the same
+    kernels, with and without the quad-lane scratch), padding untouched, and
+    every column a backward-stable solution of the dense system."""
+    torch = torch_cuda
+    rng = np.random.default_rng(23 + n + kl)
+    nrhs, ldb = 37, n + 3
+    band, ld = rand_band(rng, n, kl, ku)
+    fe = lib.sgb_factor_elems(n, kl, ku)
+    fdt = torch.complex128 if prec == "Z" else torch.complex64
+    fac = torch.zeros(fe, dtype=fdt, device="cuda")
+    ipiv = torch.zeros(n, dtype=torch.int32, device="cuda")
+    info = torch.zeros(1, dtype=torch.int32, device="cuda")
+    ab = dev(torch, band)
+    assert lib.sgb_gbtrf_batched(prec.encode(), 1, n, kl, ku, ab.data_ptr(), ld, ld * n,
+                                 fac.data_ptr(), ipiv.data_ptr(), info.data_ptr(), 0) == 0
+    B = rng.normal(size=(nrhs, ldb)) + 1j * rng.normal(size=(nrhs, ldb))
+    db = dev(torch, B)
+    facr, ipr = fac.repeat(nrhs), ipiv.repeat(nrhs)
+    bb = db[:, :n].contiguous()
+    A = oracle.band_to_dense(band, n, kl, ku, ld)
+    op = A if trans == "N" else (A.T if trans == "T" else A.conj().T)
+    for ws in (False, True):
+        x = torch.full((nrhs, ldb), float("nan"), dtype=torch.complex128, device="cuda")
+        yw = torch.zeros(nrhs * n, dtype=fdt, device="cuda") if ws else None
+        rc = lib.sgb_gbtrs_shared(prec.encode(), trans.encode(), nrhs, n, kl, ku, fac.data_ptr(),
+                                  ipiv.data_ptr(), db.data_ptr(), ldb, x.data_ptr(), ldb,
+                                  yw.data_ptr() if ws else None, 0)
+        assert rc == 0, lib.sgb_last_error().decode()
+        xr = torch.zeros_like(bb)
+        if ws:
+            ywr = torch.zeros(nrhs * n, dtype=fdt, device="cuda")
+            rc = lib.sgb_gbtrs_batched_ws(prec.encode(), trans.encode(), nrhs, n, kl, ku,
+                                          facr.data_ptr(), ipr.data_ptr(), bb.data_ptr(),
+                                          xr.data_ptr(), ywr.data_ptr(), 0)
+        else:
+            rc = lib.sgb_gbtrs_batched(prec.encode(), trans.encode(), nrhs, n, kl, ku,
+                                       facr.data_ptr(), ipr.data_ptr(), bb.data_ptr(),
+                                       xr.data_ptr(), 0)
+        assert rc == 0, lib.sgb_last_error().decode()
+        torch.cuda.synchronize()
+        xh, xrh = x.cpu().numpy(), xr.cpu().numpy()
+        assert np.array_equal(xh[:, :n].view(np.float64), xrh.view(np.float64)), ws
+        assert np.isnan(xh[:, n:].real).all() and (xh[:, n:].imag == 0).all()   # fill untouched
+        for r in range(nrhs):
+            berr = np.max(np.abs(op @ xh[r, :n] - B[r, :n])) / (
+                np.abs(op).sum(1).max() * np.abs(xh[r, :n]).max() + np.abs(B[r, :n]).max())
+            assert berr <= (1e-14 if prec == "Z" else 1e-5), (ws, r, berr)
+
+
 @pytest.mark.parametrize("n,kl,ku", [(1, 0, 0), (7, 0, 3), (13, 12, 0), (40, 3, 5),
                                      (240, 34, 34), (97, 48, 48), (50, 33, 40)])
 @pytest.mark.parametrize("prec", ["Z", "C"])
