@@ -304,6 +304,69 @@ int suzerain_diffwave_apply(const int dxcnt, const int dzcnt,
                             const int Nz, const int dNz, const int dkbz,
                             const int dkez);
 
+/** y <- alpha (i kx)^dxcnt (i kz)^dzcnt x + beta y on the same layout, with
+ *  y <- beta y on dealiased and Nyquist modes; x and y must not alias
+ *  (returns -1, where the reference asserts); suzerain/diffwave.h:142-151,
+ *  suzerain/diffwave.c:132-198. */
+int suzerain_diffwave_accumulate(const int dxcnt, const int dzcnt,
+                                 const sgb_complex_double alpha,
+                                 const sgb_complex_double *x,
+                                 const sgb_complex_double beta, sgb_complex_double *y,
+                                 const double Lx, const double Lz, const int Ny,
+                                 const int Nx, const int dNx, const int dkbx,
+                                 const int dkex, const int Nz, const int dNz,
+                                 const int dkbz, const int dkez);
+
+/** Diagonally scaled band matvecs of the explicit operator,
+ *  y <- (alpha0 D0 + ... ) op(A) x + beta y with one to five real diagonals
+ *  (entry i of D_t at d_t[i*ldd_t], ldd_t >= 0), a real n x n band A in BLAS
+ *  band storage (lda > kl + ku), x complex (_d_z) or real (_d_d), alpha_t,
+ *  beta and y complex; op(A) = A for 'N', A^T for 'T' and 'C'.  Argument
+ *  errors return the position the reference reports to xerbla (ldd_t at
+ *  7 + 3t, then lda, incx, incy); suzerain/blas_et_al/blasext.h:202-1000,
+ *  suzerain/blas_et_al/gbdmv.def ... gbdddddmv.def.  Host or device
+ *  pointers; the computation runs on the GPU. */
+int suzerain_blasext_zgbdmv_d_z(const char trans, const int n, const int kl, const int ku,
+    const sgb_complex_double alpha0, const double *d0, const int ldd0,
+    const double *a, const int lda, const sgb_complex_double *x, const int incx,
+    const sgb_complex_double beta, sgb_complex_double *y, const int incy);
+int suzerain_blasext_zgbdmv_d_d(const char trans, const int n, const int kl, const int ku,
+    const sgb_complex_double alpha0, const double *d0, const int ldd0,
+    const double *a, const int lda, const double *x, const int incx,
+    const sgb_complex_double beta, sgb_complex_double *y, const int incy);
+int suzerain_blasext_zgbddmv_d_z(const char trans, const int n, const int kl, const int ku,
+    const sgb_complex_double alpha0, const double *d0, const int ldd0, const sgb_complex_double alpha1, const double *d1, const int ldd1,
+    const double *a, const int lda, const sgb_complex_double *x, const int incx,
+    const sgb_complex_double beta, sgb_complex_double *y, const int incy);
+int suzerain_blasext_zgbddmv_d_d(const char trans, const int n, const int kl, const int ku,
+    const sgb_complex_double alpha0, const double *d0, const int ldd0, const sgb_complex_double alpha1, const double *d1, const int ldd1,
+    const double *a, const int lda, const double *x, const int incx,
+    const sgb_complex_double beta, sgb_complex_double *y, const int incy);
+int suzerain_blasext_zgbdddmv_d_z(const char trans, const int n, const int kl, const int ku,
+    const sgb_complex_double alpha0, const double *d0, const int ldd0, const sgb_complex_double alpha1, const double *d1, const int ldd1, const sgb_complex_double alpha2, const double *d2, const int ldd2,
+    const double *a, const int lda, const sgb_complex_double *x, const int incx,
+    const sgb_complex_double beta, sgb_complex_double *y, const int incy);
+int suzerain_blasext_zgbdddmv_d_d(const char trans, const int n, const int kl, const int ku,
+    const sgb_complex_double alpha0, const double *d0, const int ldd0, const sgb_complex_double alpha1, const double *d1, const int ldd1, const sgb_complex_double alpha2, const double *d2, const int ldd2,
+    const double *a, const int lda, const double *x, const int incx,
+    const sgb_complex_double beta, sgb_complex_double *y, const int incy);
+int suzerain_blasext_zgbddddmv_d_z(const char trans, const int n, const int kl, const int ku,
+    const sgb_complex_double alpha0, const double *d0, const int ldd0, const sgb_complex_double alpha1, const double *d1, const int ldd1, const sgb_complex_double alpha2, const double *d2, const int ldd2, const sgb_complex_double alpha3, const double *d3, const int ldd3,
+    const double *a, const int lda, const sgb_complex_double *x, const int incx,
+    const sgb_complex_double beta, sgb_complex_double *y, const int incy);
+int suzerain_blasext_zgbddddmv_d_d(const char trans, const int n, const int kl, const int ku,
+    const sgb_complex_double alpha0, const double *d0, const int ldd0, const sgb_complex_double alpha1, const double *d1, const int ldd1, const sgb_complex_double alpha2, const double *d2, const int ldd2, const sgb_complex_double alpha3, const double *d3, const int ldd3,
+    const double *a, const int lda, const double *x, const int incx,
+    const sgb_complex_double beta, sgb_complex_double *y, const int incy);
+int suzerain_blasext_zgbdddddmv_d_z(const char trans, const int n, const int kl, const int ku,
+    const sgb_complex_double alpha0, const double *d0, const int ldd0, const sgb_complex_double alpha1, const double *d1, const int ldd1, const sgb_complex_double alpha2, const double *d2, const int ldd2, const sgb_complex_double alpha3, const double *d3, const int ldd3, const sgb_complex_double alpha4, const double *d4, const int ldd4,
+    const double *a, const int lda, const sgb_complex_double *x, const int incx,
+    const sgb_complex_double beta, sgb_complex_double *y, const int incy);
+int suzerain_blasext_zgbdddddmv_d_d(const char trans, const int n, const int kl, const int ku,
+    const sgb_complex_double alpha0, const double *d0, const int ldd0, const sgb_complex_double alpha1, const double *d1, const int ldd1, const sgb_complex_double alpha2, const double *d2, const int ldd2, const sgb_complex_double alpha3, const double *d3, const int ldd3, const sgb_complex_double alpha4, const double *d4, const int ldd4,
+    const double *a, const int lda, const double *x, const int incx,
+    const sgb_complex_double beta, sgb_complex_double *y, const int incy);
+
 /** Solver specification (suzerain/specification_zgbsv.hpp:44-140): the
  *  method and the zcgbsvx refinement parameters.  Defaults (empty string):
  *  zcgbsvx, equil = reuse = false, aiter = 1, siter = -1, diter = 5,

@@ -130,6 +130,12 @@ _SIGS = {
     "suzerain_inorder_wavenumber": (_i, [_i, _i]),
     "suzerain_diffwave_apply": (_i, [_i, _i, ZC, _p, _d, _d, _i, _i, _i, _i,
                                      _i, _i, _i, _i, _i]),
+    "suzerain_diffwave_accumulate": (_i, [_i, _i, ZC, _p, ZC, _p, _d, _d, _i, _i,
+                                          _i, _i, _i, _i, _i, _i, _i]),
+    **{f"suzerain_blasext_{nm}_{sfx}": (_i, [C.c_char, _i, _i, _i] + [ZC, _p, _i] * k
+                                            + [_p, _i, _p, _i, ZC, _p, _i])
+       for k, nm in enumerate(("zgbdmv", "zgbddmv", "zgbdddmv", "zgbddddmv", "zgbdddddmv"), 1)
+       for sfx in ("d_z", "d_d")},
     # batched device API
     "sgb_last_error": (C.c_char_p, []),
     "sgb_device_ok": (_i, []),

@@ -11,6 +11,7 @@
 #include <cctype>
 #include <cstdlib>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <vector>
 
@@ -1117,6 +1118,31 @@ __global__ void k_diffwave(int dxcnt, int dzcnt, double2 alpha_ipow, double2 *__
     x[t] = cx_mul(x[t], ma);
 }
 
+// y <- alpha (i kx)^dxcnt (i kz)^dzcnt x + beta y per mode; dealiased and
+// Nyquist modes get y <- beta y (suzerain/diffwave.c:132-198).
+__global__ void k_diffwave_acc(int dxcnt, int dzcnt, double2 alpha_ipow,
+                               const double2 *__restrict__ x, double2 beta,
+                               double2 *__restrict__ y, double tpx, double tpz, int Ny,
+                               int Nx, int dNx, int dkbx, int dkex, int Nz, int dNz,
+                               int dkbz, int dkez)
+{
+    const long long sx = Ny, sz = (long long) (dkex - dkbx) * sx;
+    const long long tot = sz * (dkez - dkbz);
+    const long long t = (long long) blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= tot) return;
+    const int nn = (int) (t / sz) + dkbz;
+    const int m = (int) ((t % sz) / sx) + dkbx;
+    int nf = 0, mf = 0;
+    const bool nkeep = dzcnt > 0 ? (nf = wn_diff(Nz, dNz, nn)) != 0 : wn_abs(dNz, nn) <= (Nz - 1) / 2;
+    const bool mkeep = dxcnt > 0 ? (mf = wn_diff(Nx, dNx, m)) != 0 : wn_abs(dNx, m) <= (Nx - 1) / 2;
+    const double2 by = cx_mul(beta, y[t]);
+    if (!(nkeep && mkeep)) { y[t] = by; return; }
+    const double sc = pow_int(tpz * nf, dzcnt) * pow_int(tpx * mf, dxcnt);
+    const double2 ma = make_double2(sc * alpha_ipow.x, sc * alpha_ipow.y);
+    const double2 ax = cx_mul(ma, x[t]);
+    y[t] = make_double2(ax.x + by.x, ax.y + by.y);
+}
+
 extern "C" int suzerain_diffwave_apply(const int dxcnt, const int dzcnt,
                                        const sgb_complex_double alpha, sgb_complex_double *x,
                                        const double Lx, const double Lz, const int Ny, const int Nx,
@@ -1148,3 +1174,235 @@ extern "C" int suzerain_diffwave_apply(const int dxcnt, const int dzcnt,
     if (e == cudaSuccess) e = sx.back();
     return err_of(e, "suzerain_diffwave_apply");
 }
+
+extern "C" int suzerain_diffwave_accumulate(const int dxcnt, const int dzcnt,
+                                            const sgb_complex_double alpha,
+                                            const sgb_complex_double *x,
+                                            const sgb_complex_double beta, sgb_complex_double *y,
+                                            const double Lx, const double Lz, const int Ny,
+                                            const int Nx, const int dNx, const int dkbx,
+                                            const int dkex, const int Nz, const int dNz,
+                                            const int dkbz, const int dkez)
+{
+    if (dxcnt < 0 || dzcnt < 0 || Ny < 0 || Nx < 0 || dNx < Nx || dkex > dNx || dkbx > dkex ||
+        Nz < 0 || dNz < Nz || dkez > dNz || dkbz > dkez)
+        return -1;
+    const long long tot = (long long) Ny * (dkex - dkbx) * (dkez - dkbz);
+    if (tot == 0) return 0;
+    if ((const void *) x == (const void *) y) return -1;   // the reference requires x != y
+    double2 al, be;
+    std::memcpy(&al, &alpha, sizeof al);
+    std::memcpy(&be, &beta, sizeof be);
+    double2 ai;
+    switch ((dxcnt + dzcnt) & 3) {               // alpha * i^p
+    case 0: ai = al; break;
+    case 1: ai = make_double2(-al.y, al.x); break;
+    case 2: ai = make_double2(-al.x, -al.y); break;
+    default: ai = make_double2(al.y, -al.x); break;
+    }
+    const double pi = 3.1415926535897932384626433832795028841971693993751058209;
+    Stage sx(x, (size_t) tot * sizeof(double2), true);
+    Stage sy(y, (size_t) tot * sizeof(double2), true);
+    if (sx.err || sy.err) return err_of(sx.err ? sx.err : sy.err, "diffwave staging");
+    k_diffwave_acc<<<(unsigned) ((tot + 255) / 256), 256>>>(
+        dxcnt, dzcnt, ai, (const double2 *) sx.dev, be, (double2 *) sy.dev, 2 * pi / Lx,
+        2 * pi / Lz, Ny, Nx, dNx, dkbx, dkex, Nz, dNz, dkbz, dkez);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = sy.back();
+    return err_of(e, "suzerain_diffwave_accumulate");
+}
+
+// ---------------------------------------------------------------------------
+// Diagonally scaled band matvecs of the explicit operator:
+// y <- (sum_t alpha_t D_t) op(A) x + beta y with K = 1..5 real diagonals
+// D_t (entry i at d_t[i*ldd_t]), a real n x n band A (BLAS band storage), x
+// real or complex, alpha_t, beta, y complex; op(A) = A for 'N', A^T for 'T'
+// and 'C' (no conjugation: A is real).  suzerain/blas_et_al/gbdmv.def,
+// gbddmv.def, gbdddmv.def, gbddddmv.def, gbdddddmv.def (FUNCTION bodies) and
+// their z*_d_z / z*_d_d wrappers in suzerain/blas_et_al/blasext.c.  One
+// thread per output element: the band row (or column) dot product, then the
+// diagonal combination at the output index.
+namespace {
+
+struct GbdDiags {
+    double2 alpha[5];
+    const double *d[5];
+    int ldd[5];
+};
+
+__device__ __forceinline__ double2 gbd_mul(double a, double2 x) { return make_double2(a * x.x, a * x.y); }
+__device__ __forceinline__ double2 gbd_mul(double a, double x) { return make_double2(a * x, 0.0); }
+
+template <int K, typename TX>
+__global__ void k_gbdmv(int t, int n, int kl, int ku, GbdDiags g, const double *__restrict__ a,
+                        int lda, const TX *__restrict__ x, int incx, int kx, double2 beta,
+                        double2 *__restrict__ y, int incy, int ky, bool beta_one, bool beta_zero,
+                        bool alpha_zero)
+{
+    const int o = blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= n) return;
+    double2 *yp = y + ky + (long long) o * incy;
+    const double2 base = beta_zero ? make_double2(0, 0) : (beta_one ? *yp : cx_mul(beta, *yp));
+    if (alpha_zero) { *yp = base; return; }
+    double2 acc = make_double2(0, 0);
+    if (!t) {                    // row o of A times x
+        for (int j = max(0, o - kl); j <= min(n - 1, o + ku); ++j)
+            acc = cx_add(acc, gbd_mul(a[ku + o - j + (long long) j * lda], x[kx + (long long) j * incx]));
+    } else {                     // column o of A times x
+        for (int i = max(0, o - ku); i <= min(n - 1, o + kl); ++i)
+            acc = cx_add(acc, gbd_mul(a[ku + i - o + (long long) o * lda], x[kx + (long long) i * incx]));
+    }
+    double2 c = make_double2(0, 0);
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const double dv = g.d[k][(long long) o * g.ldd[k]];
+        c = make_double2(c.x + g.alpha[k].x * dv, c.y + g.alpha[k].y * dv);
+    }
+    *yp = cx_add(base, cx_mul(c, acc));
+}
+
+template <int K, typename TX>
+int gbdmv_dropin(const char *name, char trans, int n, int kl, int ku, const double2 *alpha,
+                 const double *const *d, const int *ldd, const double *a, int lda, const TX *x,
+                 int incx, double2 beta, double2 *y, int incy)
+{
+    // argument positions of the reference's checks: ldd_t at 7 + 3t, then
+    // lda, incx, incy (the one-diagonal form reports incy as 13)
+    const int p_lda = 3 * K + 6, p_incx = 3 * K + 8, p_incy = K == 1 ? 13 : 3 * K + 11;
+    trans = (char) std::toupper((unsigned char) trans);
+    int info = 0;
+    if (trans != 'N' && trans != 'T' && trans != 'C') info = 1;
+    else if (n < 0) info = 2;
+    else if (kl < 0) info = 3;
+    else if (ku < 0) info = 4;
+    for (int k = 0; k < K && !info; ++k)
+        if (ldd[k] < 0) info = 7 + 3 * k;
+    if (!info) {
+        if (lda <= kl + ku) info = p_lda;
+        else if (incx == 0) info = p_incx;
+        else if (incy == 0) info = p_incy;
+    }
+    if (info) return info;
+    if (n == 0) return 0;
+    bool alpha_zero = true;
+    GbdDiags g{};
+    std::vector<std::unique_ptr<Stage>> sd;
+    for (int k = 0; k < K; ++k) {
+        g.alpha[k] = alpha[k];
+        g.ldd[k] = ldd[k];
+        alpha_zero = alpha_zero && alpha[k].x == 0 && alpha[k].y == 0;
+        sd.emplace_back(new Stage(d[k], ((size_t) (n - 1) * ldd[k] + 1) * sizeof(double), true));
+        if (sd.back()->err) return err_of(sd.back()->err, "gbdmv staging");
+        g.d[k] = (const double *) sd.back()->dev;
+    }
+    const bool beta_one = beta.x == 1 && beta.y == 0, beta_zero = beta.x == 0 && beta.y == 0;
+    if (alpha_zero && beta_one) return 0;
+    Stage sa(a, (size_t) lda * n * sizeof(double), true);
+    Stage sx(x, span_bytes(n, incx, sizeof(TX)), true);
+    Stage sy(y, span_bytes(n, incy, sizeof(double2)), true);
+    if (sa.err || sx.err || sy.err) return err_of(cudaErrorMemoryAllocation, "gbdmv staging");
+    const int kx = incx > 0 ? 0 : (1 - n) * incx, ky = incy > 0 ? 0 : (1 - n) * incy;
+    k_gbdmv<K, TX><<<(n + 127) / 128, 128>>>(trans != 'N', n, kl, ku, g, (const double *) sa.dev, lda,
+                                             (const TX *) sx.dev, incx, kx, beta, (double2 *) sy.dev,
+                                             incy, ky, beta_one, beta_zero, alpha_zero);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = sy.back();
+    return err_of(e, name);
+}
+
+inline double2 zc2(const sgb_complex_double &z) { double2 v; std::memcpy(&v, &z, sizeof v); return v; }
+
+}  // namespace
+
+#define SGB_GBD_TAIL(TX, XT)                                                       \
+    const double *a, const int lda, const XT *x, const int incx,                   \
+    const sgb_complex_double beta, sgb_complex_double *y, const int incy
+
+#define SGB_GBD_CALL(K, TX, NAME)                                                  \
+    gbdmv_dropin<K, TX>(NAME, trans, n, kl, ku, al, d, ldd, a, lda,                \
+                        reinterpret_cast<const TX *>(x), incx, zc2(beta),          \
+                        reinterpret_cast<double2 *>(y), incy)
+
+#define SGB_GBD1(SFX, TX, XT)                                                      \
+extern "C" int suzerain_blasext_zgbdmv_##SFX(                                      \
+    const char trans, const int n, const int kl, const int ku,                     \
+    const sgb_complex_double alpha0, const double *d0, const int ldd0,             \
+    SGB_GBD_TAIL(TX, XT))                                                          \
+{                                                                                  \
+    const double2 al[1] = {zc2(alpha0)};                                           \
+    const double *d[1] = {d0};                                                     \
+    const int ldd[1] = {ldd0};                                                     \
+    return SGB_GBD_CALL(1, TX, "suzerain_blasext_zgbdmv_" #SFX);                   \
+}
+
+#define SGB_GBD2(SFX, TX, XT)                                                      \
+extern "C" int suzerain_blasext_zgbddmv_##SFX(                                     \
+    const char trans, const int n, const int kl, const int ku,                     \
+    const sgb_complex_double alpha0, const double *d0, const int ldd0,             \
+    const sgb_complex_double alpha1, const double *d1, const int ldd1,             \
+    SGB_GBD_TAIL(TX, XT))                                                          \
+{                                                                                  \
+    const double2 al[2] = {zc2(alpha0), zc2(alpha1)};                              \
+    const double *d[2] = {d0, d1};                                                 \
+    const int ldd[2] = {ldd0, ldd1};                                               \
+    return SGB_GBD_CALL(2, TX, "suzerain_blasext_zgbddmv_" #SFX);                  \
+}
+
+#define SGB_GBD3(SFX, TX, XT)                                                      \
+extern "C" int suzerain_blasext_zgbdddmv_##SFX(                                    \
+    const char trans, const int n, const int kl, const int ku,                     \
+    const sgb_complex_double alpha0, const double *d0, const int ldd0,             \
+    const sgb_complex_double alpha1, const double *d1, const int ldd1,             \
+    const sgb_complex_double alpha2, const double *d2, const int ldd2,             \
+    SGB_GBD_TAIL(TX, XT))                                                          \
+{                                                                                  \
+    const double2 al[3] = {zc2(alpha0), zc2(alpha1), zc2(alpha2)};                 \
+    const double *d[3] = {d0, d1, d2};                                             \
+    const int ldd[3] = {ldd0, ldd1, ldd2};                                         \
+    return SGB_GBD_CALL(3, TX, "suzerain_blasext_zgbdddmv_" #SFX);                 \
+}
+
+#define SGB_GBD4(SFX, TX, XT)                                                      \
+extern "C" int suzerain_blasext_zgbddddmv_##SFX(                                   \
+    const char trans, const int n, const int kl, const int ku,                     \
+    const sgb_complex_double alpha0, const double *d0, const int ldd0,             \
+    const sgb_complex_double alpha1, const double *d1, const int ldd1,             \
+    const sgb_complex_double alpha2, const double *d2, const int ldd2,             \
+    const sgb_complex_double alpha3, const double *d3, const int ldd3,             \
+    SGB_GBD_TAIL(TX, XT))                                                          \
+{                                                                                  \
+    const double2 al[4] = {zc2(alpha0), zc2(alpha1), zc2(alpha2), zc2(alpha3)};    \
+    const double *d[4] = {d0, d1, d2, d3};                                         \
+    const int ldd[4] = {ldd0, ldd1, ldd2, ldd3};                                   \
+    return SGB_GBD_CALL(4, TX, "suzerain_blasext_zgbddddmv_" #SFX);                \
+}
+
+#define SGB_GBD5(SFX, TX, XT)                                                      \
+extern "C" int suzerain_blasext_zgbdddddmv_##SFX(                                  \
+    const char trans, const int n, const int kl, const int ku,                     \
+    const sgb_complex_double alpha0, const double *d0, const int ldd0,             \
+    const sgb_complex_double alpha1, const double *d1, const int ldd1,             \
+    const sgb_complex_double alpha2, const double *d2, const int ldd2,             \
+    const sgb_complex_double alpha3, const double *d3, const int ldd3,             \
+    const sgb_complex_double alpha4, const double *d4, const int ldd4,             \
+    SGB_GBD_TAIL(TX, XT))                                                          \
+{                                                                                  \
+    const double2 al[5] = {zc2(alpha0), zc2(alpha1), zc2(alpha2), zc2(alpha3),     \
+                           zc2(alpha4)};                                           \
+    const double *d[5] = {d0, d1, d2, d3, d4};                                     \
+    const int ldd[5] = {ldd0, ldd1, ldd2, ldd3, ldd4};                             \
+    return SGB_GBD_CALL(5, TX, "suzerain_blasext_zgbdddddmv_" #SFX);               \
+}
+
+SGB_GBD1(d_z, double2, sgb_complex_double)
+SGB_GBD1(d_d, double, double)
+SGB_GBD2(d_z, double2, sgb_complex_double)
+SGB_GBD2(d_d, double, double)
+SGB_GBD3(d_z, double2, sgb_complex_double)
+SGB_GBD3(d_d, double, double)
+SGB_GBD4(d_z, double2, sgb_complex_double)
+SGB_GBD4(d_d, double, double)
+SGB_GBD5(d_z, double2, sgb_complex_double)
+SGB_GBD5(d_d, double, double)

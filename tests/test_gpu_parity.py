@@ -765,6 +765,96 @@ def test_dropin_gbmv_and_diffwave(lib, oracle):
                     sc = (1.5 - 0.5j) * (1j * 2 * np.pi / Lz * (nf or 0)) ** dz * (1j * 2 * np.pi / Lx * (mf or 0)) ** dx
                     exp[nz, mx] = f[nz, mx] * sc
         assert np.allclose(g, exp, rtol=1e-14, atol=1e-13)
+        # accumulate: y <- alpha D x + beta y, y <- beta y where D zeroes the
+        # mode; on a sub-block of modes (dkbx..dkex, dkbz..dkez)
+        bx, ex, bz, ez = 1, dNx - 2, 2, dNz
+        xs = np.ascontiguousarray(f[bz:ez, bx:ex])
+        y0 = rng.normal(size=xs.shape) + 1j * rng.normal(size=xs.shape)
+        y1 = y0.copy()
+        assert lib.suzerain_diffwave_accumulate(dx, dz, nat.zc(1.5 - 0.5j), xs.ctypes.data,
+                                                nat.zc(0.25 + 2j), y1.ctypes.data, Lx, Lz, Ny,
+                                                Nx, dNx, bx, ex, Nz, dNz, bz, ez) == 0
+        keep = (exp[bz:ez, bx:ex] != 0).any(axis=2)
+        want = np.where(keep[..., None], exp[bz:ez, bx:ex], 0) + (0.25 + 2j) * y0
+        assert np.allclose(y1, want, rtol=1e-14, atol=1e-13)
+        assert lib.suzerain_diffwave_accumulate(dx, dz, nat.zc(1.0), y1.ctypes.data, nat.zc(1.0),
+                                                y1.ctypes.data, Lx, Lz, Ny, Nx, dNx, bx, ex,
+                                                Nz, dNz, bz, ez) == -1   # x, y alias
+
+
+def _strided(v, inc):
+    s = np.zeros((len(v) - 1) * abs(inc) + 1, dtype=v.dtype)
+    s[::abs(inc)] = v if inc > 0 else v[::-1]
+    return s
+
+
+def _logical(s, n, inc):
+    v = s[::abs(inc)][:n]
+    return v if inc > 0 else v[::-1]
+
+
+@pytest.mark.parametrize("k", [1, 2, 3, 4, 5])
+@pytest.mark.parametrize("xreal", [False, True])
+def test_dropin_blasext_gbdmv(lib, k, xreal):
+    """y <- (sum alpha_t D_t) op(A) x + beta y against a dense evaluation, over
+    trans N/T/C, strides of both signs, diagonal strides 0..3; beta = 0 clears
+    NaN in y, all-zero alphas leave beta y; argument errors at the reference's
+    positions (suzerain/blas_et_al/gbd*mv.def)."""
+    from suzerain_gb300 import _native as nat
+    name = {1: "zgbdmv", 2: "zgbddmv", 3: "zgbdddmv", 4: "zgbddddmv", 5: "zgbdddddmv"}[k]
+    f = getattr(lib, f"suzerain_blasext_{name}_{'d_d' if xreal else 'd_z'}")
+    rng = np.random.default_rng(31 + k + 7 * xreal)
+    n, kl, ku = 37, 4, 3
+    lda = kl + ku + 2
+    a = rng.normal(size=lda * n)
+    A = np.zeros((n, n))
+    for j in range(n):
+        for i in range(max(0, j - ku), min(n, j + kl + 1)):
+            A[i, j] = a[ku + i - j + j * lda]
+    ldd = [1, 0, 2, 1, 3][:k]
+    ds = [rng.normal(size=(n - 1) * l + 1) for l in ldd]
+
+    def call(trans, alphas, x, incx, beta, y, incy, lda_=lda, ldd_=ldd):
+        args = [trans.encode(), n, kl, ku]
+        for al, d, l in zip(alphas, ds, ldd_):
+            args += [nat.zc(al), d.ctypes.data, l]
+        return f(*args, a.ctypes.data, lda_, x.ctypes.data, incx, nat.zc(beta), y.ctypes.data, incy)
+
+    for trans, incx, incy in (("N", 1, 1), ("T", 2, -1), ("C", -1, 3), ("n", -2, 2)):
+        alphas = [complex(rng.normal(), rng.normal()) for _ in range(k)]
+        beta = 0.5 - 0.25j
+        xl = rng.normal(size=n) if xreal else rng.normal(size=n) + 1j * rng.normal(size=n)
+        yl = rng.normal(size=n) + 1j * rng.normal(size=n)
+        xs, ys = _strided(xl, incx), _strided(yl, incy)
+        if abs(incy) > 1:
+            ys[np.arange(len(ys)) % abs(incy) != 0] = 7 + 7j    # gaps stay untouched
+        ys0 = ys.copy()
+        c = sum(al * d[np.arange(n) * l] for al, d, l in zip(alphas, ds, ldd))
+        op = A if trans.upper() == "N" else A.T
+        want = beta * yl + c * (op @ xl)
+        assert call(trans, alphas, xs, incx, beta, ys, incy) == 0
+        assert np.allclose(_logical(ys, n, incy), want, rtol=1e-13, atol=1e-13), trans
+        gap = np.arange(len(ys)) % abs(incy) != 0
+        assert np.array_equal(ys[gap], ys0[gap])
+    xs = rng.normal(size=n) if xreal else rng.normal(size=n) + 1j * rng.normal(size=n)
+    y = np.full(n, np.nan + 0j)
+    assert call("N", [1.0] * k, xs, 1, 0.0, y, 1) == 0                 # beta = 0 clears y
+    c = sum(d[np.arange(n) * l] for d, l in zip(ds, ldd))
+    assert np.allclose(y, c * (A @ xs), rtol=1e-13, atol=1e-13)
+    y0 = rng.normal(size=n) + 1j * rng.normal(size=n)
+    y = y0.copy()
+    xn = np.full(n, np.nan) if xreal else np.full(n, np.nan + 0j)
+    assert call("T", [0.0] * k, xn, 1, 2.0, y, 1) == 0                  # alphas zero: beta y
+    assert np.array_equal(y, 2.0 * y0)
+    y = y0.copy()
+    assert call("X", [1.0] * k, xs, 1, 1.0, y, 1) == 1
+    assert call("N", [1.0] * k, xs, 1, 1.0, y, 1, ldd_=[-1] + ldd[1:]) == 7
+    if k > 1:
+        assert call("N", [1.0] * k, xs, 1, 1.0, y, 1, ldd_=ldd[:-1] + [-1]) == 7 + 3 * (k - 1)
+    assert call("N", [1.0] * k, xs, 1, 1.0, y, 1, lda_=kl + ku) == 3 * k + 6
+    assert call("N", [1.0] * k, xs, 0, 1.0, y, 1) == 3 * k + 8
+    assert call("N", [1.0] * k, xs, 1, 1.0, y, 0) == (13 if k == 1 else 3 * k + 11)
+    assert np.array_equal(y, y0)
 
 
 def test_dropin_bsplineop_accumulate_golden(lib):
