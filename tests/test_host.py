@@ -32,6 +32,35 @@ def test_library_exports_every_declared_symbol(native):
     assert len(declared_symbols()) > 40
 
 
+def declared_signatures():
+    """name -> number of parameters, from the function declarations of the
+    public headers (comments removed, one declaration per ';')."""
+    out = {}
+    for fn in os.listdir(os.path.join(ROOT, "include")):
+        if not fn.endswith(".h"):
+            continue
+        src = open(os.path.join(ROOT, "include", fn)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        src = re.sub(r"//[^\n]*", "", src)
+        for m in re.finditer(r"\b((?:suzerain|sgb)_[A-Za-z0-9_]+)\s*\(([^;{]*?)\)\s*;", src):
+            params = m.group(2).strip()
+            out[m.group(1)] = 0 if params in ("", "void") else params.count(",") + 1
+    return out
+
+
+def test_bindings_match_declared_parameter_counts():
+    """Every ctypes binding of the package passes as many arguments as the C
+    declaration takes (a missing argument would shift every later one)."""
+    from suzerain_gb300 import _native as nat
+    sigs = declared_signatures()
+    assert len(sigs) > 60
+    bad = {name: (len(args), sigs[name]) for name, (_, args) in nat._SIGS.items()
+           if name in sigs and len(args) != sigs[name]}
+    assert not bad, bad
+    unbound = [n for n in nat._SIGS if n not in sigs]
+    assert not unbound, unbound
+
+
 def test_construct_q_qinv(native):
     g = native.suzerain_bsmbsm_construct(5, 192, 6, 6)
     assert (g.S, g.n, g.N, g.KL, g.KU, g.LD) == (5, 192, 960, 34, 34, 69)
