@@ -140,6 +140,12 @@ def ref():
                                                  _p, _p, _p, _p, _p]
         L.suzerain_blas_zgbmv.argtypes = [C.c_char, _i, _i, _i, _i, _Z, _p,
                                           _i, _p, _i, _Z, _p, _i]
+        for k in range(1, 6):
+            for sfx in ("dzz", "ddz"):
+                f = getattr(L, f"oracle_ref_gbd{k}mv_{sfx}")
+                f.argtypes = [C.c_char, _i, _i, _i] + [_Z, _p, _i] * k + [_p, _i, _p, _i,
+                                                                          _Z, _p, _i]
+                f.restype = _i
         L.oracle_ref_single_thread()
         _ref = L
     return _ref
@@ -371,6 +377,25 @@ def assemble_case(case, phi, kx, kz, layout="packc"):
 # --------------------------------------------------------------------------
 # Dense helpers for checks (small sizes only)
 # --------------------------------------------------------------------------
+def gbdmv(trans, n, kl, ku, alphas, ds, ldds, a, lda, x, beta, y) -> np.ndarray:
+    """y <- (sum_t alpha_t D_t) op(A) x + beta y on logical (unit-stride)
+    vectors, D_t[i] = ds[t][i*ldds[t]], A the real n x n band in BLAS storage,
+    op(A) = A for 'N' and A^T for 'T' and 'C' (A is real); beta = 0 ignores
+    y, and all-zero alphas leave beta y.  The operator of
+    suzerain/blas_et_al/gbdmv.def ... gbdddddmv.def
+    (suzerain/blas_et_al/gbddmv.def:131-190 for two diagonals)."""
+    A = np.zeros((n, n))
+    for j in range(n):
+        for i in range(max(0, j - ku), min(n, j + kl + 1)):
+            A[i, j] = a[ku + i - j + j * lda]
+    base = np.zeros(n, complex) if beta == 0 else beta * np.asarray(y, complex)
+    if all(al == 0 for al in alphas):
+        return base
+    c = sum(al * d[np.arange(n) * l] for al, d, l in zip(alphas, ds, ldds))
+    op = A if trans.upper() == "N" else A.T
+    return base + c * (op @ x)
+
+
 def band_to_dense(ab, n, kl, ku, ldab, off=0):
     """Dense A from column-major band storage with A(i,j) at
     ab[off + ku + i - j + j*ldab]."""

@@ -274,6 +274,67 @@ def test_gbmv_matches_reference(oracle):
             assert np.allclose(y1, y2, rtol=1e-13, atol=1e-13)
 
 
+def _strided(v, inc):
+    s = np.zeros((len(v) - 1) * abs(inc) + 1, dtype=v.dtype)
+    s[::abs(inc)] = v if inc > 0 else v[::-1]
+    return s
+
+
+def _logical(s, n, inc):
+    v = s[::abs(inc)][:n]
+    return v if inc > 0 else v[::-1]
+
+
+@pytest.mark.parametrize("k", [1, 2, 3, 4, 5])
+@pytest.mark.parametrize("xreal", [False, True])
+def test_gbdmv_matches_reference(oracle, k, xreal):
+    """The oracle's diagonally scaled band matvec (the formula the GPU drop-in
+    tests check against) equals the reference's own gbd*mv.def code over
+    trans N/T/C, strides of both signs, diagonal strides 0..3, beta = 0 and
+    all-zero alphas; the reference's argument-error positions (which the
+    drop-ins return) are those the GPU tests expect."""
+    R = oracle.ref()
+    if R is None:
+        pytest.skip("reference build absent")
+    f = getattr(R, f"oracle_ref_gbd{k}mv_{'ddz' if xreal else 'dzz'}")
+    rng = np.random.default_rng(41 + k + 5 * xreal)
+    n, kl, ku = 37, 4, 3
+    lda = kl + ku + 2
+    a = rng.normal(size=lda * n)
+    ldd = [1, 0, 2, 1, 3][:k]
+    ds = [rng.normal(size=(n - 1) * l + 1) for l in ldd]
+
+    def call(trans, alphas, xs, incx, beta, ys, incy, lda_=lda, ldd_=ldd):
+        args = [trans.encode(), n, kl, ku]
+        for al, d, l in zip(alphas, ds, ldd_):
+            args += [oracle._z(al), d.ctypes.data, l]
+        return f(*args, a.ctypes.data, lda_, xs.ctypes.data, incx, oracle._z(beta),
+                 ys.ctypes.data, incy)
+
+    cases = [("N", 1, 1, 0.5 - 0.25j), ("T", 2, -1, 1.0), ("C", -1, 3, 0.0), ("n", -2, 2, 2j)]
+    for trans, incx, incy, beta in cases:
+        alphas = [complex(rng.normal(), rng.normal()) for _ in range(k)]
+        xl = rng.normal(size=n) if xreal else rng.normal(size=n) + 1j * rng.normal(size=n)
+        yl = rng.normal(size=n) + 1j * rng.normal(size=n)
+        xs, ys = _strided(xl, incx), _strided(yl, incy)
+        assert call(trans, alphas, xs, incx, beta, ys, incy) == 0
+        want = oracle.gbdmv(trans, n, kl, ku, alphas, ds, ldd, a, lda, xl, beta, yl)
+        assert np.allclose(_logical(ys, n, incy), want, rtol=1e-13, atol=1e-13), trans
+    y0 = rng.normal(size=n) + 1j * rng.normal(size=n)
+    xn = np.full(n, np.nan) if xreal else np.full(n, np.nan + 0j)
+    y = y0.copy()
+    assert call("T", [0.0] * k, xn, 1, 2.0, y, 1) == 0
+    assert np.array_equal(y, oracle.gbdmv("T", n, kl, ku, [0.0] * k, ds, ldd, a, lda, xn, 2.0, y0))
+    xs = rng.normal(size=n) + (0 if xreal else 1j * rng.normal(size=n))
+    assert call("X", [1.0] * k, xs, 1, 1.0, y, 1) == 1
+    assert call("N", [1.0] * k, xs, 1, 1.0, y, 1, ldd_=[-1] + ldd[1:]) == 7
+    if k > 1:
+        assert call("N", [1.0] * k, xs, 1, 1.0, y, 1, ldd_=ldd[:-1] + [-1]) == 7 + 3 * (k - 1)
+    assert call("N", [1.0] * k, xs, 1, 1.0, y, 1, lda_=kl + ku) == 3 * k + 6
+    assert call("N", [1.0] * k, xs, 0, 1.0, y, 1) == 3 * k + 8
+    assert call("N", [1.0] * k, xs, 1, 1.0, y, 0) == (13 if k == 1 else 3 * k + 11)
+
+
 # --------------------------------------------------------------------------
 # zgbsvx: the restatement against LAPACK's own zgbsvx (SciPy's OpenBLAS, the
 # routine suzerain_lapack_zgbsvx forwards to)
