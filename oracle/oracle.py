@@ -146,6 +146,11 @@ def ref():
                 f.argtypes = [C.c_char, _i, _i, _i] + [_Z, _p, _i] * k + [_p, _i, _p, _i,
                                                                           _Z, _p, _i]
                 f.restype = _i
+        dw = [_i, _i, _Z, _p, _d, _d, _i, _i, _i, _i, _i, _i, _i, _i, _i]
+        L.suzerain_diffwave_apply.argtypes = dw
+        L.suzerain_diffwave_apply.restype = None
+        L.suzerain_diffwave_accumulate.argtypes = dw[:4] + [_Z, _p] + dw[4:]
+        L.suzerain_diffwave_accumulate.restype = None
         L.oracle_ref_single_thread()
         _ref = L
     return _ref
@@ -394,6 +399,47 @@ def gbdmv(trans, n, kl, ku, alphas, ds, ldds, a, lda, x, beta, y) -> np.ndarray:
     c = sum(al * d[np.arange(n) * l] for al, d, l in zip(alphas, ds, ldds))
     op = A if trans.upper() == "N" else A.T
     return base + c * (op @ x)
+
+
+def diffwave_factors(dxcnt, dzcnt, alpha, Lx, Lz, Nx, dNx, dkbx, dkex, Nz, dNz,
+                     dkbz, dkez) -> np.ndarray:
+    """Per-mode factor alpha (i 2 pi m / Lx)^dxcnt (i 2 pi n / Lz)^dzcnt of the
+    in-order modes dkbz..dkez-1 (rows) x dkbx..dkex-1 (columns), 0 where the
+    mode is dropped: a differentiated direction keeps the wavenumbers that
+    suzerain_inorder_wavenumber_diff maps to nonzero, an undifferentiated one
+    those with |k| <= (N-1)/2 (suzerain/diffwave.c:66-131,
+    suzerain/inorder.h:92-96, :112-116, :145-149, :282-296)."""
+    def wabs(N, i):
+        return i if i < N // 2 + 1 else N - i
+
+    def wdiff(N, dN, i):
+        return i if i < (N + 1) // 2 else (-dN + i if i >= dN - (N - 1) // 2 else 0)
+
+    f = np.zeros((dkez - dkbz, dkex - dkbx), complex)
+    for n in range(dkbz, dkez):
+        nf = wdiff(Nz, dNz, n) if dzcnt else 0
+        if not (nf != 0 if dzcnt else wabs(dNz, n) <= (Nz - 1) // 2):
+            continue
+        for m in range(dkbx, dkex):
+            mf = wdiff(Nx, dNx, m) if dxcnt else 0
+            if mf != 0 if dxcnt else wabs(dNx, m) <= (Nx - 1) // 2:
+                f[n - dkbz, m - dkbx] = (alpha * (1j * 2 * np.pi / Lz * nf) ** dzcnt
+                                         * (1j * 2 * np.pi / Lx * mf) ** dxcnt)
+    return f
+
+
+def diffwave_apply(dxcnt, dzcnt, alpha, x, Lx, Lz, Nx, dNx, dkbx, dkex, Nz, dNz,
+                   dkbz, dkez) -> np.ndarray:
+    """x (Z, X, Y in C order: Y fastest) scaled mode by mode."""
+    f = diffwave_factors(dxcnt, dzcnt, alpha, Lx, Lz, Nx, dNx, dkbx, dkex, Nz, dNz, dkbz, dkez)
+    return np.where(f[..., None] != 0, x * f[..., None], 0)
+
+
+def diffwave_accumulate(dxcnt, dzcnt, alpha, x, beta, y, Lx, Lz, Nx, dNx, dkbx, dkex,
+                        Nz, dNz, dkbz, dkez) -> np.ndarray:
+    """alpha D x + beta y, beta y on dropped modes (suzerain/diffwave.c:132-198)."""
+    return diffwave_apply(dxcnt, dzcnt, alpha, x, Lx, Lz, Nx, dNx, dkbx, dkex, Nz, dNz,
+                          dkbz, dkez) + beta * y
 
 
 def band_to_dense(ab, n, kl, ku, ldab, off=0):

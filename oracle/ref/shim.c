@@ -173,6 +173,23 @@ void suzerain_blas_zaxpy(const int n, const complex_double alpha,
     for (int i = 0; i < n; ++i, ix += incx, iy += incy) y[iy] += alpha * x[ix];
 }
 
+void suzerain_blas_zscal(const int n, const complex_double alpha,
+                         complex_double *x, const int incx)
+{
+    for (int i = 0; i < n; ++i) x[i * incx] *= alpha;
+}
+
+/* The reference's MKL configuration: scale y by beta (unless beta == 1),
+ * then y += alpha x (suzerain/blas_et_al/blas.c:636-657). */
+void suzerain_blas_zaxpby(const int n, const complex_double alpha,
+                          const complex_double *x, const int incx,
+                          const complex_double beta, complex_double *y,
+                          const int incy)
+{
+    if (beta != 1.0) suzerain_blas_zscal(n, beta, y, incy);
+    suzerain_blas_zaxpy(n, alpha, x, incx, y, incy);
+}
+
 void suzerain_blas_daxpy(const int n, const double alpha, const double *x,
                          const int incx, double *y, const int incy)
 {

@@ -335,6 +335,38 @@ def test_gbdmv_matches_reference(oracle, k, xreal):
     assert call("N", [1.0] * k, xs, 1, 1.0, y, 0) == (13 if k == 1 else 3 * k + 11)
 
 
+@pytest.mark.parametrize("Nx,dNx,Nz,dNz", [(8, 12, 6, 9), (7, 7, 6, 6), (16, 24, 11, 17)])
+def test_diffwave_matches_reference(oracle, Nx, dNx, Nz, dNz):
+    """The oracle's Fourier derivative (the formula of the GPU diffwave tests)
+    equals the reference's own suzerain/diffwave.c for apply and accumulate,
+    derivative orders 0..3, whole and partial blocks of modes, dealiased and
+    undealiased grids, odd and even N."""
+    R = oracle.ref()
+    if R is None:
+        pytest.skip("reference build absent")
+    rng = np.random.default_rng(Nx * 100 + Nz)
+    Ny, Lx, Lz = 5, 4.0, 3.0
+    al, be = 1.5 - 0.5j, 0.25 + 2j
+    for dkbx, dkex, dkbz, dkez in ((0, dNx, 0, dNz), (1, dNx - 2, 2, dNz)):
+        shape = (dkez - dkbz, dkex - dkbx, Ny)
+        for dx, dz in ((0, 0), (1, 0), (0, 2), (1, 1), (3, 2)):
+            args = (Lx, Lz, Nx, dNx, dkbx, dkex, Nz, dNz, dkbz, dkez)
+            x = rng.normal(size=shape) + 1j * rng.normal(size=shape)
+            g = x.copy()
+            R.suzerain_diffwave_apply(dx, dz, oracle._z(al), g.ctypes.data, Lx, Lz, Ny, Nx,
+                                      dNx, dkbx, dkex, Nz, dNz, dkbz, dkez)
+            want = oracle.diffwave_apply(dx, dz, al, x, *args)
+            assert np.allclose(g, want, rtol=1e-14, atol=1e-13), (dx, dz)
+            assert np.array_equal(g == 0, want == 0)
+            y0 = rng.normal(size=shape) + 1j * rng.normal(size=shape)
+            y = y0.copy()
+            R.suzerain_diffwave_accumulate(dx, dz, oracle._z(al), x.ctypes.data, oracle._z(be),
+                                           y.ctypes.data, Lx, Lz, Ny, Nx, dNx, dkbx, dkex, Nz,
+                                           dNz, dkbz, dkez)
+            want = oracle.diffwave_accumulate(dx, dz, al, x, be, y0, *args)
+            assert np.allclose(y, want, rtol=1e-14, atol=1e-13), (dx, dz)
+
+
 # --------------------------------------------------------------------------
 # zgbsvx: the restatement against LAPACK's own zgbsvx (SciPy's OpenBLAS, the
 # routine suzerain_lapack_zgbsvx forwards to)
