@@ -230,3 +230,37 @@ def test_bsmbsm_permutation_layout(native):
         [native.suzerain_bsmbsm_q(5, 12, i) for i in range(60)]
     native.sgb_permutation_free(p)
     assert not native.suzerain_bsmbsm_permutation(0, 12)
+
+
+def test_factor_shape_table(native):
+    """The process-wide shape table of the blocked factor (host logic, no
+    GPU): built-in defaults per precision, recorded shapes per (precision,
+    N, KL, KU), the supported-shape rule (nb 4/8/16, nw 1/2/4, KL within the
+    per-warp-count bound, lookahead as nw < 0), and the tuner's probe leaves
+    the table as it found it."""
+    from suzerain_gb300 import tune
+
+    def get(prec, N, KL, KU):
+        return tune.get_shape(prec, N, KL, KU)
+
+    N, KL, KU = 960, 34, 34
+    assert get("C", N, KL, KU) == (4, 2)          # measured defaults at this geometry
+    assert get("Z", N, KL, KU) == (4, 1)
+    assert get("C", 500, 60, 60)[1] == 4          # KL > 56 needs four warps
+    geo = (731, 21, 17)                           # a geometry no other test records
+    for nb, nw in ((8, 4), (16, 2), (4, -2), (8, -4), (4, 1)):
+        tune.set_shape("C", *geo, nb, nw)
+        assert get("C", *geo) == (nb, nw)
+    assert get("Z", *geo) == (4, 1)               # keyed by precision
+    L = native
+    for bad in ((3, 2), (8, 3), (4, -1), (32, 2), (4, 0)):
+        assert L.sgb_gbtrf_set_shape(b"C", *geo, *bad) != 0, bad
+    assert L.sgb_gbtrf_set_shape(b"X", *geo, 4, 2) != 0
+    assert get("C", *geo) == (4, 1)               # rejected calls change nothing
+    for nw, kmax in ((1, 52), (2, 56), (4, 63)):   # KL + 1 <= 64 overall
+        assert L.sgb_gbtrf_set_shape(b"Z", 400, kmax, 10, 4, nw) == 0
+        assert L.sgb_gbtrf_set_shape(b"Z", 400, kmax + 1, 10, 4, nw) != 0
+    before = get("C", *geo)
+    assert tune._supported(L, b"C", *geo, 16, 4) is True
+    assert tune._supported(L, b"C", *geo, 3, 4) is False
+    assert get("C", *geo) == before
