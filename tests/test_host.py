@@ -264,3 +264,27 @@ def test_factor_shape_table(native):
     assert tune._supported(L, b"C", *geo, 16, 4) is True
     assert tune._supported(L, b"C", *geo, 3, 4) is False
     assert get("C", *geo) == before
+
+
+def test_configuration_geometries():
+    """Configurations 1/2 (and the stiff variant) are 129 x 192 = 24,768
+    systems of N = 960; configuration 3 draws 64 cases from the stated sets
+    (Ny in {32, 48, ..., 256}, k in {6, 8}, S in {5, 7}, (Nx, Nz) in
+    {(32, 32), (64, 48), (128, 96)}), deterministically: 172,160 systems over
+    44 (S, Ny, k) geometries, each case contributing (Nx/2 + 1) Nz systems."""
+    from suzerain_gb300 import synth
+    for key in (1, 2, "2stiff"):
+        c = synth.CONFIGS[key]
+        assert (c.S, c.Ny, c.k, c.nsys) == (5, 192, 8, 24768)
+    assert synth.CONFIGS["2stiff"].phi == 5e-2
+    cases = synth.config3_cases()
+    again = synth.config3_cases()
+    assert [(c.S, c.Ny, c.k, c.Nx, c.Nz) for c in cases] == \
+        [(c.S, c.Ny, c.k, c.Nx, c.Nz) for c in again]
+    assert len(cases) == 64
+    assert sum(c.nsys for c in cases) == 172160
+    assert len({(c.S, c.Ny, c.k) for c in cases}) == 44
+    for c in cases:
+        assert c.Ny in range(32, 257, 16) and c.k in (6, 8) and c.S in (5, 7)
+        assert (c.Nx, c.Nz) in ((32, 32), (64, 48), (128, 96))
+        assert c.nsys == (c.Nx // 2 + 1) * c.Nz
