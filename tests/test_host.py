@@ -288,3 +288,64 @@ def test_configuration_geometries():
         assert c.Ny in range(32, 257, 16) and c.k in (6, 8) and c.S in (5, 7)
         assert (c.Nx, c.Nz) in ((32, 32), (64, 48), (128, 96))
         assert c.nsys == (c.Nx // 2 + 1) * c.Nz
+
+
+C_CALLER = r"""
+#include <stdio.h>
+#include <string.h>
+#include "suzerain_gb300.h"
+
+int main(void)
+{
+    suzerain_bsmbsm A = suzerain_bsmbsm_construct(5, 192, 6, 6);
+    sgb_solver_spec s;
+    char err[256], buf[256];
+    int nb = 0, nw = 0;
+    double xv[20] = {0}, yv[20] = {0};
+    printf("geom %d %d %d %d\n", A.N, A.KL, A.KU, A.LD);
+    printf("q %d %d\n", suzerain_bsmbsm_q(5, 192, 7), suzerain_bsmbsm_qinv(5, 192, 193));
+    printf("wn %d %d\n", suzerain_inorder_wavenumber(24, 13), suzerain_inorder_wavenumber(24, 12));
+    if (sgb_solver_spec_parse("zcgbsvx,aiter=5,siter=25,diter=5,tolsc=145", &s, err, sizeof err))
+        return 1;
+    sgb_solver_spec_format(&s, buf, sizeof buf);
+    printf("spec %s\n", buf);
+    printf("bad %d\n", sgb_solver_spec_parse("zcgbsvx,bogus=1", &s, err, sizeof err));
+    sgb_gbtrf_get_shape('C', 960, 34, 34, &nb, &nw);
+    printf("shape %d %d\n", nb, nw);
+    printf("args %d %d %d\n", suzerain_bsmbsm_daPxpby('X', 5, 4, 1.0, xv, 1, 0.0, yv, 1),
+           suzerain_bsmbsm_daPxpby('N', 5, 4, 1.0, xv, 1, 0.0, xv, 1),
+           suzerain_bsmbsm_zpack(5, 4, 5, 0, 1, 1, 1.0 + 0.5 * I, 0, 3, 9, 9, 0, 19));
+    return 0;
+}
+"""
+
+
+def test_c99_caller_links_and_calls_the_library(native, tmp_path):
+    """A C99 translation unit includes the public header, links the library
+    by its C names and calls host-side entry points (geometry, q, wavenumbers,
+    the specification grammar, the shape table, argument errors): the
+    boundary is a C ABI that the reference's C code can call unchanged."""
+    import shutil
+    import subprocess
+    from suzerain_gb300 import build as B
+    if not shutil.which("gcc"):
+        pytest.skip("gcc absent")
+    src = tmp_path / "caller.c"
+    src.write_text(C_CALLER)
+    exe = tmp_path / "caller"
+    libdir = os.path.dirname(B.LIB)
+    cmd = ["gcc", "-std=c99", "-Wall", "-Wextra", "-Werror", "-pedantic",
+           "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe),
+           "-L", libdir, "-l:" + os.path.basename(B.LIB), "-Wl,-rpath," + libdir]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    out = dict(line.split(" ", 1) for line in r.stdout.strip().splitlines())
+    assert out["geom"] == "960 34 34 69"
+    assert out["q"] == f"{(7 % 5) * 192 + 7 // 5} {(193 % 192) * 5 + 193 // 192}"
+    assert out["wn"] == "-11 12"
+    assert out["spec"] == "zcgbsvx,reuse=false,aiter=5,siter=25,diter=5,tolsc=145"
+    assert out["bad"] == "-1"
+    assert out["shape"] == "4 2"
+    assert out["args"] == "1 58 3"          # suzerain/bsmbsm_aPxpby_real.def:47-56, bsmbsm_pack.def:43-64
