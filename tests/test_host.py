@@ -349,3 +349,25 @@ def test_c99_caller_links_and_calls_the_library(native, tmp_path):
     assert out["bad"] == "-1"
     assert out["shape"] == "4 2"
     assert out["args"] == "1 58 3"          # suzerain/bsmbsm_aPxpby_real.def:47-56, bsmbsm_pack.def:43-64
+
+
+def test_reference_arm_prints_one_contract_line(native, oracle):
+    """bench.py --impl reference (the reference algorithm on the host cores)
+    prints one JSON line with the contract's keys, on a small sample."""
+    import subprocess
+    import sys
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
+                        "--steps", "1", "--warmup", "0", "--ref-sample", "32"],
+                       capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.strip().startswith("{")]
+    assert len(lines) == 1, r.stdout
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["unit"] == "systems/s" and d["value"] > 0
+    assert d["higher_is_better"] is True and d["steps"] == 1
+    for k in ("metric", "n_gpus", "warmup", "ms_per_step", "scaling", "dtype", "data", "config"):
+        assert k in d, k
+    cb = d["cpu_baseline"]
+    assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["value"] == d["value"]
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}
