@@ -371,3 +371,28 @@ def test_reference_arm_prints_one_contract_line(native, oracle):
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["value"] == d["value"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}
+
+
+def test_plan_memory_estimate(native):
+    """sgb_plan_estimate_bytes (host-only; serving admits cases with it) is
+    linear in the number of systems, covers both methods when asked for
+    both, and bounds the device memory that plans of the benchmark geometry
+    actually held on a GB300 from above, by less than 1 KB per plan
+    (allocations round up to 256 bytes): 2,144,368,304 bytes for one
+    2,048-system plan with 256 complex128 slots, 24,270,595,776 bytes for
+    four 6,192-system plans with 512 slots each (method 'M')."""
+    from suzerain_gb300 import plan as P, synth
+    cs = synth.CONFIGS[2].batch()[0]
+    est = P.Plan.estimate_bytes
+    for m in ("M", "Z"):
+        d1 = est(cs, 2000, 100, m) - est(cs, 1000, 100, m)
+        d2 = est(cs, 3000, 100, m) - est(cs, 2000, 100, m)
+        assert d1 > 0 and abs(d1 - d2) <= 4096
+    assert est(cs, 1000, 1000, "M") > est(cs, 1000, 100, "M")     # complex128 slots
+    assert est(cs, 1000, 100, "Z") > est(cs, 1000, 100, "M")      # complex64 factors
+    fac_c64 = 8 * native.sgb_factor_elems(cs.N, cs.KL, cs.KU)
+    assert est(cs, 1000, 1, "M") > 1000 * fac_c64
+    one = est(cs, 2048, 256, "M")
+    assert 2_144_368_304 <= one <= 2_144_368_304 + 1024
+    four = 4 * est(cs, 6192, 512, "M")
+    assert 24_270_595_776 <= four <= 24_270_595_776 + 4 * 1024
