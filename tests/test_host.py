@@ -396,3 +396,19 @@ def test_plan_memory_estimate(native):
     assert 2_144_368_304 <= one <= 2_144_368_304 + 1024
     four = 4 * est(cs, 6192, 512, "M")
     assert 24_270_595_776 <= four <= 24_270_595_776 + 4 * 1024
+
+
+def test_htstretch2_matches_reference_formula(native):
+    """suzerain_htstretch2(delta, L, x) = (1 + tanh(delta (x/L - 1/2)) /
+    tanh(delta/2)) / 2, and x/L for delta = 0 (suzerain/htstretch.c:112-125):
+    the stretching of the breakpoints toward both walls."""
+    import math
+    for delta in (0.0, 0.5, 2.0, 7.0):
+        for L in (1.0, 2.0):
+            for x in np.linspace(0.0, L, 11):
+                got = native.suzerain_htstretch2(delta, L, float(x))
+                want = x / L if delta == 0 else \
+                    0.5 * (1 + math.tanh(delta * (x / L - 0.5)) / math.tanh(delta / 2.0))
+                assert abs(got - want) <= 2e-16 * max(1.0, abs(want)), (delta, L, x)
+    assert native.suzerain_htstretch2(2.0, 1.0, 0.0) == 0.0
+    assert native.suzerain_htstretch2(2.0, 1.0, 1.0) == 1.0
