@@ -415,3 +415,17 @@ def test_zgbsvx_fact_f_and_singular(oracle):
     assert got["info"] == want["info"] == 5
     assert_close(got, want, 10, 2, 2, "singular")
     assert not got["x"].any()
+
+
+def test_inorder_wavenumber_matches_reference(oracle, native):
+    """The library's suzerain_inorder_wavenumber equals the reference's own
+    (suzerain/inorder.h:92-96, extern definition in suzerain/inorder.c) for
+    every index of even and odd N."""
+    R = oracle.ref()
+    if R is None:
+        pytest.skip("reference build absent")
+    R.suzerain_inorder_wavenumber.argtypes = [C.c_int, C.c_int]
+    R.suzerain_inorder_wavenumber.restype = C.c_int
+    for N in (1, 2, 3, 8, 13, 24, 192, 257):
+        for i in range(N):
+            assert native.suzerain_inorder_wavenumber(N, i) == R.suzerain_inorder_wavenumber(N, i)
