@@ -5,7 +5,8 @@ event completes when the work recorded before it on its stream has run; a
 plan's substep advances the case's state), so that admission in arrival
 order, the HBM budget, overlap of resident cases, the alternating state
 buffers, plan release and latency accounting are checked on CPU, as are
-BatchPlan's row partition and stream fork/join.  The GPU counterpart
+BatchPlan's row partition and stream fork/join and MultiCase's SMR91
+substep coefficients, stream assignment and state ping-pong.  The GPU counterpart
 (test_serving_result_same_alone_and_in_the_mix) checks that each case's
 result is the same alone and in the mix."""
 import dataclasses
@@ -268,3 +269,95 @@ def test_batch_plan_parts_partition_rows_and_join_streams(monkeypatch):
 
     bp = P.BatchPlan(case, kx[:3], kz[:3], parts=8)       # more parts than systems
     assert bp.bounds == [0, 1, 2, 3]
+
+
+def test_multicase_step_scales_smr91_substeps_and_ping_pongs(monkeypatch):
+    """MultiCase.step_eager issues every case's three SMR91 substeps in order
+    on its stream (cases round-robin over the streams, forked from and joined
+    into the caller's stream), with phi_explicit = dt alpha_i and
+    phi_implicit = -dt beta_i for dt = phi / beta_0 (alpha = 29/96, -3/40,
+    1/6; beta = 37/160, 5/24, 1/6; suzerain/lowstorage.hpp:1286-1304), and
+    ping-pongs the state: substep j reads buffer j % 2 and writes the other,
+    so the result after three substeps is buffer 1.  Cases are grouped by
+    (N, KL, KU) for the tuner."""
+    from suzerain_gb300 import multicase as MC
+    events = []
+
+    class Stream:
+        n = 0
+
+        def __init__(self):
+            Stream.n += 1
+            self.cuda_stream = Stream.n
+
+        def wait_stream(self, other):
+            events.append(("wait", self.cuda_stream, other.cuda_stream))
+
+    caller = Stream()
+
+    class Ctx:
+        def __init__(self, st):
+            self.st = st
+
+        def __enter__(self):
+            return self.st
+
+        def __exit__(self, *a):
+            return False
+
+    class T:
+        def __init__(self, a):
+            self.a = a
+
+        def cuda(self):
+            return T(self.a.copy())
+
+        def clone(self):
+            return T(self.a.copy())
+
+    cuda = types.SimpleNamespace(Stream=Stream, current_stream=lambda: caller, stream=Ctx)
+    monkeypatch.setitem(sys.modules, "torch", types.SimpleNamespace(
+        cuda=cuda, from_numpy=lambda a: T(np.asarray(a)),
+        empty_like=lambda t: T(np.zeros_like(t.a))))
+
+    class Plan:
+        def __init__(self, cs, kx, kz, max_double_slots=0):
+            self.cs, self.nsys = cs, len(kx)
+
+        def substep(self, method, pe, pi, a, b, spec, stream=0):
+            b.a[...] = a.a + 1
+            events.append(("substep", self.cs.rid, stream, pe, pi, id(a), id(b)))
+
+    monkeypatch.setattr(MC.P, "Plan", Plan)
+    monkeypatch.setattr(MC.synth, "zero_dirichlet_rows", lambda cs, u: u)
+
+    @dataclasses.dataclass
+    class Cfg:
+        rid: int
+        N: int
+        phi: float
+
+        def batch(self, complex_coupling=False):
+            cs = types.SimpleNamespace(rid=self.rid, N=self.N, KL=34, KU=34)
+            return cs, np.zeros(4), np.zeros(4), np.full((4, self.N), float(self.rid))
+
+    cfgs = [Cfg(0, 960, 1e-3), Cfg(1, 480, 2e-3), Cfg(2, 960, 1e-3)]
+    mc = MC.MultiCase(cfgs, nstreams=2)
+    assert mc.geometries() == {(960, 34, 34): [0, 2], (480, 34, 34): [1]}
+    events.clear()
+    mc.step_eager("M")
+    part = [s.cuda_stream for s in mc.streams]
+    assert events[:2] == [("wait", s, caller.cuda_stream) for s in part]
+    assert events[-2:] == [("wait", caller.cuda_stream, s) for s in part]
+    subs = [e for e in events if e[0] == "substep"]
+    alpha, beta = (29 / 96, -3 / 40, 1 / 6), (37 / 160, 5 / 24, 1 / 6)
+    for ci, cfg in enumerate(cfgs):
+        mine = [e for e in subs if e[1] == ci]
+        assert len(mine) == 3 and all(e[2] == part[ci % 2] for e in mine)
+        dt = cfg.phi / beta[0]
+        for i, e in enumerate(mine):
+            assert np.isclose(e[3], dt * alpha[i], rtol=1e-15)
+            assert np.isclose(e[4], -dt * beta[i], rtol=1e-15)
+        b0, b1 = (id(x) for x in mc.bufs[ci])
+        assert [(e[5], e[6]) for e in mine] == [(b0, b1), (b1, b0), (b0, b1)]
+        np.testing.assert_array_equal(mc.result(ci).a, ci + 3)
