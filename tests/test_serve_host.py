@@ -361,3 +361,32 @@ def test_multicase_step_scales_smr91_substeps_and_ping_pongs(monkeypatch):
         b0, b1 = (id(x) for x in mc.bufs[ci])
         assert [(e[5], e[6]) for e in mine] == [(b0, b1), (b1, b0), (b0, b1)]
         np.testing.assert_array_equal(mc.result(ci).a, ci + 3)
+
+
+def test_poisson_trace_matches_configuration_4():
+    """Configuration 4's request stream: exponential inter-arrival times of
+    mean 1/rate (arrivals increasing), case shapes drawn from configuration
+    3's distribution (its own seeded set of cases unless a pool is given), lifetimes uniform on 3..30 substeps, each request its own
+    seeded state, the same trace for the same seed."""
+    from suzerain_gb300 import synth
+    pool = synth.config3_cases()
+    tr = serve.poisson_trace(4000, rate=100.0, seed=11)
+    t = np.array([r.t_arrival for r in tr])
+    assert (np.diff(t) > 0).all() and t[0] > 0
+    gaps = np.diff(np.concatenate([[0.0], t]))
+    assert abs(gaps.mean() - 0.01) < 0.001 and abs(gaps.std() - 0.01) < 0.0015
+    lives = np.array([r.nsubsteps for r in tr])
+    assert lives.min() == 3 and lives.max() == 30
+    assert abs(lives.mean() - 16.5) < 0.6
+    for r in tr:
+        c = r.config
+        assert c.Ny in range(32, 257, 16) and c.k in (6, 8) and c.S in (5, 7)
+        assert (c.Nx, c.Nz) in ((32, 32), (64, 48), (128, 96))
+    assert len({r.config.seed for r in tr}) == len(tr)
+    assert [r.rid for r in tr] == list(range(len(tr)))
+    again = serve.poisson_trace(4000, rate=100.0, seed=11)
+    assert [(r.t_arrival, r.nsubsteps, r.config.Ny) for r in again] == \
+        [(r.t_arrival, r.nsubsteps, r.config.Ny) for r in tr]
+    short = serve.poisson_trace(50, rate=10.0, seed=3, configs=pool[:2], life=(4, 4))
+    assert {r.nsubsteps for r in short} == {4}
+    assert {r.config.Ny for r in short} <= {pool[0].Ny, pool[1].Ny}
