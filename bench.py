@@ -128,65 +128,243 @@ class ClockSampler:
 
 
 def cpu_baseline(cfg, cs, kx, kz, u, phi_e, phi_i, nsample: int, nthreads: int,
-                 mixed: bool = True):
-    """The reference algorithm on host threads over a bounded sample."""
+                 mixed: bool = True, idx=None):
+    """The reference algorithm on host threads over a bounded sample (evenly
+    spaced systems of the batch, or the given indices).  Returns the
+    baseline record and the oracle's per-system results."""
     from oracle import oracle as O
-    import numpy as np
-    idx = np.linspace(0, len(kx) - 1, nsample).astype(int)
+    if idx is None:
+        idx = np.linspace(0, len(kx) - 1, nsample).round().astype(int)
+    nsample = len(idx)
     ob = O.openblas_path() is not None
     r = O.batch_solve(cs, kx[idx], kz[idx], u[idx], phi_exp=phi_e, phi_imp=phi_i, mixed=mixed,
                       aiter=SPEC["aiter"], siter=SPEC["siter"], diter=SPEC["diter"],
                       tolsc=SPEC["tolsc"], nthreads=nthreads, openblas=ob)
     lat = r["latency"]
-    return dict(value=nsample / r["wall"], unit=UNIT, cores=nthreads, kind="port",
-                sample=(f"{nsample} of {len(kx)} systems of the same batch, evenly spaced; "
-                        f"{'zcgbsvx' if mixed else 'zgbsv'} driver restated in C over "
-                        f"{'SciPy OpenBLAS' if ob else 'restated zgbtf2'} LAPACK, one system "
-                        f"per thread, {nthreads} threads"),
-                p50_ms=float(np.percentile(lat, 50) * 1e3),
-                p99_ms=float(np.percentile(lat, 99) * 1e3),
-                wall_s=r["wall"], info_nonzero=int((r["info"] != 0).sum()))
+    rec = dict(value=nsample / r["wall"], unit=UNIT, cores=nthreads, kind="port",
+               sample=(f"{nsample} of {len(kx)} systems of the same batch, evenly spaced; "
+                       f"{'zcgbsvx' if mixed else 'zgbsv'} driver restated in C over "
+                       f"{'SciPy OpenBLAS' if ob else 'restated zgbtf2'} LAPACK, one system "
+                       f"per thread, {nthreads} threads"),
+               p50_ms=float(np.percentile(lat, 50) * 1e3),
+               p99_ms=float(np.percentile(lat, 99) * 1e3),
+               wall_s=r["wall"], info_nonzero=int((r["info"] != 0).sum()))
+    if mixed:
+        rec["fact_double"] = r["fact"].count("D")
+        rec["siter_mean"] = float(r["siter"].mean())
+    return rec, r, idx
+
+
+EDGES = [0.0] + [10.0 ** e for e in range(-17, -5)] + [float("inf")]
+EDGE_NAMES = ["0"] + [f"1e{e}" for e in range(-17, -5)] + ["inf"]
+
+
+def rel_err_hist(x, ref) -> dict:
+    """Per-system ||x - ref||_inf / ||ref||_inf as a histogram over decades."""
+    err = np.max(np.abs(x - ref), axis=1) / np.max(np.abs(ref), axis=1)
+    counts = [int(((err >= lo) & (err < hi)).sum()) for lo, hi in zip(EDGES[:-1], EDGES[1:])]
+    return {"systems": int(len(err)), "max": float(err.max()), "median": float(np.median(err)),
+            "edges": EDGE_NAMES, "counts": counts}
+
+
+def oracle_parity(cs, kx, kz, u, phi_e, phi_i, idx, x_mixed, x_plain, fact_gpu, nthreads,
+                  mixed_ref=None) -> dict:
+    """GPU results against the FP64 oracle (the zgbsv restatement pinned to
+    the reference build) on the same systems: per-system forward error of
+    the mixed and complex128 solutions, and the mixed path's complex128
+    decisions against the oracle's zcgbsvx."""
+    from oracle import oracle as O
+    ob = O.openblas_path() is not None
+    o = O.batch_solve(cs, kx[idx], kz[idx], u[idx], phi_exp=phi_e, phi_imp=phi_i,
+                      nthreads=nthreads, openblas=ob)
+    out = {"oracle": f"zgbsv restated in C over {'SciPy OpenBLAS' if ob else 'restated zgbtf2'}",
+           "mixed_vs_fp64_oracle": rel_err_hist(x_mixed, o["x"])}
+    if x_plain is not None:
+        out["plain_vs_fp64_oracle"] = rel_err_hist(x_plain, o["x"])
+    if mixed_ref is not None:
+        f_o = mixed_ref["fact"]
+        out["fact_agree"] = float(np.mean([a == b for a, b in zip(fact_gpu, f_o)]))
+        out["fact_double_gpu"] = fact_gpu.count("D")
+        out["fact_double_oracle"] = f_o.count("D")
+    return out
 
 
 def run_reference(args):
+    """The reference algorithm (the oracle's C restatement of the bsmbsm +
+    zcgbsvx driver over SciPy's OpenBLAS) on the host cores, over the whole
+    batch by default, with inputs from the host-only generator: this process
+    never loads the GPU library."""
     rank, local, world = dist_env()
     if rank != 0:
         return 0
-    from suzerain_gb300 import synth
     from oracle import oracle as O
     O.build()
-    from suzerain_gb300 import build as B
-    B.build()
+    from suzerain_gb300 import _native as nat
+    nat.bind_generator(O.SYNTH_PATH)
+    from suzerain_gb300 import synth
     cfg = synth.CONFIGS[args.config]
     cs, kx, kz, u = cfg.batch()
     phi_e, phi_i = synth.smr91_phis(cfg.phi)
     nthreads = os.cpu_count() or 1
-    nsample = args.ref_sample
+    nsample = args.ref_sample if args.ref_sample > 0 else len(kx)
     times = []
+    r = None
     for step in range(args.warmup + args.steps):
-        r = cpu_baseline(cfg, cs, kx, kz, u, phi_e, phi_i, nsample, nthreads)
+        r, _, _ = cpu_baseline(cfg, cs, kx, kz, u, phi_e, phi_i, nsample, nthreads)
         if step >= args.warmup:
             times.append(nsample / r["value"])
     t = sum(times)
     value = nsample * args.steps / t
+    same = nsample == len(kx)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64+f64",
         "data": "synthetic (seeded generator of the reference's shapes)",
-        "config": {"workload": f"SMR91 substep, config {args.config}: S=5 Ny=192 k=8 N=960 KL=KU=34, "
-                               f"{nsample}-system sample of the {cfg.nsys}-system batch per step",
-                   "global_batch": nsample, "seq_len": cs.N, "parallelism": "host threads"},
+        "config": {"workload": workload_name(args.config, cfg, cs,
+                                             len(kx) if same else nsample, len(kx)),
+                   "operator": synth.describe_operator(cfg),
+                   "global_batch": nsample, "seq_len": cs.N, "parallelism": "host threads",
+                   "same_config": same},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
-                         "sample": r["sample"]},
+                         "sample": r["sample"], "p50_ms": r["p50_ms"], "p99_ms": r["p99_ms"]},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "native_libraries": loaded_libraries(),
     }
     print(json.dumps(line))
     return 0
 
 
+def loaded_libraries() -> list:
+    """The repository's shared libraries mapped into this process."""
+    out = set()
+    try:
+        with open("/proc/self/maps") as f:
+            for ln in f:
+                path = ln.split()[-1] if ln.strip() else ""
+                if path.startswith(ROOT) and path.endswith(".so"):
+                    out.add(os.path.relpath(path, ROOT))
+    except OSError:
+        pass
+    return sorted(out)
+
+
+def workload_name(config, cfg, cs, nsys, nbatch) -> str:
+    return (f"SMR91 substep, configuration {config}: S={cs.S} Ny={cs.n} k={cfg.k} N={cs.N} "
+            f"KL=KU={cs.KL}, {nsys} of {nbatch} systems per step")
+
+
+def timed(fn, steps: int, stream) -> float:
+    """ms for `steps` calls of fn, CUDA events on stream, synchronized both sides."""
+    import torch
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def run_variant(key, args, nthreads) -> dict:
+    """A bounded run of another operator of the production shape (the
+    literal wall mask or the stiff variant): mixed and complex128
+    systems/s over the whole batch, decisions, backward error, forward
+    error against the FP64 oracle and the host-core reference on a sample."""
+    import torch
+    from suzerain_gb300 import plan as P, synth
+    cfg = synth.CONFIGS[key]
+    cs, kx, kz, u = cfg.batch()
+    nsys = len(kx)
+    phi_e, phi_i = synth.smr91_phis(cfg.phi)
+    spec = P.RefineSpec(**SPEC)
+    stream = torch.cuda.current_stream()
+    du = torch.from_numpy(u).cuda()
+    dout = torch.empty_like(du)
+    # every system may fall back to complex128 (the literal mask sends most)
+    bp = P.BatchPlan(cs, kx, kz, parts=args.parts, max_double_slots=nsys, method="M")
+    bp.substep("M", phi_e, phi_i, du, dout, spec)
+    ms = timed(lambda: bp.substep("M", phi_e, phi_i, du, dout, spec), args.variant_steps, stream)
+    rep = bp.report()
+    berr = bp.backward_error()
+    unserved = bp.unserved()
+    x_mixed = dout.cpu().numpy()
+    bp.close()
+    bz = P.BatchPlan(cs, kx, kz, parts=args.parts, method="Z")
+    bz.substep("Z", phi_e, phi_i, du, dout, spec)
+    zms = timed(lambda: bz.substep("Z", phi_e, phi_i, du, dout, spec), 1, stream)
+    zberr = bz.backward_error()
+    x_plain = dout.cpu().numpy()
+    bz.close()
+    del du, dout
+    torch.cuda.empty_cache()
+    cpu, om, idx = cpu_baseline(cfg, cs, kx, kz, u, phi_e, phi_i, args.variant_sample, nthreads)
+    par = oracle_parity(cs, kx, kz, u, phi_e, phi_i, idx, x_mixed[idx], x_plain[idx],
+                        "".join(rep["fact"][i] for i in idx), nthreads, mixed_ref=om)
+    return {
+        "workload": workload_name(key, cfg, cs, nsys, nsys),
+        "operator": synth.describe_operator(cfg),
+        "value": nsys * args.variant_steps / (ms / 1e3), "unit": UNIT,
+        "ms_per_step": ms / args.variant_steps, "steps": args.variant_steps,
+        "rel_resid_max": float(berr.max()), "fact_double": rep["fact"].count("D"),
+        "siter_mean": float(rep["siter"].mean()), "siter_max": int(rep["siter"].max()),
+        "unserved": int(unserved),
+        "plain_c128": {"value": nsys / (zms / 1e3), "ms_per_step": zms,
+                       "rel_resid_max": float(zberr.max())},
+        "parity": par, "cpu_baseline": cpu,
+    }
+
+
+def run_packed(cfg, cs, kx, kz, u, phi_i, args, peak) -> dict:
+    """The caller-packed form: every system's P A P^T as a packed complex128
+    band in HBM (packc, LD x N), solved by sgb_zcgbsvx_batched, the
+    batched counterpart of bsmbsm_solver_zcgbsvx's solve
+    (suzerain/bsmbsm_solver.cpp:377-414).  Here the algorithmic bytes
+    16 N (LD + 2) per system are what the kernels really read."""
+    import ctypes as C
+    import torch
+    from suzerain_gb300 import _native as nat, plan as P
+    L = nat.load()
+    nsys, N = u.shape
+    LD = cs.LD
+    stream = torch.cuda.current_stream()
+    pl = P.Plan(cs, kx, kz)
+    ab = torch.empty((nsys, N * LD), dtype=torch.complex128, device="cuda")
+    pl.assemble_packed(phi_i, ab, LD, 0, stream=stream.cuda_stream)
+    pl.close()
+    q = np.array([(i % cs.S) * cs.n + i // cs.S for i in range(N)])
+    b = torch.from_numpy(u).cuda()[:, torch.from_numpy(q).cuda()].contiguous()
+    x = torch.empty_like(b)
+    rep = {k: torch.zeros(nsys, dtype=t, device="cuda") for k, t in
+           (("info", torch.int32), ("siter", torch.int32), ("diter", torch.int32),
+            ("res", torch.float64), ("tolsc", torch.float64), ("fact", torch.uint8))}
+    R = nat.RefineReport(*(rep[k].data_ptr() for k in ("info", "siter", "diter", "res",
+                                                         "tolsc", "fact")))
+    S = nat.RefineSpec(SPEC["aiter"], SPEC["siter"], SPEC["diter"], SPEC["tolsc"])
+
+    def step():
+        nat.check(L.sgb_zcgbsvx_batched(nsys, N, cs.KL, cs.KU, b"N", ab.data_ptr(), LD,
+                                        LD * N, b.data_ptr(), x.data_ptr(), C.byref(S),
+                                        C.byref(R), stream.cuda_stream), "sgb_zcgbsvx_batched")
+    step()
+    ms = timed(step, args.packed_steps, stream) / args.packed_steps
+    fact = rep["fact"].cpu().numpy().tobytes().decode()
+    tolsc = rep["tolsc"].cpu().numpy()
+    bytes_per_sys = 16 * N * (LD + 2)
+    achieved = nsys * bytes_per_sys / (ms / 1e3) / 1e9
+    del ab, b, x
+    torch.cuda.empty_cache()
+    return {"value": nsys / (ms / 1e3), "unit": UNIT, "ms_per_step": ms,
+            "steps": args.packed_steps,
+            "entry": "sgb_zcgbsvx_batched over packc bands (LD x N complex128 per system)",
+            "band_bytes": int(nsys * LD * N * 16),
+            "fact_double": fact.count("D"), "converged": bool((tolsc <= 1.0).all()),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "note": "whole solve, B_sys = 16 N (LD+2)"}}
+
+
 def run_ours(args):
-    import numpy as np
     import torch
     rank, local, world = dist_env()
     if world > 1:
@@ -199,6 +377,7 @@ def run_ours(args):
     L = nat.load()
     if L.sgb_device_ok() != 0:
         raise RuntimeError(nat.last_error())
+    nthreads = os.cpu_count() or 1
     cfg = synth.CONFIGS[args.config]
     cfg = rank_config(cfg, rank, world)
     cs, kx, kz, u = cfg.batch()
@@ -215,17 +394,11 @@ def run_ours(args):
     # streams (capturable substeps: no host synchronization inside), so that
     # one part's FP64 kernels overlap another's complex64 factor.
     parts = max(1, min(args.parts, nsys))
-    if parts > 1:
-        runner = P.BatchPlan(cs, kx, kz, parts=parts,
-                             max_double_slots=-(-args.double_slots // parts), method=args.method)
+    runner = P.BatchPlan(cs, kx, kz, parts=parts, max_double_slots=args.double_slots,
+                         method=args.method)
 
-        def step():
-            runner.substep(args.method, phi_e, phi_i, du, dout, spec)
-    else:
-        runner = P.Plan(cs, kx, kz, max_double_slots=args.double_slots)
-
-        def step():
-            runner.substep(args.method, phi_e, phi_i, du, dout, spec, stream=sptr)
+    def step():
+        runner.substep(args.method, phi_e, phi_i, du, dout, spec, stream=sptr)
 
     def barrier():
         if world > 1:
@@ -255,20 +428,31 @@ def run_ours(args):
 
     # ---- accuracy of the last step (untimed) ------------------------------
     rep = runner.report()
-    berr = runner.backward_error() if parts > 1 else runner.backward_error(stream=sptr)
-    ok = bool(berr.max() <= 1e-12 and (rep["info"] == 0).all())
-    if parts > 1:
-        ok = ok and runner.unserved() == 0
+    berr = runner.backward_error()
+    ok = bool(berr.max() <= 1e-12 and (rep["info"] == 0).all()) and runner.unserved() == 0
+    x_mixed = dout.cpu().numpy()
     dev_bytes = runner.device_bytes()
-    # phase attribution, end to end and the complex128 pass use one plan
-    if parts > 1:
-        runner.close()
-        plan = P.Plan(cs, kx, kz, max_double_slots=args.double_slots)
-        plan.substep(args.method, phi_e, phi_i, du, dout, spec, stream=sptr)
-    else:
-        plan = runner
 
-    # ---- per-phase attribution (separate pass with events) ----------------
+    # ---- end to end through the public API, host buffers -----------------
+    # every step copies the whole batch in from pinned host memory and the
+    # result out, part by part on the parts' streams (sgb_batch_substep_host)
+    hu = torch.from_numpy(u).pin_memory()
+    ho = torch.empty_like(hu).pin_memory()
+    hun, hon = hu.numpy(), ho.numpy()
+    runner.substep_host(args.method, phi_e, phi_i, hun, hon, spec, stream=sptr)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        runner.substep_host(args.method, phi_e, phi_i, hun, hon, spec, stream=sptr)
+    e2e_s = time.perf_counter() - t0
+    e2e = nsys * args.e2e_steps / e2e_s
+    e2e_same = bool(np.array_equal(hon, x_mixed))
+    runner.close()
+    del hu, ho
+
+    # ---- per-phase attribution (one plan, separate pass with events) ------
+    plan = P.Plan(cs, kx, kz, max_double_slots=args.double_slots)
+    plan.substep(args.method, phi_e, phi_i, du, dout, spec, stream=sptr)
     plan.set_timing(True)
     for _ in range(max(1, min(args.steps, 3))):
         plan.substep(args.method, phi_e, phi_i, du, dout, spec, stream=sptr)
@@ -276,42 +460,21 @@ def run_ours(args):
     phases = plan.timings()
     plan.set_timing(False)
 
-    # ---- end to end through the public API, host buffers -----------------
-    hu = torch.from_numpy(u).pin_memory()
-    ho = torch.empty_like(hu).pin_memory()
-    plan.substep_host(args.method, phi_e, phi_i, hu.numpy(), ho.numpy(), spec, stream=sptr)
-    t0 = time.perf_counter()
-    for _ in range(args.e2e_steps):
-        plan.substep_host(args.method, phi_e, phi_i, hu.numpy(), ho.numpy(), spec, stream=sptr)
-    e2e_s = time.perf_counter() - t0
-    e2e = nsys * args.e2e_steps / e2e_s
-
     # ---- complex128 plain path for the mixed-vs-FP64 ratio ---------------
     fp64 = None
+    x_plain = None
     if args.fp64_steps > 0:
-        plan.substep(args.method, phi_e, phi_i, du, dout, spec, stream=sptr)
-        x_mixed = dout.clone()
         plan.substep("Z", phi_e, phi_i, du, dout, spec, stream=sptr)
-        torch.cuda.synchronize()
-        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        f0.record(stream)
-        for _ in range(args.fp64_steps):
-            plan.substep("Z", phi_e, phi_i, du, dout, spec, stream=sptr)
-        f1.record(stream)
-        torch.cuda.synchronize()
-        fms = f0.elapsed_time(f1) / args.fp64_steps
+        fms = timed(lambda: plan.substep("Z", phi_e, phi_i, du, dout, spec, stream=sptr),
+                    args.fp64_steps, stream) / args.fp64_steps
         berr64 = plan.backward_error(stream=sptr)
-        # per-system error of the mixed solution against the complex128 one
-        # (max-norm relative), as a histogram over decades
-        err = ((x_mixed - dout).abs().amax(dim=1) / dout.abs().amax(dim=1)).cpu().numpy()
-        edges = [0.0] + [10.0 ** e for e in range(-17, -5)] + [float("inf")]
-        counts = [int(((err >= lo) & (err < hi)).sum()) for lo, hi in zip(edges[:-1], edges[1:])]
+        x_plain = dout.cpu().numpy()
         fp64 = {"systems_per_s": nsys / (fms / 1e3), "ms_per_step": fms,
                 "rel_resid_max": float(berr64.max()),
-                "mixed_speedup": (nsys / (ms / args.steps / 1e3)) / (nsys / (fms / 1e3)),
-                "err_vs_fp64_hist": {"edges": ["0"] + [f"1e{e}" for e in range(-17, -5)] + ["inf"],
-                                     "counts": counts, "max": float(err.max()),
-                                     "median": float(np.median(err))}}
+                "mixed_speedup": (nsys / (ms / args.steps / 1e3)) / (nsys / (fms / 1e3))}
+    plan.close()
+    del du, dout
+    torch.cuda.empty_cache()
 
     # ---- roofline of the dominant kernel ----------------------------------
     peak, peak_src = read_peaks()
@@ -334,9 +497,24 @@ def run_ours(args):
     step_ms = ms / args.steps
     whole = nsys * bytes_per_sys / (step_ms / 1e3) / 1e9
 
-    cpu = None
+    cpu = parity = None
     if rank == 0 and not args.no_cpu:
-        cpu = cpu_baseline(cfg, cs, kx, kz, u, phi_e, phi_i, args.cpu_sample, os.cpu_count() or 1)
+        cpu, om, idx = cpu_baseline(cfg, cs, kx, kz, u, phi_e, phi_i, args.cpu_sample, nthreads)
+        parity = oracle_parity(cs, kx, kz, u, phi_e, phi_i, idx, x_mixed[idx],
+                               None if x_plain is None else x_plain[idx],
+                               "".join(rep["fact"][i] for i in idx), nthreads, mixed_ref=om)
+
+    extras = {}
+    if rank == 0 and not args.no_extras:
+        for key in ("2literal", "2stiff"):
+            try:
+                extras[key] = run_variant(key, args, nthreads)
+            except Exception as exc:      # recorded, the headline stands
+                extras[key] = {"error": repr(exc)}
+        try:
+            extras["packed_path"] = run_packed(cfg, cs, kx, kz, u, phi_i, args, peak)
+        except Exception as exc:
+            extras["packed_path"] = {"error": repr(exc)}
 
     if rank == 0:
         line = {
@@ -344,27 +522,33 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "c64 factor + f64 refinement",
             "data": "synthetic (seeded generator of the reference's shapes)",
-            "config": {"workload": f"SMR91 substep, config {args.config}: S=5 Ny=192 k=8 "
-                                   f"N={N} KL=KU={cs.KL}, {nsys} systems per GPU, method "
-                                   f"{args.method}",
+            "config": {"workload": workload_name(args.config, cfg, cs, nsys, nsys)
+                                   + f", method {args.method}",
+                       "operator": synth.describe_operator(cfg),
                        "global_batch": nsys * world, "seq_len": N,
                        "parallelism": f"wavenumber blocks x{world}",
                        "parts": parts,
                        "l2": "inputs larger than L2 (u 380 MB, factors 20 GB)"},
             "rel_resid_max": float(berr.max()), "all_converged": ok,
-            "fact_double": int(sum(1 for f in rep["fact"] if f == "D")),
+            "fact_double": rep["fact"].count("D"),
             "siter_mean": float(rep["siter"].mean()),
             "gpu_launches": int(launches),
             "clocks": clocks,
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(nsys * N * 16),
-                    "d2h_bytes_per_step": int(nsys * N * 16)},
+                    "d2h_bytes_per_step": int(nsys * N * 16), "steps": args.e2e_steps,
+                    "entry": "sgb_batch_substep_host (pinned host buffers, per-part copies "
+                             "overlapped with the other parts' substeps)",
+                    "same_result_as_device_entry": e2e_same},
             "roofline": roof,
             "path_hbm_fraction": {"achieved_GBs": whole, "frac": whole / peak,
                                   "note": "whole substep, algorithmic bytes 16*N*(LD+2) per system"},
             "phases_ms": {k: v[0] / v[1] for k, v in phases.items()},
             "fp64_plain": fp64,
+            "parity": parity,
             "cpu_baseline": cpu,
             "device_bytes": dev_bytes,
+            **extras,
+            "native_libraries": loaded_libraries(),
         }
         print(json.dumps(line))
     if world > 1:
@@ -500,15 +684,22 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--config", default=2, type=lambda s: s if s == "2stiff" else int(s))
+    ap.add_argument("--config", default=2,
+                    type=lambda s: s if s in ("2stiff", "2literal") else int(s))
     ap.add_argument("--method", default="M", choices=["M", "Z"])
     ap.add_argument("--double-slots", type=int, default=2048)
     ap.add_argument("--parts", type=int, default=4,
                     help="resident plans (one stream each) the timed batch is split into")
-    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--fp64-steps", type=int, default=1)
     ap.add_argument("--cpu-sample", type=int, default=4096)
-    ap.add_argument("--ref-sample", type=int, default=4096)
+    ap.add_argument("--ref-sample", type=int, default=0,
+                    help="reference arm: systems per step (0: the whole batch)")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the literal-mask, stiff and packed-band runs")
+    ap.add_argument("--variant-steps", type=int, default=2)
+    ap.add_argument("--variant-sample", type=int, default=1024)
+    ap.add_argument("--packed-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cases", type=int, default=64, help="configuration 3: number of cases")
     ap.add_argument("--requests", type=int, default=40,

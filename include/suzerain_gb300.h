@@ -576,12 +576,12 @@ int sgb_plan_substep(sgb_plan *p, char method, double phi_exp, double phi_imp,
  *  host synchronization, allocation or host-to-device copy.  Call
  *  sgb_plan_substep once with the same method first (it allocates the
  *  workspace; sgb_plan_prepare does the allocation alone).  Method 'M' runs
- *  min(siter + 1, 4) complex64 correction solves
- *  whose grids are bounded by device-side counts (exactly the reference's
- *  bound when siter <= 3; with a larger siter, systems still refining after
- *  four solves move to the complex128 fallback as if siter were exhausted),
- *  and one fallback chunk of at most max_double_slots systems with the
- *  reference's diter bound.  sgb_plan_unserved reports, after the work has
+ *  the reference's bounds: up to siter + 1 complex64 correction solves and,
+ *  for systems that leave for complex128, up to diter + 2 corrections;
+ *  every launch of the loop is issued and its grid is bounded by a
+ *  device-side count, so once every system has converged the remaining
+ *  launches exit at once.  The complex128 fallback runs one chunk of at
+ *  most max_double_slots systems.  sgb_plan_unserved reports, after the work has
  *  run, how many fallback systems did not fit the chunk (their solution is
  *  the complex64 one, flagged fact = 'S' with tolsc > 1). */
 int sgb_plan_substep_capturable(sgb_plan *plan, char method, double phi_exp,
@@ -598,6 +598,17 @@ int sgb_plan_substep_host(sgb_plan *p, char method, double phi_exp,
                           void *u_out_host, const sgb_refine_spec *spec,
                           void *stream);
 
+/** The implicit operator M + phi L of every system of the plan, written as
+ *  packed complex128 bands (device memory): A(r, c) at
+ *  ab[s ab_stride + off + KU + r - c + c ldab]; the other rows of each
+ *  column and positions outside the matrix are zero.  off = 0 with
+ *  ldab = KL + KU + 1 is the packc layout that zcgbsvx reads
+ *  (suzerain/bsmbsm.h:543-610), off = KL with ldab = 2 KL + KU + 1 the packf
+ *  layout of zgbsv.  The caller-packed form of the solve then runs through
+ *  sgb_zcgbsvx_batched on these bands. */
+int sgb_plan_assemble_packed(sgb_plan *p, double phi, void *ab, int ldab,
+                             long long ab_stride, int off, void *stream);
+
 /** Copy the last substep's per-system statistics to host arrays (any may be
  *  NULL): info, siter, diter, res (||r||_2), tolsc, fact ('S'/'D'). */
 int sgb_plan_report(const sgb_plan *p, int *info, int *siter, int *diter,
@@ -606,6 +617,44 @@ int sgb_plan_report(const sgb_plan *p, int *info, int *siter, int *diter,
 /** Normwise backward error ||b - A x||_inf / (||A||_inf ||x||_inf + ||b||_inf)
  *  of the last substep for every system, computed in FP64 on the device. */
 int sgb_plan_backward_error(sgb_plan *p, double *berr_host, void *stream);
+
+/** A batch: one case's nsys systems split into `parts` resident plans over
+ *  consecutive rows (sgb_batch_bounds), each substepped on a stream of its
+ *  own that is forked from and joined back into the caller's stream, in the
+ *  capturable form (no host synchronization inside, so the parts overlap on
+ *  the device; the calls record into a CUDA graph being captured on the
+ *  caller's stream).  max_double_slots is the batch's total of complex128
+ *  fallback slots, shared evenly by the parts.  Results equal one plan's
+ *  capturable substep over the whole batch.  No counterpart in the
+ *  reference: its caller loops over wavenumbers one solver at a time
+ *  (apps/perfect/operator_hybrid_isothermal.cpp:612-689). */
+typedef struct sgb_batch sgb_batch;
+/** Row offsets of the parts: bounds[i] = i nsys / parts (integer division),
+ *  parts + 1 entries (parts clamped to nsys); returns the part count. */
+int sgb_batch_bounds(int nsys, int parts, int *bounds);
+sgb_batch *sgb_batch_create(const sgb_case *host_case, int nsys, const double *kx,
+                            const double *kz, int parts, int max_double_slots,
+                            char method);
+int sgb_batch_destroy(sgb_batch *b);
+int sgb_batch_parts(const sgb_batch *b);
+/** The plan of one part (owned by the batch). */
+sgb_plan *sgb_batch_plan(sgb_batch *b, int part);
+size_t sgb_batch_device_bytes(const sgb_batch *b);
+/** sgb_plan_substep over the batch: device buffers nsys x N, natural order. */
+int sgb_batch_substep(sgb_batch *b, char method, double phi_exp, double phi_imp,
+                      const void *u_in, void *u_out, const sgb_refine_spec *spec,
+                      void *stream);
+/** The same from and to HOST buffers (pinned for overlap): each part copies
+ *  its rows in, substeps and copies them out on its own stream, so copies
+ *  of one part overlap the computation of the others; returns when the
+ *  output is in host memory. */
+int sgb_batch_substep_host(sgb_batch *b, char method, double phi_exp, double phi_imp,
+                           const void *u_in_host, void *u_out_host,
+                           const sgb_refine_spec *spec, void *stream);
+int sgb_batch_report(const sgb_batch *b, int *info, int *siter, int *diter,
+                     double *res, double *tolsc, char *fact);
+int sgb_batch_backward_error(sgb_batch *b, double *berr_host, void *stream);
+int sgb_batch_unserved(sgb_batch *b, int *count);
 
 /** Record CUDA events around each phase of later substeps (on the stream
  *  they run in); sgb_plan_timings returns "name total_ms calls" lines. */

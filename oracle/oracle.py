@@ -23,6 +23,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_lib", "liboracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "libsuzref.so")
+# the seeded input generator alone (host C++, no CUDA): lets a CPU-only
+# process make the benchmark inputs without loading the GPU library
+SYNTH_PATH = os.path.join(HERE, "_lib", "libsynth.so")
 
 _i = C.c_int
 _d = C.c_double
@@ -40,12 +43,26 @@ def _z(v) -> _Z:
     return _Z(v.real, v.imag)
 
 
+def reference_dir() -> str | None:
+    """The reference checkout the reference build reads: the environment
+    variable SUZERAIN_REFERENCE_DIR, else the default of the build recipe
+    (oracle/ref/Makefile); None when that directory is absent."""
+    d = os.environ.get("SUZERAIN_REFERENCE_DIR")
+    if not d:
+        r = subprocess.run(["make", "-s", "-C", os.path.join(HERE, "ref"), "print-ref"],
+                           capture_output=True, text=True)
+        d = r.stdout.strip() if r.returncode == 0 else ""
+    return d if d and os.path.isdir(os.path.join(d, "suzerain")) else None
+
+
 def build(quiet: bool = True) -> None:
-    """Compile oracle.c (always) and the reference build (when possible)."""
+    """Compile oracle.c and the host-only generator (always) and the
+    reference build (when the reference checkout is present)."""
     out = subprocess.DEVNULL if quiet else None
     subprocess.run(["make", "-C", HERE], check=True, stdout=out, stderr=out)
-    if os.path.isdir("/root/reference/suzerain"):
-        subprocess.run(["make", "-C", HERE, "ref"], check=True, stdout=out,
+    ref = reference_dir()
+    if ref:
+        subprocess.run(["make", "-C", HERE, "ref", f"REF={ref}"], check=True, stdout=out,
                        stderr=out)
 
 

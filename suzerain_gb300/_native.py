@@ -183,6 +183,18 @@ _SIGS = {
     "sgb_plan_set_timing": (_i, [_p, _i]),
     "sgb_plan_timings": (_i, [_p, C.c_char_p, _i]),
     "sgb_launch_count": (_ll, []),
+    "sgb_plan_assemble_packed": (_i, [_p, _d, _p, _i, _ll, _i, _p]),
+    "sgb_batch_bounds": (_i, [_i, _i, _p]),
+    "sgb_batch_create": (_p, [C.POINTER(Case), _i, _p, _p, _i, _i, C.c_char]),
+    "sgb_batch_destroy": (_i, [_p]),
+    "sgb_batch_parts": (_i, [_p]),
+    "sgb_batch_plan": (_p, [_p, _i]),
+    "sgb_batch_device_bytes": (C.c_size_t, [_p]),
+    "sgb_batch_substep": (_i, [_p, C.c_char, _d, _d, _p, _p, _p, _p]),
+    "sgb_batch_substep_host": (_i, [_p, C.c_char, _d, _d, _p, _p, _p, _p]),
+    "sgb_batch_report": (_i, [_p, _p, _p, _p, _p, _p, _p]),
+    "sgb_batch_backward_error": (_i, [_p, _p, _p]),
+    "sgb_batch_unserved": (_i, [_p, _p]),
     "sgb_synth_case": (_i, [_i, _i, _i, _d, _d, _d, _d, _i, _u64, C.c_uint,
                             _p, _p, _p, _p, _p, _p, _p, _p, _p]),
     "sgb_synth_wavenumbers": (_i, [_i, _i, _d, _d, _p, _p]),
@@ -190,6 +202,27 @@ _SIGS = {
 }
 
 _lib = None
+_generator = None
+_GEN_SIGS = ("sgb_synth_case", "sgb_synth_wavenumbers", "sgb_synth_rhs")
+
+
+def bind_generator(path: str):
+    """Use a host-only build of the seeded input generator (the same C++
+    sources, without the CUDA code) for the sgb_synth_* calls, so that a
+    process that only generates inputs never maps the GPU library."""
+    global _generator
+    G = C.CDLL(path)
+    for name in _GEN_SIGS:
+        f = getattr(G, name)
+        f.restype, f.argtypes = _SIGS[name]
+    _generator = G
+    return G
+
+
+def generator():
+    """The library that serves sgb_synth_*: the bound host-only generator,
+    else the full native library."""
+    return _generator if _generator is not None else load()
 
 
 def library_path() -> str:

@@ -620,7 +620,7 @@ static int plan_alloc_m(sgb_plan *p)
 }
 
 // capturable: no host synchronization, no allocation, no host-to-device copy
-// (the refinement runs its capped, device-counted form), so the call can be
+// (the refinement runs its device-counted form), so the call can be
 // recorded into a CUDA graph after one ordinary call of the same method.
 static int plan_substep(sgb_plan *p, char method, double phi_exp, double phi_imp,
                         const void *u_in, void *u_out, const sgb_refine_spec *spec,
@@ -682,7 +682,7 @@ static int plan_substep(sgb_plan *p, char method, double phi_exp, double phi_imp
         P.timer = capturable ? nullptr : &p->timer;
         if (capturable) {
             P.graph = true;
-            P.graph_siter = P.siter < 0 ? 0 : std::min(P.siter + 1, 4);
+            P.graph_siter = P.siter < 0 ? 0 : P.siter + 1;
             P.graph_diter = P.diter + 2;
         }
         const size_t need = refine_workspace_bytes(P);
@@ -893,5 +893,276 @@ extern "C" int sgb_plan_backward_error(sgb_plan *p, double *berr_host, void *str
     cudaFreeAsync(d, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return sgb_set_error(e, "backward error", __FILE__, __LINE__);
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Batch: one case's systems split into resident parts, each a plan on its
+// own stream.  The parts' substeps overlap on the device (one part's FP64
+// kernels beside another's complex64 factor), and the host-buffer form
+// pipelines each part's copy in, substep and copy out on the part's stream,
+// so that only the first part's copy in and the last part's copy out are
+// not hidden behind computation.
+// ---------------------------------------------------------------------------
+struct sgb_batch {
+    std::vector<sgb_plan *> plans;
+    std::vector<int> bounds;                 // parts + 1 row offsets
+    std::vector<cudaStream_t> streams;
+    std::vector<cudaEvent_t> joins;
+    std::vector<double2 *> stage;            // host form: per-part device staging
+    cudaEvent_t fork = nullptr;
+    int nsys = 0, N = 0;
+    std::mutex mu;
+};
+
+extern "C" int sgb_batch_bounds(int nsys, int parts, int *bounds)
+{
+    if (nsys < 1 || parts < 1 || !bounds) return fail("sgb_batch_bounds: bad arguments");
+    parts = std::min(parts, nsys);
+    for (int i = 0; i <= parts; ++i) bounds[i] = (int) ((long long) i * nsys / parts);
+    return parts;
+}
+
+extern "C" int sgb_batch_destroy(sgb_batch *b)
+{
+    if (!b) return 0;
+    for (cudaStream_t s : b->streams) cudaStreamSynchronize(s);
+    for (sgb_plan *p : b->plans) sgb_plan_destroy(p);
+    if (!b->stage.empty()) {
+        std::lock_guard<std::mutex> lk(g_pool.mu);
+        for (double2 *s : b->stage) if (s) cudaFreeAsync(s, g_pool.st);
+    }
+    for (cudaEvent_t e : b->joins) cudaEventDestroy(e);
+    if (b->fork) cudaEventDestroy(b->fork);
+    for (cudaStream_t s : b->streams) cudaStreamDestroy(s);
+    delete b;
+    return 0;
+}
+
+extern "C" sgb_batch *sgb_batch_create(const sgb_case *hcase, int nsys, const double *kx,
+                                       const double *kz, int parts, int max_double_slots,
+                                       char method)
+{
+    if (!hcase || nsys < 1 || !kx || !kz || parts < 1) {
+        fail("sgb_batch_create: bad arguments");
+        return nullptr;
+    }
+    method = (char) toupper(method);
+    if (method != 'M' && method != 'Z' && method != 0) {
+        fail("sgb_batch_create: method must be 'M', 'Z' or 0");
+        return nullptr;
+    }
+    sgb_batch *b = new (std::nothrow) sgb_batch;
+    if (!b) { fail("sgb_batch_create: out of host memory"); return nullptr; }
+    b->nsys = nsys;
+    b->N = hcase->S * hcase->n;
+    b->bounds.resize((size_t) std::min(parts, nsys) + 1);
+    parts = sgb_batch_bounds(nsys, parts, b->bounds.data());
+    const int slots = max_double_slots > 0 ? (max_double_slots + parts - 1) / parts : 0;
+    for (int i = 0; i < parts; ++i) {
+        const int lo = b->bounds[i], cnt = b->bounds[i + 1] - lo;
+        sgb_plan *p = sgb_plan_create(hcase, cnt, kx + lo, kz + lo, slots);
+        if (!p) { sgb_batch_destroy(b); return nullptr; }
+        b->plans.push_back(p);
+        if (sgb_plan_prepare(p, method) != 0) { sgb_batch_destroy(b); return nullptr; }
+        cudaStream_t s = nullptr;
+        cudaEvent_t e = nullptr;
+        cudaError_t err = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+        if (err == cudaSuccess) b->streams.push_back(s);
+        if (err == cudaSuccess) err = cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+        if (err == cudaSuccess) b->joins.push_back(e);
+        if (err != cudaSuccess) {
+            sgb_set_error(err, "sgb_batch_create(stream)", __FILE__, __LINE__);
+            sgb_batch_destroy(b);
+            return nullptr;
+        }
+    }
+    cudaError_t err = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+    if (err != cudaSuccess) {
+        sgb_set_error(err, "sgb_batch_create(event)", __FILE__, __LINE__);
+        sgb_batch_destroy(b);
+        return nullptr;
+    }
+    return b;
+}
+
+extern "C" int sgb_batch_parts(const sgb_batch *b) { return b ? (int) b->plans.size() : 0; }
+
+extern "C" sgb_plan *sgb_batch_plan(sgb_batch *b, int part)
+{
+    if (!b || part < 0 || part >= (int) b->plans.size()) return nullptr;
+    return b->plans[part];
+}
+
+extern "C" size_t sgb_batch_device_bytes(const sgb_batch *b)
+{
+    if (!b) return 0;
+    size_t t = 0;
+    for (const sgb_plan *p : b->plans) t += p->dev_bytes;
+    for (size_t i = 0; i < b->stage.size(); ++i)
+        if (b->stage[i]) t += (size_t) (b->bounds[i + 1] - b->bounds[i]) * b->N * sizeof(double2);
+    return t;
+}
+
+// Fork every part's stream from st, run body(part, part stream) on each, join
+// them back into st.  The same call sequence records correctly into a CUDA
+// graph being captured on st.
+template <typename Body>
+static int batch_fork_join(sgb_batch *b, cudaStream_t st, Body &&body)
+{
+    SGB_CUDA_TRY(cudaEventRecord(b->fork, st));
+    int rc = 0;
+    const int parts = (int) b->plans.size();
+    for (int i = 0; i < parts; ++i) {
+        cudaStream_t ps = b->streams[i];
+        SGB_CUDA_TRY(cudaStreamWaitEvent(ps, b->fork, 0));
+        if (!rc) rc = body(i, ps);
+        SGB_CUDA_TRY(cudaEventRecord(b->joins[i], ps));
+        SGB_CUDA_TRY(cudaStreamWaitEvent(st, b->joins[i], 0));
+    }
+    return rc;
+}
+
+extern "C" int sgb_batch_substep(sgb_batch *b, char method, double phi_exp, double phi_imp,
+                                 const void *u_in, void *u_out, const sgb_refine_spec *spec,
+                                 void *stream)
+{
+    if (!b || !u_in || !u_out) return fail("sgb_batch_substep: null argument");
+    std::lock_guard<std::mutex> lk(b->mu);
+    const char m = (char) toupper(method);
+    return batch_fork_join(b, (cudaStream_t) stream, [&](int i, cudaStream_t ps) {
+        sgb_plan *p = b->plans[i];
+        const size_t off = (size_t) b->bounds[i] * b->N;
+        std::lock_guard<std::mutex> pk(p->mu);
+        const int rc = plan_substep(p, m, phi_exp, phi_imp,
+                                    reinterpret_cast<const double2 *>(u_in) + off,
+                                    reinterpret_cast<double2 *>(u_out) + off, spec, ps, true);
+        p->note(ps);
+        return rc;
+    });
+}
+
+extern "C" int sgb_batch_substep_host(sgb_batch *b, char method, double phi_exp, double phi_imp,
+                                      const void *u_in_host, void *u_out_host,
+                                      const sgb_refine_spec *spec, void *stream)
+{
+    if (!b || !u_in_host || !u_out_host) return fail("sgb_batch_substep_host: null argument");
+    std::lock_guard<std::mutex> lk(b->mu);
+    const int parts = (int) b->plans.size();
+    if (b->stage.empty()) {
+        b->stage.assign(parts, nullptr);
+        for (int i = 0; i < parts; ++i) {
+            const size_t bytes = (size_t) (b->bounds[i + 1] - b->bounds[i]) * b->N * sizeof(double2);
+            cudaError_t e = g_pool.alloc((void **) &b->stage[i], bytes);
+            if (e != cudaSuccess) return sgb_set_error(e, "sgb_batch_substep_host(staging)", __FILE__, __LINE__);
+        }
+    }
+    const char m = (char) toupper(method);
+    cudaStream_t st = (cudaStream_t) stream;
+    int rc = batch_fork_join(b, st, [&](int i, cudaStream_t ps) {
+        sgb_plan *p = b->plans[i];
+        const size_t off = (size_t) b->bounds[i] * b->N;
+        const size_t bytes = (size_t) (b->bounds[i + 1] - b->bounds[i]) * b->N * sizeof(double2);
+        cudaError_t e = cudaMemcpyAsync(b->stage[i], reinterpret_cast<const double2 *>(u_in_host) + off,
+                                        bytes, cudaMemcpyHostToDevice, ps);
+        if (e != cudaSuccess) return sgb_set_error(e, "sgb_batch_substep_host(copy in)", __FILE__, __LINE__);
+        std::lock_guard<std::mutex> pk(p->mu);
+        int r = plan_substep(p, m, phi_exp, phi_imp, b->stage[i], b->stage[i], spec, ps, true);
+        p->note(ps);
+        if (r) return r;
+        e = cudaMemcpyAsync(reinterpret_cast<double2 *>(u_out_host) + off, b->stage[i], bytes,
+                            cudaMemcpyDeviceToHost, ps);
+        if (e != cudaSuccess) return sgb_set_error(e, "sgb_batch_substep_host(copy out)", __FILE__, __LINE__);
+        return 0;
+    });
+    if (rc) return rc;
+    SGB_CUDA_TRY(cudaStreamSynchronize(st));
+    return 0;
+}
+
+extern "C" int sgb_batch_report(const sgb_batch *b, int *info, int *siter, int *diter,
+                                double *res, double *tolsc, char *fact)
+{
+    if (!b) return fail("sgb_batch_report: null batch");
+    for (size_t i = 0; i < b->plans.size(); ++i) {
+        const int o = b->bounds[i];
+        int rc = sgb_plan_report(b->plans[i], info ? info + o : nullptr, siter ? siter + o : nullptr,
+                                 diter ? diter + o : nullptr, res ? res + o : nullptr,
+                                 tolsc ? tolsc + o : nullptr, fact ? fact + o : nullptr);
+        if (rc) return rc;
+    }
+    return 0;
+}
+
+extern "C" int sgb_batch_backward_error(sgb_batch *b, double *berr_host, void *stream)
+{
+    if (!b || !berr_host) return fail("sgb_batch_backward_error: null argument");
+    for (size_t i = 0; i < b->plans.size(); ++i) {
+        int rc = sgb_plan_backward_error(b->plans[i], berr_host + b->bounds[i], stream);
+        if (rc) return rc;
+    }
+    return 0;
+}
+
+extern "C" int sgb_batch_unserved(sgb_batch *b, int *count)
+{
+    if (!b || !count) return fail("sgb_batch_unserved: null argument");
+    *count = 0;
+    for (sgb_plan *p : b->plans) {
+        int c = 0;
+        int rc = sgb_plan_unserved(p, &c);
+        if (rc) return rc;
+        *count += c;
+    }
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Packed bands of a plan's operator (the caller-packed form of the solve)
+// ---------------------------------------------------------------------------
+// One thread per band element: column c = t / ldab, band row i = t % ldab;
+// rows off .. off + KL + KU hold A(r, c), r = c + i - off - KU, the others
+// and every position outside the matrix are zero (what suzerain_bsmbsm_zpack
+// leaves around the band, suzerain/bsmbsm_pack.def:66-119).
+__global__ void k_assemble_packed(int nsys, ModelSource ms, int KL, int KU, double2 *__restrict__ ab,
+                                  int ldab, long long ab_stride, int off)
+{
+    const int s = blockIdx.y;
+    const sgb_case &cs = ms.cs;
+    const int S = cs.S, N = S * cs.n;
+    const long long t = (long long) blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nsys || t >= (long long) ldab * N) return;
+    const int c = (int) (t / ldab), i = (int) (t - (long long) c * ldab);
+    const int r = c + i - off - KU;
+    double2 v = make_double2(0.0, 0.0);
+    if (i >= off && i <= off + KL + KU && r >= 0 && r < N) {
+        const int p = r / S, e = r - p * S, q = c / S, f = c - q * S;
+        if (sgb_is_dirichlet_row(&cs, r)) {
+            v.x = (r == c) ? 1.0 : 0.0;
+        } else if (p - q <= cs.kl && q - p <= cs.ku) {
+            sgb_coef cM, cD1, cD2;
+            sgb_block_coefs(&cs, e, f, ms.phi, ms.kx[s], ms.kz[s], &cM, &cD1, &cD2);
+            const int k = cs.ku + p - q + q * cs.ld;
+            sgb_block_entry(cM, cD1, cD2, cs.M[k], cs.D1[k], cs.D2[k], &v.x, &v.y);
+        }
+    }
+    ab[s * ab_stride + t] = v;
+}
+
+extern "C" int sgb_plan_assemble_packed(sgb_plan *p, double phi, void *ab, int ldab,
+                                        long long ab_stride, int off, void *stream)
+{
+    if (!p || !ab) return fail("sgb_plan_assemble_packed: null argument");
+    if (off < 0 || ldab < off + p->KL + p->KU + 1 || ab_stride < (long long) ldab * p->N)
+        return fail("sgb_plan_assemble_packed: ldab must be >= off + KL + KU + 1 and "
+                    "ab_stride >= ldab * N");
+    std::lock_guard<std::mutex> lk(p->mu);
+    const long long per = (long long) ldab * p->N;
+    dim3 grd((unsigned) ((per + 255) / 256), (unsigned) p->nsys);
+    count_launch(1);
+    k_assemble_packed<<<grd, 256, 0, (cudaStream_t) stream>>>(
+        p->nsys, p->ms(phi), p->KL, p->KU, reinterpret_cast<double2 *>(ab), ldab, ab_stride, off);
+    SGB_CUDA_TRY(cudaGetLastError());
+    p->note((cudaStream_t) stream);
     return 0;
 }

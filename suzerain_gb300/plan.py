@@ -178,6 +178,14 @@ class Plan:
         return dict(info=info, siter=siter, diter=diter, res=res, tolsc=tolsc,
                     fact=fact.tobytes().decode())
 
+    def assemble_packed(self, phi: float, ab, ldab: int, off: int = 0, stream=0) -> None:
+        """Write every system's operator M + phi L as a packed complex128 band
+        into the device buffer ab (nsys x ldab x N, column-major per system):
+        off = 0, ldab = LD is packc; off = KL, ldab = LD + KL is packf."""
+        nat.check(self.L.sgb_plan_assemble_packed(self.handle, phi, _ptr(ab), int(ldab),
+                                                  int(ldab) * self.N, int(off), _ptr(stream)),
+                  "sgb_plan_assemble_packed")
+
     def set_timing(self, on: bool) -> None:
         nat.check(self.L.sgb_plan_set_timing(self.handle, int(on)), "sgb_plan_set_timing")
 
@@ -200,61 +208,104 @@ class Plan:
 
 
 class BatchPlan:
-    """One batch of systems of a case split into `parts` resident Plans over
-    consecutive wavenumber ranges, each substep issued on its own CUDA stream
-    (forked from and joined into the caller's stream) in the capturable form,
-    which keeps the host out of the refinement loop: the parts' kernels
-    overlap on the device, the FP64 residual and explicit-operator kernels
-    of one part alongside the complex64 factor of another.  Results are
-    those of one Plan over the whole batch with the capturable substep (each
-    system is solved by the same kernels on the same data)."""
+    """One batch of systems of a case split into `parts` resident plans over
+    consecutive wavenumber ranges (sgb_batch_*), each substep issued on the
+    part's own CUDA stream (forked from and joined into the caller's stream)
+    in the capturable form, which keeps the host out of the refinement loop:
+    the parts' kernels overlap on the device, the FP64 residual and
+    explicit-operator kernels of one part alongside the complex64 factor of
+    another.  Results are those of one Plan over the whole batch with the
+    capturable substep (each system is solved by the same kernels on the
+    same data).  substep_host runs the same from host buffers with each
+    part's copies overlapping the other parts' computation."""
 
     def __init__(self, case: SynthCase, kx: np.ndarray, kz: np.ndarray,
                  parts: int = 4, max_double_slots: int = 0, method: str = "M"):
-        import torch
-        self.torch = torch
-        n = int(len(kx))
-        parts = max(1, min(int(parts), n))
-        self.bounds = [int(b) for b in np.linspace(0, n, parts + 1)]
-        self.plans = []
-        for a, b in zip(self.bounds[:-1], self.bounds[1:]):
-            pl = Plan(case, kx[a:b], kz[a:b], max_double_slots=max_double_slots)
-            pl.prepare(method)
-            self.plans.append(pl)
-        self.streams = [torch.cuda.Stream() for _ in self.plans]
-        self.nsys = n
+        self.L = nat.load()
+        self.case = case
+        self._kx = np.ascontiguousarray(kx, dtype=np.float64)
+        self._kz = np.ascontiguousarray(kz, dtype=np.float64)
+        self.nsys = int(len(self._kx))
         self.N = case.N
+        self._cs = case.ctypes_case()
+        h = self.L.sgb_batch_create(C.byref(self._cs), self.nsys, self._kx.ctypes.data,
+                                    self._kz.ctypes.data, int(parts), int(max_double_slots),
+                                    method.encode() if method else b"\0")
+        if not h:
+            raise RuntimeError(f"sgb_batch_create failed: {nat.last_error()}")
+        self.handle = h
+        self.bounds = bounds(self.nsys, parts)
+
+    @property
+    def parts(self) -> int:
+        return len(self.bounds) - 1
 
     def substep(self, method: str, phi_exp: float, phi_imp: float, u_in, u_out,
-                spec: RefineSpec | None = None) -> None:
-        """u_in, u_out: device tensors (nsys x N), rows split by part."""
-        torch = self.torch
-        cur = torch.cuda.current_stream()
-        for s in self.streams:
-            s.wait_stream(cur)
-        for pl, s, a, b in zip(self.plans, self.streams, self.bounds[:-1], self.bounds[1:]):
-            with torch.cuda.stream(s):
-                pl.substep_capturable(method, phi_exp, phi_imp, u_in[a:b], u_out[a:b], spec,
-                                      stream=s.cuda_stream)
-        for s in self.streams:
-            cur.wait_stream(s)
+                spec: RefineSpec | None = None, stream=None) -> None:
+        """u_in, u_out: device tensors (nsys x N); stream: the caller's
+        stream (default torch's current stream)."""
+        if stream is None:
+            import torch
+            stream = torch.cuda.current_stream().cuda_stream
+        sp = (spec or RefineSpec()).ctypes()
+        nat.check(self.L.sgb_batch_substep(self.handle, method.encode(), phi_exp, phi_imp,
+                                           _ptr(u_in), _ptr(u_out), C.byref(sp), _ptr(stream)),
+                  "sgb_batch_substep")
+
+    def substep_host(self, method: str, phi_exp: float, phi_imp: float,
+                     u_in: np.ndarray, u_out: np.ndarray, spec: RefineSpec | None = None,
+                     stream=0) -> None:
+        """u_in, u_out: host arrays (nsys x N complex128, pinned for overlap);
+        returns when u_out holds the result."""
+        sp = (spec or RefineSpec()).ctypes()
+        nat.check(self.L.sgb_batch_substep_host(self.handle, method.encode(), phi_exp, phi_imp,
+                                                _ptr(u_in), _ptr(u_out), C.byref(sp),
+                                                _ptr(stream)),
+                  "sgb_batch_substep_host")
 
     def report(self) -> dict:
-        reps = [pl.report() for pl in self.plans]
-        out = {k: np.concatenate([r[k] for r in reps]) for k in reps[0] if k != "fact"}
-        out["fact"] = "".join(r["fact"] for r in reps)
+        n = self.nsys
+        info = np.zeros(n, np.int32)
+        siter = np.zeros(n, np.int32)
+        diter = np.zeros(n, np.int32)
+        res = np.zeros(n)
+        tolsc = np.zeros(n)
+        fact = np.zeros(n, np.uint8)
+        nat.check(self.L.sgb_batch_report(self.handle, info.ctypes.data, siter.ctypes.data,
+                                          diter.ctypes.data, res.ctypes.data,
+                                          tolsc.ctypes.data, fact.ctypes.data),
+                  "sgb_batch_report")
+        return dict(info=info, siter=siter, diter=diter, res=res, tolsc=tolsc,
+                    fact=fact.tobytes().decode())
+
+    def backward_error(self, stream=0) -> np.ndarray:
+        out = np.zeros(self.nsys)
+        nat.check(self.L.sgb_batch_backward_error(self.handle, out.ctypes.data, _ptr(stream)),
+                  "sgb_batch_backward_error")
         return out
 
-    def backward_error(self) -> np.ndarray:
-        return np.concatenate([pl.backward_error() for pl in self.plans])
-
     def unserved(self) -> int:
-        return sum(pl.unserved() for pl in self.plans)
+        n = C.c_int()
+        nat.check(self.L.sgb_batch_unserved(self.handle, C.byref(n)), "sgb_batch_unserved")
+        return n.value
 
     def device_bytes(self) -> int:
-        return sum(pl.device_bytes() for pl in self.plans)
+        return int(self.L.sgb_batch_device_bytes(self.handle))
 
     def close(self) -> None:
-        for pl in self.plans:
-            pl.close()
-        self.plans = []
+        if getattr(self, "handle", None):
+            self.L.sgb_batch_destroy(self.handle)
+            self.handle = None
+
+    __del__ = close
+
+
+def bounds(nsys: int, parts: int) -> list:
+    """Row offsets of a batch's parts (sgb_batch_bounds): consecutive ranges,
+    part i holding rows i nsys / parts .. (i + 1) nsys / parts - 1."""
+    L = nat.load()
+    out = (C.c_int * (max(1, min(parts, nsys)) + 1))()
+    p = L.sgb_batch_bounds(int(nsys), int(parts), out)
+    if p < 1:
+        raise ValueError(f"sgb_batch_bounds({nsys}, {parts}): {nat.last_error()}")
+    return [int(out[i]) for i in range(p + 1)]

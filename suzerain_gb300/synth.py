@@ -77,16 +77,21 @@ class SynthCase:
         return cs
 
 
+def _check(rc: int, what: str) -> None:
+    if rc != 0:
+        raise RuntimeError(f"{what} failed ({rc})")
+
+
 def make_case(S=5, Ny=48, k=8, htdelta=2.0, left=0.0, right=2.0,
               offscale=0.1, complex_coupling=False, seed=SEED_BASE,
               dirichlet_mask=DIRICHLET_ALL) -> SynthCase:
-    L = nat.load()
+    L = nat.generator()
     kl, ku = C.c_int(0), C.c_int(0)
     rc = L.sgb_synth_case(S, Ny, k, htdelta, left, right, offscale,
                           int(complex_coupling), seed, dirichlet_mask,
                           C.byref(kl), C.byref(ku), None, None, None, None,
                           None, None, None)
-    nat.check(rc, "sgb_synth_case(query)")
+    _check(rc, "sgb_synth_case(query)")
     ld = kl.value + 1 + ku.value
     arrs = {nm: np.zeros(ld * Ny) for nm in ("M", "D1", "D2")}
     co = {nm: np.zeros(S * S) for nm in ("a", "b", "c", "g")}
@@ -96,7 +101,7 @@ def make_case(S=5, Ny=48, k=8, htdelta=2.0, left=0.0, right=2.0,
                           arrs["D1"].ctypes.data, arrs["D2"].ctypes.data,
                           co["a"].ctypes.data, co["b"].ctypes.data,
                           co["c"].ctypes.data, co["g"].ctypes.data)
-    nat.check(rc, "sgb_synth_case")
+    _check(rc, "sgb_synth_case")
     return SynthCase(S=S, Ny=Ny, k=k, htdelta=htdelta, left=left, right=right,
                      offscale=offscale, complex_coupling=complex_coupling,
                      seed=seed, dirichlet_mask=dirichlet_mask, kl=kl.value,
@@ -105,19 +110,19 @@ def make_case(S=5, Ny=48, k=8, htdelta=2.0, left=0.0, right=2.0,
 
 def wavenumbers(Nx: int, Nz: int, Lx: float, Lz: float):
     """(kx, kz) of every retained R2C mode pair, m fastest."""
-    L = nat.load()
+    L = nat.generator()
     nsys = (Nx // 2 + 1) * Nz
     kx, kz = np.zeros(nsys), np.zeros(nsys)
-    nat.check(L.sgb_synth_wavenumbers(Nx, Nz, Lx, Lz, kx.ctypes.data,
-                                      kz.ctypes.data), "sgb_synth_wavenumbers")
+    _check(L.sgb_synth_wavenumbers(Nx, Nz, Lx, Lz, kx.ctypes.data,
+                                   kz.ctypes.data), "sgb_synth_wavenumbers")
     return kx, kz
 
 
 def rhs(seed: int, nsys: int, N: int) -> np.ndarray:
     """(nsys, N) complex128 with independent N(0,1) parts, natural order."""
-    L = nat.load()
+    L = nat.generator()
     u = np.zeros((nsys, N), dtype=np.complex128)
-    nat.check(L.sgb_synth_rhs(seed, nsys, N, u.ctypes.data), "sgb_synth_rhs")
+    _check(L.sgb_synth_rhs(seed, nsys, N, u.ctypes.data), "sgb_synth_rhs")
     return u
 
 
@@ -171,7 +176,22 @@ CONFIGS = {
               1e-3, seed=SEED_BASE + 2),
     "2stiff": Config("mixed-stiff", 5, 192, 8, 256, 192, FOURPI, FOURPI / 3,
                      5e-2, offscale=0.5, seed=SEED_BASE + 2),
+    # the configuration text's wall rows (momentum equations 1..3 only)
+    "2literal": Config("mixed-literal-walls", 5, 192, 8, 256, 192, FOURPI, FOURPI / 3,
+                       1e-3, seed=SEED_BASE + 2, dirichlet_mask=DIRICHLET_MOMENTUM),
 }
+
+
+def describe_operator(cfg: Config) -> str:
+    """One line naming the operator a configuration solves: wall rows, the
+    sign of the implicit scale, phi dt and the off-diagonal scale."""
+    if cfg.dirichlet_mask == DIRICHLET_ALL:
+        walls = "wall rows on every equation"
+    else:
+        eqs = [e for e in range(cfg.S) if (cfg.dirichlet_mask >> e) & 1]
+        walls = "wall rows on equations " + ",".join(map(str, eqs))
+    return (f"(M - phi dt L) x = (M + dt alpha_0 L) u, L = a D1 + b D2 - c k^2 M, "
+            f"phi dt = {cfg.phi:g}, off-diagonal scale {cfg.offscale:g}, {walls}")
 
 # SMR91 coefficients (suzerain/lowstorage.hpp:1242-1305), numerators / 480.
 SMR91_ALPHA = (29 / 96, -3 / 40, 1 / 6)

@@ -96,4 +96,12 @@ def main(ref: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    # the reference checkout: argument, else SUZERAIN_REFERENCE_DIR, else the
+    # oracle build recipe's default
+    ROOT = os.path.dirname(os.path.dirname(HERE))
+    sys.path.insert(0, ROOT)
+    from oracle import oracle as O
+    ref = sys.argv[1] if len(sys.argv) > 1 else O.reference_dir()
+    if not ref:
+        sys.exit("no reference checkout: pass its path or set SUZERAIN_REFERENCE_DIR")
+    main(ref)

@@ -579,7 +579,7 @@ def test_batch_plan_parts_match_one_plan(lib, torch_cuda):
     one.substep_capturable("M", 0.0, -c.phi, du, want, spec)
     torch.cuda.synchronize()
     one.close()
-    bp = P.BatchPlan(cs, kx, kz, parts=3, max_double_slots=22)
+    bp = P.BatchPlan(cs, kx, kz, parts=3, max_double_slots=66)
     got = torch.zeros_like(du)
     bp.substep("M", 0.0, -c.phi, du, got, spec)
     torch.cuda.synchronize()
@@ -903,8 +903,8 @@ def _three_substeps(plan_fn, phis, du, spec):
 
 def test_plan_three_substeps_in_a_cuda_graph(lib, torch_cuda):
     """Three SMR91 substeps recorded into one CUDA graph give the same bits
-    as the ordinary host-driven substeps (the capped refinement makes the
-    same decisions when every system converges within the cap)."""
+    as the ordinary host-driven substeps (the device-counted refinement
+    makes the same decisions)."""
     torch = torch_cuda
     from suzerain_gb300 import plan as P, synth
     c, cs, kx, kz, u = config0()
@@ -945,17 +945,20 @@ def test_plan_three_substeps_in_a_cuda_graph(lib, torch_cuda):
     assert np.array_equal(bufs[2].cpu().numpy(), ref[2])
 
 
-def test_plan_capturable_fallback_matches_host_driven(lib, oracle, torch_cuda):
-    """The stress mask (walls on momentum only) sends many systems to the
-    complex128 fallback: the capturable form, with enough fallback slots,
-    reaches the same backward error bar and the same fallback set."""
+@pytest.mark.parametrize("siter", [3, 25])
+def test_plan_capturable_fallback_matches_host_driven(lib, oracle, torch_cuda, siter):
+    """The stress mask (walls on momentum only) makes complex64 refinement
+    slow (up to ~10 solves) and sends many systems to the complex128
+    fallback: the capturable form, with enough fallback slots, runs the same
+    decisions as the host-driven one (the reference's siter + 1 and
+    diter + 2 bounds), so fact, siter and the solution are identical."""
     torch = torch_cuda
     from suzerain_gb300 import plan as P, synth
     c = synth.Config(**{**synth.CONFIGS[0].__dict__, "dirichlet_mask": synth.DIRICHLET_MOMENTUM})
     cs, kx, kz, u = c.batch()
     synth.zero_dirichlet_rows(cs, u)
     phi_e, phi_i = synth.smr91_phis(c.phi)
-    spec = P.RefineSpec(aiter=5, siter=3, diter=5, tolsc=145.0)
+    spec = P.RefineSpec(aiter=5, siter=siter, diter=5, tolsc=145.0)
     pl = P.Plan(cs, kx, kz, max_double_slots=len(kx))
     du = dev(torch, u)
     a = torch.zeros_like(du)
@@ -967,8 +970,12 @@ def test_plan_capturable_fallback_matches_host_driven(lib, oracle, torch_cuda):
     rep_b = pl.report()
     assert pl.unserved() == 0
     assert list(rep_a["fact"]) == list(rep_b["fact"])
+    assert np.array_equal(rep_a["siter"], rep_b["siter"])
+    assert np.array_equal(rep_a["diter"], rep_b["diter"])
     assert np.array_equal(a.cpu().numpy(), b.cpu().numpy())
     assert pl.backward_error().max() <= 1e-12
+    if siter == 25:
+        assert rep_a["siter"].max() > 4      # beyond the old four-solve cap
 
 
 def test_multicase_graph_matches_eager(lib, torch_cuda):
@@ -980,8 +987,8 @@ def test_multicase_graph_matches_eager(lib, torch_cuda):
     cfgs = [synth.Config("a", 5, 48, 6, 8, 8, synth.FOURPI, synth.FOURPI / 3, 1e-3, seed=11),
             synth.Config("b", 7, 64, 8, 8, 6, synth.FOURPI, synth.FOURPI / 3, 1e-3, seed=12),
             synth.Config("c", 5, 96, 8, 16, 8, synth.FOURPI, synth.FOURPI / 3, 1e-3, seed=13)]
-    # siter = 3: the capturable form's complex64 bound (siter + 1 solves) is
-    # then the reference's own, so graph and host-driven runs agree bit for bit
+    # graph and host-driven runs make the same decisions (siter + 1 complex64
+    # correction solves at most in both), so they agree bit for bit
     spec = P.RefineSpec(aiter=5, siter=3, diter=5, tolsc=145.0)
     mc = multicase.MultiCase(cfgs, nstreams=2)
     mc.step_eager("M", spec)
@@ -1000,8 +1007,7 @@ def test_multicase_graph_matches_eager(lib, torch_cuda):
     solo.step_eager("M", spec)
     torch.cuda.synchronize()
     assert np.array_equal(solo.result(0).cpu().numpy(), eager[1])
-    # the production spec (siter = 25, capped at four solves in the graph)
-    # still meets the backward error bar
+    # the production spec (siter = 25) meets the backward error bar
     mc2 = multicase.MultiCase(cfgs, nstreams=2)
     mc2.capture("M", P.RefineSpec(aiter=5, siter=25, diter=5, tolsc=145.0))
     mc2.replay()

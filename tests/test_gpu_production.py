@@ -1,0 +1,146 @@
+"""GPU parity at the benchmarked geometries, against the FP64 oracle.
+
+The plan-level tests of test_gpu_parity.py run the small CPU-runnable batch
+(N = 240).  These run the geometries that are timed: the production batch
+(S = 5, Ny = 192, k = 8: N = 960, KL = KU = 34), its stiff variant, the
+literal wall mask, and two configuration-3 geometries (S = 7, k = 8: KL = 48;
+S = 5, k = 6: KL = 24), each on an evenly spaced sample of its wavenumber
+pairs (a system's result does not depend on the rest of the batch,
+test_plan_result_independent_of_batch), for both methods.
+
+Bars (per system):
+  * complex128 ('Z'): forward difference ||x - x_oracle||_inf / ||x_oracle||_inf
+    <= 1e-11 and normwise backward error <= 1e-13; info equal;
+  * mixed ('M'): normwise backward error <= 1e-12; fact and info equal to the
+    oracle's zcgbsvx restatement run on the same system; forward difference
+    against the FP64 oracle <= 1e-10 (refinement stops at a backward error of
+    about 1e-12, and these operators have kappa_inf of a few thousand).
+The literal wall mask (walls on the momentum equations only) is
+near-singular (kappa_inf up to 1e13), so there the forward bar is the
+kappa-scaled one of two backward-stable solvers, 8 kappa_inf eps.
+"""
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+SPEC = dict(aiter=5, siter=25, diter=5, tolsc=145.0)
+NT = os.cpu_count() or 1
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.fail("GPU tests need a CUDA device")
+    return torch
+
+
+@pytest.fixture(scope="module")
+def lib(native, torch_cuda):
+    assert native.sgb_device_ok() == 0, native.sgb_last_error().decode()
+    return native
+
+
+def sample(cfg, nsamp):
+    """The case and an evenly spaced sample of the batch's systems."""
+    cs, kx, kz, u = cfg.batch()
+    idx = np.linspace(0, len(kx) - 1, nsamp).round().astype(int)
+    return cs, kx[idx], kz[idx], u[idx]
+
+
+def run_plan(torch, cs, kx, kz, u, method, phi_e, phi_i, max_double_slots=0):
+    from suzerain_gb300 import plan as P
+    pl = P.Plan(cs, kx, kz, max_double_slots=max_double_slots)
+    du = torch.from_numpy(np.ascontiguousarray(u)).cuda()
+    out = torch.zeros_like(du)
+    pl.substep(method, phi_e, phi_i, du, out, P.RefineSpec(**SPEC))
+    torch.cuda.synchronize()
+    res = dict(x=out.cpu().numpy(), berr=pl.backward_error(), **pl.report())
+    pl.close()
+    return res
+
+
+def rel_diff(x, ref):
+    return np.max(np.abs(x - ref), axis=1) / np.max(np.abs(ref), axis=1)
+
+
+def production(name, **over):
+    from suzerain_gb300 import synth
+    base = synth.CONFIGS[name]
+    return synth.Config(**{**base.__dict__, **over})
+
+
+CASES = {
+    # configuration 1/2: the benchmarked batch
+    "config2": lambda: production(2),
+    # configuration 2's stiff variant (phi dt = 5e-2, off-diagonal scale 0.5)
+    "config2stiff": lambda: production("2stiff"),
+    # configuration 3 geometries: S = 7, k = 8 (KL = 48) and S = 5, k = 6 (KL = 24)
+    "S7k8": lambda: production(2, name="S7k8", S=7, Ny=256, k=8, Nx=64, Nz=48),
+    "S5k6": lambda: production(2, name="S5k6", S=5, Ny=128, k=6, Nx=128, Nz=96),
+}
+
+
+@pytest.mark.parametrize("name", list(CASES))
+@pytest.mark.parametrize("explicit", [True, False])
+def test_production_plain_fp64_matches_oracle(lib, oracle, torch_cuda, name, explicit):
+    from suzerain_gb300 import synth
+    cfg = CASES[name]()
+    cs, kx, kz, u = sample(cfg, 256)
+    phi_e, phi_i = synth.smr91_phis(cfg.phi, explicit=explicit)
+    g = run_plan(torch_cuda, cs, kx, kz, u, "Z", phi_e, phi_i)
+    o = oracle.batch_solve(cs, kx, kz, u, phi_exp=phi_e, phi_imp=phi_i, nthreads=NT)
+    assert (g["info"] == o["info"]).all() and (o["info"] == 0).all()
+    assert g["berr"].max() <= 1e-13, g["berr"].max()
+    rel = rel_diff(g["x"], o["x"])
+    assert rel.max() <= 1e-11, rel.max()
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_production_mixed_matches_oracle(lib, oracle, torch_cuda, name):
+    from suzerain_gb300 import synth
+    cfg = CASES[name]()
+    cs, kx, kz, u = sample(cfg, 256)
+    phi_e, phi_i = synth.smr91_phis(cfg.phi)
+    g = run_plan(torch_cuda, cs, kx, kz, u, "M", phi_e, phi_i)
+    o = oracle.batch_solve(cs, kx, kz, u, phi_exp=phi_e, phi_imp=phi_i, nthreads=NT)
+    om = oracle.batch_solve(cs, kx, kz, u, phi_exp=phi_e, phi_imp=phi_i, mixed=True,
+                            nthreads=NT, **SPEC)
+    assert (g["info"] == 0).all() and (om["info"] == 0).all()
+    assert g["berr"].max() <= 1e-12, g["berr"].max()
+    assert (g["tolsc"] <= 1.0).all()
+    assert list(g["fact"]) == list(om["fact"])
+    rel = rel_diff(g["x"], o["x"])
+    assert rel.max() <= 1e-10, rel.max()
+
+
+def test_literal_wall_mask_at_production_size(lib, oracle, torch_cuda):
+    """Walls on the momentum equations only, the configuration text's mask:
+    the implicit operator is near-singular, the reference's zcgbsvx refines
+    for several complex64 solves and drops part of the batch to complex128.
+    Both methods still meet their backward error bars, and the mixed path
+    sends a comparable share of systems to complex128 as the oracle."""
+    from suzerain_gb300 import synth
+    cfg = production(2, dirichlet_mask=synth.DIRICHLET_MOMENTUM)
+    cs, kx, kz, u = sample(cfg, 128)
+    phi_e, phi_i = synth.smr91_phis(cfg.phi)
+    gz = run_plan(torch_cuda, cs, kx, kz, u, "Z", phi_e, phi_i)
+    gm = run_plan(torch_cuda, cs, kx, kz, u, "M", phi_e, phi_i, max_double_slots=len(kx))
+    o = oracle.batch_solve(cs, kx, kz, u, phi_exp=phi_e, phi_imp=phi_i, nthreads=NT)
+    om = oracle.batch_solve(cs, kx, kz, u, phi_exp=phi_e, phi_imp=phi_i, mixed=True,
+                            nthreads=NT, **SPEC)
+    assert (gz["info"] == o["info"]).all()
+    assert gz["berr"].max() <= 1e-13, gz["berr"].max()
+    assert gm["berr"].max() <= 1e-12, gm["berr"].max()
+    # kappa-scaled forward bar of two backward-stable solvers
+    eps = 2.220446049250313e-16
+    kap = np.array([np.linalg.cond(oracle.band_to_dense(
+        oracle.assemble_case(cs, phi_i, kx[s], kz[s]), cs.N, cs.KL, cs.KU, cs.LD), np.inf)
+        for s in range(0, len(kx), 8)])
+    rel = rel_diff(gz["x"], o["x"])[::8]
+    assert (rel <= np.maximum(1e-11, 8 * kap * eps)).all(), (rel / (kap * eps)).max()
+    nd, nd_o = gm["fact"].count("D"), om["fact"].count("D")
+    assert abs(nd - nd_o) <= max(2, 0.05 * len(kx)), (nd, nd_o)

@@ -5,7 +5,7 @@ event completes when the work recorded before it on its stream has run; a
 plan's substep advances the case's state), so that admission in arrival
 order, the HBM budget, overlap of resident cases, the alternating state
 buffers, plan release and latency accounting are checked on CPU, as are
-BatchPlan's row partition and stream fork/join and MultiCase's SMR91
+the batch's row partition and MultiCase's SMR91
 substep coefficients, stream assignment and state ping-pong.  The GPU counterpart
 (test_serving_result_same_alone_and_in_the_mix) checks that each case's
 result is the same alone and in the mix."""
@@ -192,84 +192,22 @@ def test_case_larger_than_the_budget_runs_alone(fake):
     assert fake.closed == [0, 1]
 
 
-def test_batch_plan_parts_partition_rows_and_join_streams(monkeypatch):
-    """BatchPlan splits the batch into consecutive row ranges, one resident
-    plan and stream each, forks every part's stream from the caller's stream
-    before issuing and joins them back after, and concatenates the parts'
-    reports in row order."""
+def test_batch_bounds_partition_rows():
+    """A batch's parts are consecutive row ranges, part i holding rows
+    i n / parts .. (i + 1) n / parts - 1 (sgb_batch_bounds, host code), with
+    the part count clamped to the systems; bad arguments are refused."""
     from suzerain_gb300 import plan as P
-    events = []
-
-    class Stream:
-        n = 0
-
-        def __init__(self):
-            Stream.n += 1
-            self.cuda_stream = Stream.n
-
-        def wait_stream(self, other):
-            events.append(("wait", self.cuda_stream, other.cuda_stream))
-
-    caller = Stream()
-
-    class Ctx:
-        def __init__(self, st):
-            self.st = st
-
-        def __enter__(self):
-            return self.st
-
-        def __exit__(self, *a):
-            return False
-
-    cuda = types.SimpleNamespace(Stream=Stream, current_stream=lambda: caller, stream=Ctx)
-    monkeypatch.setitem(sys.modules, "torch", types.SimpleNamespace(cuda=cuda))
-
-    class Plan:
-        def __init__(self, case, kx, kz, max_double_slots=0):
-            self.kx = np.asarray(kx)
-            self.nsys = len(kx)
-
-        def prepare(self, method):
-            events.append(("prepare", method, self.nsys))
-
-        def substep_capturable(self, method, pe, pi, u_in, u_out, spec, stream=0):
-            u_out[...] = u_in * 2
-            events.append(("substep", stream, int(self.kx[0]), self.nsys))
-
-        def report(self):
-            return {"info": np.zeros(self.nsys, np.int32), "siter": self.kx.astype(np.int32),
-                    "fact": "S" * self.nsys}
-
-        def close(self):
-            events.append(("close", self.nsys))
-
-    monkeypatch.setattr(P, "Plan", Plan)
-    case = types.SimpleNamespace(N=3)
-    n = 10
-    kx, kz = np.arange(n, dtype=float), np.zeros(n)
-    bp = P.BatchPlan(case, kx, kz, parts=4, method="M")
-    assert bp.bounds == [0, 2, 5, 7, 10]
-    assert [e[2] for e in events if e[0] == "prepare"] == [2, 3, 2, 3]
-    events.clear()
-    u = np.arange(n * 3, dtype=float).reshape(n, 3)
-    out = np.zeros_like(u)
-    bp.substep("M", 0.1, -0.2, u, out)
-    np.testing.assert_array_equal(out, 2 * u)
-    part_streams = [s.cuda_stream for s in bp.streams]
-    assert events[:4] == [("wait", s, caller.cuda_stream) for s in part_streams]
-    assert [e[1:] for e in events[4:8]] == [(s, a, b - a) for s, a, b in
-                                            zip(part_streams, bp.bounds[:-1], bp.bounds[1:])]
-    assert events[8:] == [("wait", caller.cuda_stream, s) for s in part_streams]
-    rep = bp.report()
-    np.testing.assert_array_equal(rep["siter"], np.arange(n))
-    assert rep["fact"] == "S" * n
-    bp.close()
-    assert bp.plans == []
-
-    bp = P.BatchPlan(case, kx[:3], kz[:3], parts=8)       # more parts than systems
-    assert bp.bounds == [0, 1, 2, 3]
-
+    assert P.bounds(10, 4) == [0, 2, 5, 7, 10]
+    assert P.bounds(5, 8) == [0, 1, 2, 3, 4, 5]
+    assert P.bounds(24768, 4) == [0, 6192, 12384, 18576, 24768]
+    b = P.bounds(172160, 7)
+    assert b[0] == 0 and b[-1] == 172160 and len(b) == 8
+    sizes = np.diff(b)
+    assert sizes.max() - sizes.min() <= 1
+    with pytest.raises(ValueError):
+        P.bounds(0, 4)
+    with pytest.raises(ValueError):
+        P.bounds(10, 0)
 
 def test_multicase_step_scales_smr91_substeps_and_ping_pongs(monkeypatch):
     """MultiCase.step_eager issues every case's three SMR91 substeps in order
