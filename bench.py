@@ -139,7 +139,7 @@ def cpu_baseline(cfg, cs, kx, kz, u, phi_e, phi_i, nsample: int, nthreads: int,
     ob = O.openblas_path() is not None
     r = O.batch_solve(cs, kx[idx], kz[idx], u[idx], phi_exp=phi_e, phi_imp=phi_i, mixed=mixed,
                       aiter=SPEC["aiter"], siter=SPEC["siter"], diter=SPEC["diter"],
-                      tolsc=SPEC["tolsc"], nthreads=nthreads, openblas=ob)
+                      tolsc=cfg.tolsc, nthreads=nthreads, openblas=ob)
     lat = r["latency"]
     rec = dict(value=nsample / r["wall"], unit=UNIT, cores=nthreads, kind="port",
                sample=(f"{nsample} of {len(kx)} systems of the same batch, evenly spaced; "
@@ -278,7 +278,7 @@ def run_variant(key, args, nthreads) -> dict:
     cs, kx, kz, u = cfg.batch()
     nsys = len(kx)
     phi_e, phi_i = synth.smr91_phis(cfg.phi)
-    spec = P.RefineSpec(**SPEC)
+    spec = P.RefineSpec(**{**SPEC, "tolsc": cfg.tolsc})
     stream = torch.cuda.current_stream()
     du = torch.from_numpy(u).cuda()
     dout = torch.empty_like(du)
@@ -341,7 +341,7 @@ def run_packed(cfg, cs, kx, kz, u, phi_i, args, peak) -> dict:
             ("res", torch.float64), ("tolsc", torch.float64), ("fact", torch.uint8))}
     R = nat.RefineReport(*(rep[k].data_ptr() for k in ("info", "siter", "diter", "res",
                                                          "tolsc", "fact")))
-    S = nat.RefineSpec(SPEC["aiter"], SPEC["siter"], SPEC["diter"], SPEC["tolsc"])
+    S = nat.RefineSpec(SPEC["aiter"], SPEC["siter"], SPEC["diter"], cfg.tolsc)
 
     def step():
         nat.check(L.sgb_zcgbsvx_batched(nsys, N, cs.KL, cs.KU, b"N", ab.data_ptr(), LD,
@@ -385,7 +385,7 @@ def run_ours(args):
         kx, kz, u = kx[:args.nsys], kz[:args.nsys], u[:args.nsys]
     nsys, N = u.shape
     phi_e, phi_i = synth.smr91_phis(cfg.phi)
-    spec = P.RefineSpec(**SPEC)
+    spec = P.RefineSpec(**{**SPEC, "tolsc": cfg.tolsc})
     stream = torch.cuda.current_stream()
     sptr = stream.cuda_stream
     du = torch.from_numpy(u).cuda()

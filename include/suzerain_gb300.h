@@ -519,8 +519,11 @@ int sgb_zcgbsvx_batched(int nsys, int N, int KL, int KU, char trans,
  *  cudaMalloc/cudaFree and no allocating library routine: its scratch is a
  *  fixed 64 MiB __device__ array inside this library, which every GPU that
  *  loads the library holds until process exit.  Problems whose scratch
- *  (about 2.4 MB per system at N = 960, KL = KU = 34) exceeds 64 MiB are
- *  rejected with an error naming both sizes.  The first call on a device
+ *  exceeds 64 MiB are rejected with an error naming both sizes: at N = 960,
+ *  KL = KU = 34 the scratch is 6.3 MB for four complex128 fallback slots
+ *  (fallback systems pass through them four at a time) plus 0.82 MB per
+ *  system, so up to 74 systems per call.  Argument errors return the codes
+ *  of sgb_zcgbsvx_batched.  The first call on a device
  *  looks up the array's device address (cudaGetSymbolAddress) with that
  *  device current; make that first call before any stream capture.  All
  *  calls share the one array: calls that overlap on the GPU (different

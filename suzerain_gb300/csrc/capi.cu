@@ -315,16 +315,31 @@ __global__ void k_report_copy(int nsys, RefineState st, int *info, int *siter, i
     if (fact) fact[s] = st.fact[s];
 }
 
+namespace sgb {
+// Argument checks shared by the batched zcgbsvx entry points: 0, or the
+// negative code with the message set (-4 trans, -5 geometry or ldab,
+// -16 tolsc, -99 siter and diter both negative, -1 nsys < 0).
+int zcgbsvx_batched_check(const char *who, int nsys, int N, int KL, int KU, char trans, int ldab,
+                          const sgb_refine_spec *spec)
+{
+    std::string w(who);
+    if (trans != 'N' && trans != 'T' && trans != 'C') return fail((w + ": bad trans").c_str(), -4);
+    if (!geom_ok(N, KL, KU) || ldab < KL + KU + 1) return fail((w + ": bad geometry").c_str(), -5);
+    if (!spec || spec->tolsc < 0) return fail((w + ": bad tolsc").c_str(), -16);
+    if (spec->siter < 0 && spec->diter < 0) return fail((w + ": siter and diter < 0").c_str(), -99);
+    if (nsys < 0) return fail((w + ": nsys < 0").c_str(), -1);
+    return 0;
+}
+}  // namespace sgb
+
 extern "C" int sgb_zcgbsvx_batched(int nsys, int N, int KL, int KU, char trans, const void *ab,
                                    int ldab, long long ab_stride, const void *b, void *x,
                                    const sgb_refine_spec *spec, const sgb_refine_report *report,
                                    void *stream)
 {
     trans = (char) toupper(trans);
-    if (trans != 'N' && trans != 'T' && trans != 'C') return fail("sgb_zcgbsvx_batched: bad trans", -4);
-    if (!geom_ok(N, KL, KU) || ldab < KL + KU + 1) return fail("sgb_zcgbsvx_batched: bad geometry", -5);
-    if (!spec || spec->tolsc < 0) return fail("sgb_zcgbsvx_batched: bad tolsc", -16);
-    if (spec->siter < 0 && spec->diter < 0) return fail("sgb_zcgbsvx_batched: siter and diter < 0", -99);
+    const int bad = zcgbsvx_batched_check("sgb_zcgbsvx_batched", nsys, N, KL, KU, trans, ldab, spec);
+    if (bad) return bad;
     if (nsys == 0) return 0;
     std::lock_guard<std::mutex> lk(g_zc.mu);
     RefineProblem P;

@@ -57,6 +57,10 @@ struct RefineOutputs {
 };
 
 size_t refine_workspace_bytes(const RefineProblem &P);
+// Argument checks of the batched zcgbsvx entry points (capi.cu): 0 or the
+// negative error code, with the library's last-error message set.
+int zcgbsvx_batched_check(const char *who, int nsys, int N, int KL, int KU, char trans, int ldab,
+                          const sgb_refine_spec *spec);
 int refine_batched(const RefineProblem &P, void *workspace, size_t workspace_bytes,
                    RefineOutputs &out, cudaStream_t st);
 

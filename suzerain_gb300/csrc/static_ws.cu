@@ -13,8 +13,10 @@
 // The array is SGB_STATIC_WS_BYTES (64 MiB) of file-scope __device__ storage:
 // every GPU that loads this library holds it until the process exits, whether
 // or not this entry point is called.  A problem whose workspace exceeds it
-// (refine_workspace_bytes with one complex128 fallback slot per system;
-// roughly 2.4 MB per system at N = 960, KL = KU = 34) is rejected.
+// (refine_workspace_bytes with SGB_STATIC_SLOTS64 complex128 fallback slots,
+// through which the fallback systems pass in chunks; at N = 960,
+// KL = KU = 34 that is 6.3 MB plus about 0.82 MB per system, so up to 74
+// systems per call) is rejected.
 #include "suzerain_gb300.h"
 #include "sgb_internal.h"
 #include "sgb_refine.h"
@@ -26,6 +28,7 @@
 using namespace sgb;
 
 #define SGB_STATIC_WS_BYTES (64ull << 20)
+#define SGB_STATIC_SLOTS64 4
 #define SGB_STATIC_MAX_DEVICES 64
 
 static __device__ __align__(256) unsigned char g_sgb_static_ws[SGB_STATIC_WS_BYTES];
@@ -65,13 +68,9 @@ extern "C" int sgb_zcgbsvx_batched_static(int nsys, int N, int KL, int KU, char 
                                           const sgb_refine_report *report, void *stream)
 {
     trans = (char) std::toupper((unsigned char) trans);
-    if (trans != 'N' && trans != 'T' && trans != 'C')
-        return static_fail("sgb_zcgbsvx_batched_static: bad trans");
-    if (N < 1 || KL < 0 || KU < 0 || KL + 1 > 64 || KL + KU + 1 > 192 || ldab < KL + KU + 1)
-        return static_fail("sgb_zcgbsvx_batched_static: bad geometry");
-    if (!spec || spec->tolsc < 0 || (spec->siter < 0 && spec->diter < 0))
-        return static_fail("sgb_zcgbsvx_batched_static: bad refinement spec");
-    if (nsys < 0) return static_fail("sgb_zcgbsvx_batched_static: nsys < 0");
+    const int bad = zcgbsvx_batched_check("sgb_zcgbsvx_batched_static", nsys, N, KL, KU, trans,
+                                          ldab, spec);
+    if (bad) return bad;
     if (nsys == 0) return 0;
 
     RefineProblem P;
@@ -82,7 +81,9 @@ extern "C" int sgb_zcgbsvx_batched_static(int nsys, int N, int KL, int KU, char 
     P.b = reinterpret_cast<const double2 *>(b); P.b_stride = N;
     P.x = reinterpret_cast<double2 *>(x); P.x_stride = N;
     P.aiter = spec->aiter; P.siter = spec->siter; P.diter = spec->diter; P.tolsc = spec->tolsc;
-    P.nslot64 = nsys;
+    // complex128 fallback slots: the fallback runs in chunks of this many
+    // systems, so a few slots serve any number of fallback systems
+    P.nslot64 = nsys < SGB_STATIC_SLOTS64 ? nsys : SGB_STATIC_SLOTS64;
     const size_t need = refine_workspace_bytes(P);
     if (need > SGB_STATIC_WS_BYTES) {
         char msg[256];

@@ -25,7 +25,7 @@ def _band_batch(rng, nsys, n, kl, ku):
     return ab, ld
 
 
-def _solve(native, entry, torch, ab, b, n, kl, ku, ld):
+def _solve(native, entry, torch, ab, b, n, kl, ku, ld, spec=(5, 25, 5, 1.0)):
     from suzerain_gb300 import _native as nat
     nsys = b.shape[0]
     dab = torch.from_numpy(ab).cuda()
@@ -35,7 +35,7 @@ def _solve(native, entry, torch, ab, b, n, kl, ku, ld):
            (("info", torch.int32), ("siter", torch.int32), ("diter", torch.int32),
             ("res", torch.float64), ("tolsc", torch.float64), ("fact", torch.uint8))}
     R = nat.RefineReport(*(rep[k].data_ptr() for k in ("info", "siter", "diter", "res", "tolsc", "fact")))
-    S = nat.RefineSpec(5, 25, 5, 1.0)
+    S = nat.RefineSpec(*spec)
     rc = getattr(native, entry)(nsys, n, kl, ku, b"N", dab.data_ptr(), ld, ld * n, db.data_ptr(),
                                 x.data_ptr(), C.byref(S), C.byref(R), 0)
     assert rc == 0, native.sgb_last_error().decode()
@@ -63,10 +63,49 @@ def test_static_entry_matches_allocating_entry_twice(native):
         assert (got["tolsc"] <= 1.0).all()
 
 
+def test_static_entry_complex128_fallback_matches(native):
+    """siter = 0 sends every system to the complex128 fallback, which the
+    static scratch serves four systems at a time: the results, two calls in
+    a row, are the allocating entry's."""
+    torch = pytest.importorskip("torch")
+    assert torch.cuda.is_available()
+    rng = np.random.default_rng(7)
+    nsys, n, kl, ku = 9, 240, 34, 34
+    ab, ld = _band_batch(rng, nsys, n, kl, ku)
+    for call in range(2):
+        b = rng.normal(size=(nsys, n)) + 1j * rng.normal(size=(nsys, n))
+        ref = _solve(native, "sgb_zcgbsvx_batched", torch, ab, b, n, kl, ku, ld, (5, 0, 5, 1.0))
+        got = _solve(native, "sgb_zcgbsvx_batched_static", torch, ab, b, n, kl, ku, ld,
+                     (5, 0, 5, 1.0))
+        assert bytes(got["fact"]) == b"D" * nsys, (call, bytes(got["fact"]))
+        rel = np.max(np.abs(got["x"] - ref["x"])) / np.max(np.abs(ref["x"]))
+        assert rel <= 1e-11, (call, rel)
+        for k in ("info", "siter", "diter", "fact"):
+            assert np.array_equal(got[k], ref[k]), (call, k)
+
+
+def test_static_entry_argument_codes_match(native):
+    """Both entries return the same negative codes for bad arguments."""
+    from suzerain_gb300 import _native as nat
+    good = nat.RefineSpec(5, 25, 5, 1.0)
+    cases = [(6, 240, 34, 34, b"X", 69, good),                      # trans: -4
+             (6, 240, 70, 34, b"N", 105, good),                     # geometry: -5
+             (6, 240, 34, 34, b"N", 60, good),                      # ldab: -5
+             (6, 240, 34, 34, b"N", 69, nat.RefineSpec(5, 25, 5, -1.0)),   # tolsc: -16
+             (6, 240, 34, 34, b"N", 69, nat.RefineSpec(5, -1, -1, 1.0))]   # -99
+    want = [-4, -5, -5, -16, -99]
+    for (nsys, n, kl, ku, tr, ld, sp), w in zip(cases, want):
+        a = native.sgb_zcgbsvx_batched(nsys, n, kl, ku, tr, None, ld, ld * n, None, None,
+                                       C.byref(sp), None, 0)
+        b = native.sgb_zcgbsvx_batched_static(nsys, n, kl, ku, tr, None, ld, ld * n, None,
+                                              None, C.byref(sp), None, 0)
+        assert a == b == w, (a, b, w)
+
+
 def test_static_entry_rejects_oversized_problem(native):
     torch = pytest.importorskip("torch")
     from suzerain_gb300 import _native as nat
-    nsys, n, kl, ku = 64, 960, 34, 34      # ~150 MB of scratch > 64 MiB
+    nsys, n, kl, ku = 75, 960, 34, 34      # 67.7 MB of scratch > 64 MiB
     ld = kl + ku + 1
     S = nat.RefineSpec(5, 25, 5, 1.0)
     rc = native.sgb_zcgbsvx_batched_static(nsys, n, kl, ku, b"N", None, ld, ld * n, None, None,
