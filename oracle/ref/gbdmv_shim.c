@@ -53,3 +53,28 @@
 #define KL       const int kl,
 #define KU       const int ku,
 #include GBD_DEF
+
+/* The same body once more under the reference's own name of the
+ * general-bandwidth routine (real diagonals and band, complex x and y),
+ * which suzerain/blas_et_al/blasext.c's zgb<d..>mv_d_z wrappers call; the
+ * reference build of suzerain/rholut_imexop.c reaches it through them. */
+#if GBD_K == 1
+#define GBD_REF_NAME suzerain_gbdmv_dzz
+#elif GBD_K == 2
+#define GBD_REF_NAME suzerain_gbddmv_dzz
+#elif GBD_K == 3
+#define GBD_REF_NAME suzerain_gbdddmv_dzz
+#elif GBD_K == 4
+#define GBD_REF_NAME suzerain_gbddddmv_dzz
+#else
+#define GBD_REF_NAME suzerain_gbdddddmv_dzz
+#endif
+#define STATIC   /*exported*/
+#define FUNCTION GBD_REF_NAME
+#define TYPE_D   double
+#define TYPE_A   double
+#define TYPE_X   complex_double
+#define TYPE_Y   complex_double
+#define KL       const int kl,
+#define KU       const int ku,
+#include GBD_DEF

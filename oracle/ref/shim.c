@@ -208,58 +208,8 @@ double suzerain_blas_dnrm2(const int n, const double *x, const int incx)
     return scipy_dnrm2_(&n, x, &incx);
 }
 
-/* ---- blasext demote/promote (suzerain/blas_et_al/blasext.c:2823-2866) --- */
-int suzerain_blasext_zdemote(const int n, void *x)
-{
-    if (n < 0) return -1;
-    if (!x) return -2;
-    char *p = (char *) x;
-    for (int i = 0; i < n; ++i) {
-        complex_double in; memcpy(&in, p + i * sizeof(in), sizeof(in));
-        complex_float out = (complex_float) in;
-        memcpy(p + i * sizeof(out), &out, sizeof(out));
-    }
-    return 0;
-}
-
-int suzerain_blasext_zpromote(const int n, void *x)
-{
-    if (n < 0) return -1;
-    if (!x) return -2;
-    char *p = (char *) x;
-    for (int i = n; i-- > 0;) {
-        complex_float in; memcpy(&in, p + i * sizeof(in), sizeof(in));
-        complex_double out = in;
-        memcpy(p + i * sizeof(out), &out, sizeof(out));
-    }
-    return 0;
-}
-
-int suzerain_blasext_ddemote(const int n, void *x)
-{
-    if (n < 0) return -1;
-    if (!x) return -2;
-    char *p = (char *) x;
-    for (int i = 0; i < n; ++i) {
-        double in; memcpy(&in, p + i * sizeof(in), sizeof(in));
-        float out = (float) in;
-        memcpy(p + i * sizeof(out), &out, sizeof(out));
-    }
-    return 0;
-}
-
-int suzerain_blasext_dpromote(const int n, void *x)
-{
-    if (n < 0) return -1;
-    if (!x) return -2;
-    char *p = (char *) x;
-    for (int i = n; i-- > 0;) {
-        float in; memcpy(&in, p + i * sizeof(in), sizeof(in));
-        double out = in;
-        memcpy(p + i * sizeof(out), &out, sizeof(out));
-    }
-    return 0;
-}
+/* blasext demote/promote come from the reference's own blasext.c, which
+ * the reference build compiles too. */
 
 /* ---- banded matvec: general-bandwidth code from the reference's gbmv.def */
 #define STATIC   static

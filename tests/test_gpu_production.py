@@ -15,8 +15,9 @@ Bars (per system):
     oracle's zcgbsvx restatement run on the same system (the same spec:
     tolsc 145, or 20 for the stiff and literal-wall operators, whose
     backward error 145 would leave up to ~6e-12); forward difference against
-    the FP64 oracle <= 1e-10 (refinement stops at a backward error of about
-    1e-12, and these operators have kappa_inf of a few thousand).
+    the FP64 oracle <= 1e-10, or <= 8 kappa_inf 1e-12 on the systems whose
+    condition allows more (refinement stops at a backward error of about
+    1e-12), and a median <= 1e-12.
 The literal wall mask (walls on the momentum equations only) is
 near-singular (kappa_inf up to 1e13), so there the forward bar is the
 kappa-scaled one of two backward-stable solvers, 8 kappa_inf eps.
@@ -115,8 +116,14 @@ def test_production_mixed_matches_oracle(lib, oracle, torch_cuda, name):
     assert g["berr"].max() <= 1e-12, g["berr"].max()
     assert (g["tolsc"] <= 1.0).all()
     assert list(g["fact"]) == list(om["fact"])
+    # forward error of a backward error <= 1e-12 solution: <= 1e-10 where
+    # kappa_inf is moderate, else within 8 kappa_inf 1e-12
     rel = rel_diff(g["x"], o["x"])
-    assert rel.max() <= 1e-10, rel.max()
+    for s in np.nonzero(rel > 1e-10)[0]:
+        kap = np.linalg.cond(oracle.band_to_dense(
+            oracle.assemble_case(cs, phi_i, kx[s], kz[s]), cs.N, cs.KL, cs.KU, cs.LD), np.inf)
+        assert rel[s] <= 8 * kap * 1e-12, (s, rel[s], kap)
+    assert np.median(rel) <= 1e-12, np.median(rel)
 
 
 def test_literal_wall_mask_at_production_size(lib, oracle, torch_cuda):
