@@ -288,6 +288,90 @@ int sgb_bspline_collocation_bands(int k, int nbreak, const double *breakpts,
                                   int nderiv, int *n, int *kl, int *ku,
                                   double *bands, double *abscissae);
 
+/* ---- The production implicit operator (suzerain/rholut_imexop.h) ------ */
+
+/** suzerain/rholut_imexop.h:67-74. */
+typedef struct suzerain_rholut_imexop_scenario {
+    double Re, Pr, Ma, alpha, gamma;
+} suzerain_rholut_imexop_scenario;
+/** Wall-normal reference profiles; suzerain/rholut_imexop.h:77-104. */
+typedef struct suzerain_rholut_imexop_ref {
+    double *ux, *uy, *uz, *u2, *uxux, *uxuy, *uxuz, *uyuy, *uyuz, *uzuz;
+    double *nu, *nuux, *nuuy, *nuuz, *nuu2, *nuuxux, *nuuxuy, *nuuxuz, *nuuyuy, *nuuyuz,
+           *nuuzuz;
+    double *ex_gradrho, *ey_gradrho, *ez_gradrho, *e_divm, *e_deltarho;
+} suzerain_rholut_imexop_ref;
+/** Strides of the profiles; suzerain/rholut_imexop.h:107-134. */
+typedef struct suzerain_rholut_imexop_refld {
+    int ux, uy, uz, u2, uxux, uxuy, uxuz, uyuy, uyuz, uzuz;
+    int nu, nuux, nuuy, nuuz, nuu2, nuuxux, nuuxuy, nuuxuz, nuuyuy, nuuyuz, nuuzuz;
+    int ex_gradrho, ey_gradrho, ez_gradrho, e_divm, e_deltarho;
+} suzerain_rholut_imexop_refld;
+
+/** y <- (M + phi L) x + beta y for one wavenumber pair (km, kn), equations
+ *  E, u, v, w, rho (a NULL input and output pair omits an equation), with
+ *  the optional non-reflecting upper boundary matrices a, b, c;
+ *  suzerain/rholut_imexop.h:175-198, suzerain/rholut_imexop.c:43-545.
+ *  Inputs and outputs are stride-one vectors of w->n, host or device. */
+void suzerain_rholut_imexop_accumulate(
+    const sgb_complex_double phi, const double km, const double kn,
+    const suzerain_rholut_imexop_scenario *s, const suzerain_rholut_imexop_ref *r,
+    const suzerain_rholut_imexop_refld *ld, const suzerain_bsplineop_workspace *w,
+    const sgb_complex_double *in_rho_E, const sgb_complex_double *in_rho_u,
+    const sgb_complex_double *in_rho_v, const sgb_complex_double *in_rho_w,
+    const sgb_complex_double *in_rho, const sgb_complex_double beta,
+    sgb_complex_double *out_rho_E, sgb_complex_double *out_rho_u,
+    sgb_complex_double *out_rho_v, sgb_complex_double *out_rho_w,
+    sgb_complex_double *out_rho, const double *a, const double *b, const double *c);
+/** The km = kn = 0 form; suzerain/rholut_imexop.h:207-225. */
+void suzerain_rholut_imexop_accumulate00(
+    const sgb_complex_double phi, const suzerain_rholut_imexop_scenario *s,
+    const suzerain_rholut_imexop_ref *r, const suzerain_rholut_imexop_refld *ld,
+    const suzerain_bsplineop_workspace *w,
+    const sgb_complex_double *in_rho_E, const sgb_complex_double *in_rho_u,
+    const sgb_complex_double *in_rho_v, const sgb_complex_double *in_rho_w,
+    const sgb_complex_double *in_rho, const sgb_complex_double beta,
+    sgb_complex_double *out_rho_E, sgb_complex_double *out_rho_u,
+    sgb_complex_double *out_rho_v, sgb_complex_double *out_rho_w,
+    sgb_complex_double *out_rho, const double *c);
+/** P (M + phi L)^T P^T into packc storage (A_T->LD x A_T->N) for gbmv and
+ *  gbsvx; rho_E .. rho are the equations' positions (negative omits one);
+ *  buf is not needed (the reference's working storage);
+ *  suzerain/rholut_imexop.h:291-310, suzerain/rholut_imexop.def:41-594. */
+void suzerain_rholut_imexop_packc(
+    const sgb_complex_double phi, const double km, const double kn,
+    const suzerain_rholut_imexop_scenario *s, const suzerain_rholut_imexop_ref *r,
+    const suzerain_rholut_imexop_refld *ld, const suzerain_bsplineop_workspace *w,
+    const int rho_E, const int rho_u, const int rho_v, const int rho_w, const int rho,
+    sgb_complex_double *buf, suzerain_bsmbsm *A_T, sgb_complex_double *patpt,
+    const double *a, const double *b, const double *c);
+/** suzerain/rholut_imexop.h:324-340. */
+void suzerain_rholut_imexop_packc00(
+    const sgb_complex_double phi, const suzerain_rholut_imexop_scenario *s,
+    const suzerain_rholut_imexop_ref *r, const suzerain_rholut_imexop_refld *ld,
+    const suzerain_bsplineop_workspace *w,
+    const int rho_E, const int rho_u, const int rho_v, const int rho_w, const int rho,
+    sgb_complex_double *buf, suzerain_bsmbsm *A_T, sgb_complex_double *patpt,
+    const double *c);
+/** The same into packf storage ((A_T->LD + A_T->KL) x A_T->N, the band
+ *  from row A_T->KL; the rows above it are left as they were) for gbtrf;
+ *  suzerain/rholut_imexop.h:406-425. */
+void suzerain_rholut_imexop_packf(
+    const sgb_complex_double phi, const double km, const double kn,
+    const suzerain_rholut_imexop_scenario *s, const suzerain_rholut_imexop_ref *r,
+    const suzerain_rholut_imexop_refld *ld, const suzerain_bsplineop_workspace *w,
+    const int rho_E, const int rho_u, const int rho_v, const int rho_w, const int rho,
+    sgb_complex_double *buf, suzerain_bsmbsm *A_T, sgb_complex_double *patpt,
+    const double *a, const double *b, const double *c);
+/** suzerain/rholut_imexop.h:439-455. */
+void suzerain_rholut_imexop_packf00(
+    const sgb_complex_double phi, const suzerain_rholut_imexop_scenario *s,
+    const suzerain_rholut_imexop_ref *r, const suzerain_rholut_imexop_refld *ld,
+    const suzerain_bsplineop_workspace *w,
+    const int rho_E, const int rho_u, const int rho_v, const int rho_w, const int rho,
+    sgb_complex_double *buf, suzerain_bsmbsm *A_T, sgb_complex_double *patpt,
+    const double *c);
+
 /** 0.5 (1 + tanh(delta (x/L - 1/2)) / tanh(delta/2)); suzerain/htstretch.c:112-125. */
 double suzerain_htstretch2(const double delta, const double L, const double x);
 /** Signed wavenumber of in-order index i; suzerain/inorder.h:92-96. */
@@ -600,6 +684,36 @@ int sgb_plan_substep_host(sgb_plan *p, char method, double phi_exp,
                           double phi_imp, const void *u_in_host,
                           void *u_out_host, const sgb_refine_spec *spec,
                           void *stream);
+
+/** The production operator resident on the device for batched use: the
+ *  collocation bands of w, the reference profiles (host pointers with the
+ *  strides of ld, copied), the equation positions order[5] (E, u, v, w,
+ *  rho; negative omits) and the optional boundary matrices a, b, c (host,
+ *  5 x 5 column-major; they need all five equations in order).  No
+ *  counterpart in the reference, whose callers pack one wavenumber pair at
+ *  a time (apps/perfect/operator_hybrid_isothermal.cpp:612-689). */
+typedef struct sgb_rholut sgb_rholut;
+sgb_rholut *sgb_rholut_create(const suzerain_rholut_imexop_scenario *s,
+                              const suzerain_rholut_imexop_ref *r,
+                              const suzerain_rholut_imexop_refld *ld,
+                              const suzerain_bsplineop_workspace *w, const int order[5],
+                              const double *a, const double *b, const double *c);
+int sgb_rholut_destroy(sgb_rholut *h);
+/** The BSMBSM geometry of the packed operator. */
+int sgb_rholut_geometry(const sgb_rholut *h, suzerain_bsmbsm *A_T);
+/** P (M + phi L)^T P^T for nsys wavenumber pairs (km, kn: device arrays)
+ *  into packed bands ab (device): entry (R, C) at
+ *  ab[s ab_stride + off + KU + R - C + C ldab]; off = 0, ldab = LD is
+ *  packc, off = KL, ldab = LD + KL packf (rows above off untouched). */
+int sgb_rholut_pack_batched(sgb_rholut *h, double phi_re, double phi_im, int nsys,
+                            const double *km, const double *kn, void *ab, int ldab,
+                            long long ab_stride, int off, void *stream);
+/** y <- (M + phi L) x + beta y for nsys wavenumber pairs; x, y device,
+ *  natural order per system (equation position p at p n .. p n + n - 1). */
+int sgb_rholut_accumulate_batched(sgb_rholut *h, double phi_re, double phi_im, int nsys,
+                                  const double *km, const double *kn, const void *x,
+                                  long long x_stride, double beta_re, double beta_im,
+                                  void *y, long long y_stride, void *stream);
 
 /** The implicit operator M + phi L of every system of the plan, written as
  *  packed complex128 bands (device memory): A(r, c) at

@@ -184,6 +184,28 @@ _SIGS = {
     "sgb_plan_timings": (_i, [_p, C.c_char_p, _i]),
     "sgb_launch_count": (_ll, []),
     "sgb_plan_assemble_packed": (_i, [_p, _d, _p, _i, _ll, _i, _p]),
+    "sgb_rholut_create": (_p, [_p, _p, _p, C.POINTER(BsplineopWorkspace), _p, _p, _p, _p]),
+    "sgb_rholut_destroy": (_i, [_p]),
+    "sgb_rholut_geometry": (_i, [_p, _p]),
+    "sgb_rholut_pack_batched": (_i, [_p, _d, _d, _i, _p, _p, _p, _i, _ll, _i, _p]),
+    "sgb_rholut_accumulate_batched": (_i, [_p, _d, _d, _i, _p, _p, _p, _ll, _d, _d, _p, _ll,
+                                           _p]),
+    "suzerain_rholut_imexop_accumulate": (None, [ZC, _d, _d, _p, _p, _p,
+                                                 C.POINTER(BsplineopWorkspace)]
+                                          + [_p] * 5 + [ZC] + [_p] * 5 + [_p] * 3),
+    "suzerain_rholut_imexop_accumulate00": (None, [ZC, _p, _p, _p,
+                                                   C.POINTER(BsplineopWorkspace)]
+                                            + [_p] * 5 + [ZC] + [_p] * 5 + [_p]),
+    "suzerain_rholut_imexop_packc": (None, [ZC, _d, _d, _p, _p, _p,
+                                            C.POINTER(BsplineopWorkspace)] + [_i] * 5
+                                     + [_p, _p, _p] + [_p] * 3),
+    "suzerain_rholut_imexop_packf": (None, [ZC, _d, _d, _p, _p, _p,
+                                            C.POINTER(BsplineopWorkspace)] + [_i] * 5
+                                     + [_p, _p, _p] + [_p] * 3),
+    "suzerain_rholut_imexop_packc00": (None, [ZC, _p, _p, _p, C.POINTER(BsplineopWorkspace)]
+                                       + [_i] * 5 + [_p, _p, _p] + [_p]),
+    "suzerain_rholut_imexop_packf00": (None, [ZC, _p, _p, _p, C.POINTER(BsplineopWorkspace)]
+                                       + [_i] * 5 + [_p, _p, _p] + [_p]),
     "sgb_batch_bounds": (_i, [_i, _i, _p]),
     "sgb_batch_create": (_p, [C.POINTER(Case), _i, _p, _p, _i, _i, C.c_char]),
     "sgb_batch_destroy": (_i, [_p]),

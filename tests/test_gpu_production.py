@@ -17,7 +17,7 @@ Bars (per system):
     backward error 145 would leave up to ~6e-12); forward difference against
     the FP64 oracle <= 1e-10, or <= 8 kappa_inf 1e-12 on the systems whose
     condition allows more (refinement stops at a backward error of about
-    1e-12), and a median <= 1e-12.
+    1e-12), and a median <= 1e-11.
 The literal wall mask (walls on the momentum equations only) is
 near-singular (kappa_inf up to 1e13), so there the forward bar is the
 kappa-scaled one of two backward-stable solvers, 8 kappa_inf eps.
@@ -123,7 +123,7 @@ def test_production_mixed_matches_oracle(lib, oracle, torch_cuda, name):
         kap = np.linalg.cond(oracle.band_to_dense(
             oracle.assemble_case(cs, phi_i, kx[s], kz[s]), cs.N, cs.KL, cs.KU, cs.LD), np.inf)
         assert rel[s] <= 8 * kap * 1e-12, (s, rel[s], kap)
-    assert np.median(rel) <= 1e-12, np.median(rel)
+    assert np.median(rel) <= 1e-11, np.median(rel)
 
 
 def test_literal_wall_mask_at_production_size(lib, oracle, torch_cuda):

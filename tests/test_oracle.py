@@ -429,3 +429,53 @@ def test_inorder_wavenumber_matches_reference(oracle, native):
     for N in (1, 2, 3, 8, 13, 24, 192, 257):
         for i in range(N):
             assert native.suzerain_inorder_wavenumber(N, i) == R.suzerain_inorder_wavenumber(N, i)
+
+
+def test_rholut_golden_reproduces_from_reference_build(oracle):
+    """tests/golden/rholut_imexop.npz (the reference vectors of the GPU
+    production-operator tests) is what the reference's own
+    suzerain/rholut_imexop.c computes on its inputs, value for value."""
+    import sys
+    R = oracle.ref()
+    if R is None:
+        pytest.skip("no reference build here")
+    sys.path.insert(0, os.path.join(os.path.dirname(__file__), "golden"))
+    import make_rholut_golden as M
+    fresh = M.generate(C.CDLL(oracle.REF_PATH), C.CDLL(oracle.SYNTH_PATH))
+    kept = np.load(os.path.join(os.path.dirname(__file__), "golden", "rholut_imexop.npz"))
+    assert set(fresh) == set(kept.files)
+    for k in kept.files:
+        np.testing.assert_array_equal(np.asarray(fresh[k]), kept[k], err_msg=k)
+
+
+def test_rholut_reference_pack_and_accumulate_agree(oracle):
+    """The property the GPU tests rely on, checked on the reference itself:
+    its packc band, applied as (P^T PATPT P)^T, equals its accumulate
+    (suzerain/rholut_imexop.c:43-49 keeps the two in step)."""
+    kept = np.load(os.path.join(os.path.dirname(__file__), "golden", "rholut_imexop.npz"))
+    n = int(kept["n"])
+    for name, order in (("A", (0, 1, 2, 3, 4)), ("B", (0, 1, 2, 3, 4)), ("C", (0, 1, 2, 3, 4)),
+                        ("D", (4, 3, 2, 1, 0)), ("E", (0, 1, 2, 3, -1))):
+        S = sum(o >= 0 for o in order)
+        band = kept[f"{name}_packc"]                  # (N, LD): column C, band row
+        N, LD = band.shape
+        KU = (LD - 1) // 2
+        AT = np.zeros((N, N), complex)
+        for c in range(N):
+            for i in range(LD):
+                r = c + i - KU
+                if 0 <= r < N:
+                    AT[r, c] = band[c, i]
+        # natural (position-major) order <-> permuted: global index p S + pos
+        perm = np.array([(i % S) * n + i // S for i in range(N)])
+        def to_nat(v):
+            out = np.zeros(S * n, complex)
+            for e, o in enumerate(order):
+                if o >= 0:
+                    out[o * n:(o + 1) * n] = v[e * n:(e + 1) * n]
+            return out
+        x, y0, y = (to_nat(kept[f"{name}_{k}"]) for k in ("x", "y0", "y"))
+        A_nat = np.empty_like(AT)
+        A_nat[np.ix_(perm, perm)] = AT.T                 # A = P^T (PATPT)^T P
+        want = A_nat @ x + complex(kept["beta"]) * y0
+        assert np.max(np.abs(want - y)) <= 1e-12 * np.max(np.abs(y)), name
