@@ -288,6 +288,57 @@ int sgb_bspline_collocation_bands(int k, int nbreak, const double *breakpts,
                                   int nderiv, int *n, int *kl, int *ku,
                                   double *bands, double *abscissae);
 
+/* ---- Band assembly helpers (suzerain/blas_et_al/blasext.h, blas.h) ----- */
+
+/** B <- A (alpha D) + beta B (side 'R') or (alpha D) A + beta B (side 'L')
+ *  for a real band A (kl, ku; element (i, j) at a[(ku+i-j) inca + j lda]),
+ *  a real diagonal D (stride ldd, 0 for a constant) and a complex band B;
+ *  returns the reference's positive argument position on error;
+ *  suzerain/blas_et_al/blasext.h:1525-1540, blasext.c:2070-2141. */
+int suzerain_blasext_zgb_diag_scale_acc_d(
+    char side, int m, int n, int kl, int ku, const sgb_complex_double alpha, const double *d,
+    int ldd, const double *a, int inca, int lda, const sgb_complex_double beta,
+    sgb_complex_double *b, int incb, int ldb);
+/** The two- to five-diagonal forms, sum_k alpha_k D_k;
+ *  suzerain/blas_et_al/blasext.h:1576-1800, blasext.c:2143-2500. */
+int suzerain_blasext_zgb_ddiag_scale_acc_d(
+    char side, int m, int n, int kl, int ku, const sgb_complex_double alpha0, const double *d0,
+    int ldd0, const sgb_complex_double alpha1, const double *d1, int ldd1, const double *a,
+    int inca, int lda, const sgb_complex_double beta, sgb_complex_double *b, int incb, int ldb);
+int suzerain_blasext_zgb_dddiag_scale_acc_d(
+    char side, int m, int n, int kl, int ku, const sgb_complex_double alpha0, const double *d0,
+    int ldd0, const sgb_complex_double alpha1, const double *d1, int ldd1,
+    const sgb_complex_double alpha2, const double *d2, int ldd2, const double *a, int inca,
+    int lda, const sgb_complex_double beta, sgb_complex_double *b, int incb, int ldb);
+int suzerain_blasext_zgb_ddddiag_scale_acc_d(
+    char side, int m, int n, int kl, int ku, const sgb_complex_double alpha0, const double *d0,
+    int ldd0, const sgb_complex_double alpha1, const double *d1, int ldd1,
+    const sgb_complex_double alpha2, const double *d2, int ldd2,
+    const sgb_complex_double alpha3, const double *d3, int ldd3, const double *a, int inca,
+    int lda, const sgb_complex_double beta, sgb_complex_double *b, int incb, int ldb);
+int suzerain_blasext_zgb_dddddiag_scale_acc_d(
+    char side, int m, int n, int kl, int ku, const sgb_complex_double alpha0, const double *d0,
+    int ldd0, const sgb_complex_double alpha1, const double *d1, int ldd1,
+    const sgb_complex_double alpha2, const double *d2, int ldd2,
+    const sgb_complex_double alpha3, const double *d3, int ldd3,
+    const sgb_complex_double alpha4, const double *d4, int ldd4, const double *a, int inca,
+    int lda, const sgb_complex_double beta, sgb_complex_double *b, int incb, int ldb);
+/** B <- alpha A + beta B for a real band A and complex band B;
+ *  suzerain/blas_et_al/blas.c:1408-1421. */
+int suzerain_blas_zgb_acc_d(int m, int n, int kl, int ku, const sgb_complex_double alpha,
+                            const double *a, int lda, const sgb_complex_double beta,
+                            sgb_complex_double *b, int ldb);
+/** In-place complex128 -> complex64 (demote) and back (promote), and the
+ *  real forms; suzerain/blas_et_al/blasext.c:2780-2866. */
+int suzerain_blasext_zdemote(const int n, void *x);
+int suzerain_blasext_zpromote(const int n, void *x);
+int suzerain_blasext_ddemote(const int n, void *x);
+int suzerain_blasext_dpromote(const int n, void *x);
+/** Maximum column sum of |a_ij| over an m x n complex band;
+ *  suzerain/blas_et_al/blasext.c:2741-2778. */
+int suzerain_blasext_zgbnorm1(const int m, const int n, const int kl, const int ku,
+                              const sgb_complex_double *a, const int lda, double *norm1);
+
 /* ---- The production implicit operator (suzerain/rholut_imexop.h) ------ */
 
 /** suzerain/rholut_imexop.h:67-74. */

@@ -64,7 +64,58 @@ private:
     sgb_solver_spec s_;
 };
 
-class bsmbsm_solver {
+/** Column-major complex storage with the members of the reference's Eigen
+ *  matrices that Suzerain's operators use on a solver's LU, PAPT, PB and PX
+ *  (data(), colStride(), rows(), cols(), element access,
+ *  apps/perfect/operator_hybrid_isothermal.cpp:643-661): it owns its
+ *  elements, or views another's (the in-place solver's PAPT inside LU). */
+class cmatrix {
+public:
+    using value_type = std::complex<double>;
+    cmatrix() = default;
+    cmatrix(int rows, int cols, value_type fill = value_type(0))
+        : own_((size_t) rows * cols, fill), p_(own_.data()), rows_(rows), cols_(cols), ld_(rows)
+    {
+    }
+    static cmatrix view(value_type *p, int rows, int cols, int ld)
+    {
+        cmatrix m;
+        m.p_ = p; m.rows_ = rows; m.cols_ = cols; m.ld_ = ld;
+        return m;
+    }
+    cmatrix(cmatrix &&o) noexcept { *this = std::move(o); }
+    cmatrix &operator=(cmatrix &&o) noexcept
+    {
+        const bool owned = o.p_ == o.own_.data() && !o.own_.empty();
+        own_ = std::move(o.own_);
+        p_ = owned ? own_.data() : o.p_;
+        rows_ = o.rows_; cols_ = o.cols_; ld_ = o.ld_;
+        return *this;
+    }
+    cmatrix(const cmatrix &) = delete;
+    cmatrix &operator=(const cmatrix &) = delete;
+    value_type *data() { return p_; }
+    const value_type *data() const { return p_; }
+    int rows() const { return rows_; }
+    int cols() const { return cols_; }
+    int colStride() const { return ld_; }
+    value_type &operator()(int i, int j) { return p_[i + (size_t) j * ld_]; }
+    const value_type &operator()(int i, int j) const { return p_[i + (size_t) j * ld_]; }
+    void setConstant(value_type v)
+    {
+        for (int j = 0; j < cols_; ++j) std::fill(p_ + (size_t) j * ld_, p_ + (size_t) j * ld_ + rows_, v);
+    }
+
+private:
+    std::vector<value_type> own_;
+    value_type *p_ = nullptr;
+    int rows_ = 0, cols_ = 0, ld_ = 0;
+};
+
+/** suzerain::bsmbsm_solver: the solver is the BSMBSM geometry (as the
+ *  reference's derives from suzerain_bsmbsm, so a solver pointer is passed
+ *  where the packing routines take the geometry) plus its storage. */
+class bsmbsm_solver : public suzerain_bsmbsm {
 public:
     using complex_double = std::complex<double>;
 
@@ -74,18 +125,19 @@ public:
     static std::unique_ptr<bsmbsm_solver> build(const suzerain_bsmbsm &A,
                                                 const specification_zgbsv &spec, int nrhs);
 
-    const suzerain_bsmbsm A;
+    /** The geometry (this object viewed as its suzerain_bsmbsm base). */
+    const suzerain_bsmbsm &A;
     const specification_zgbsv spec;
 
-    // Storage (column-major).  PAPT is the packed band P A P^T with leading
-    // dimension ld_PAPT() (KL + LD for the in-place zgbsv, LD otherwise);
-    // callers fill it (e.g. with suzerain_bsmbsm_zpackc/zpackf) and call
-    // supplied_PAPT().
-    std::vector<complex_double> LU, PB;
+    // Storage (column-major), the reference's public members: LU holds the
+    // factor; PAPT the packed band P A P^T that callers fill (e.g. with
+    // suzerain_bsmbsm_zpackc/zpackf or suzerain_rholut_imexop_packc/packf,
+    // writing through PAPT.data() with leading dimension PAPT.colStride():
+    // rows KL.. of LU for the in-place zgbsv, its own LD x N otherwise)
+    // before calling supplied_PAPT(); PB the permuted right hand sides, PX
+    // the permuted solutions (PB itself for zgbsv); ipiv the pivots.
+    cmatrix LU, PAPT, PB, PX;
     std::vector<int> ipiv;
-    complex_double *PAPT() { return PAPT_; }
-    int ld_PAPT() const { return ld_PAPT_; }
-    complex_double *PX() { return PX_; }
     int nrhs() const { return nrhs_; }
 
     /** PB(:, j) = P b */
@@ -152,7 +204,7 @@ public:
     {
         check_col(j);
         return suzerain_bsmbsm_zaPxpby('T', A.S, A.n, complex_double(1),
-                                       PX_ + (size_t) j * A.N, 1, complex_double(0), x, incx);
+                                       PX.data() + (size_t) j * A.N, 1, complex_double(0), x, incx);
     }
     int demand_X(complex_double *X, int ldX, int incX = 1) const
     {
@@ -169,19 +221,19 @@ public:
 
 protected:
     bsmbsm_solver(const suzerain_bsmbsm &a, const specification_zgbsv &s, int nrhs)
-        : A(a), spec(s), PB((size_t) a.N * nrhs), ipiv(a.N), nrhs_(nrhs),
+        : suzerain_bsmbsm(a), A(*this), spec(s), PB(a.N, nrhs), ipiv(a.N), nrhs_(nrhs),
           fact_(s.equil() ? 'E' : 'N'), apprx_(0)
     {
         if (nrhs < 1) throw std::invalid_argument("nrhs must be positive");
     }
+    bsmbsm_solver(const bsmbsm_solver &) = delete;
+    bsmbsm_solver &operator=(const bsmbsm_solver &) = delete;
     virtual int solve_hook(char trans, int nrhs) = 0;
     void check_col(int j) const
     {
         if (j < 0 || j >= nrhs_) throw std::out_of_range("right hand side column");
     }
 
-    complex_double *PAPT_ = nullptr, *PX_ = nullptr;
-    int ld_PAPT_ = 0;
     int nrhs_;
     char fact_;
     int apprx_;
@@ -195,11 +247,9 @@ public:
         : bsmbsm_solver(a, s, nrhs)
     {
         if (!s.in_place()) throw std::invalid_argument("Invalid method in bsmbsm_solver_zgbsv");
-        LU.assign((size_t) (a.KL + a.LD) * a.N,
-                  complex_double(std::numeric_limits<double>::quiet_NaN()));
-        ld_PAPT_ = a.KL + a.LD;
-        PAPT_ = LU.data() + a.KL;
-        PX_ = PB.data();
+        LU = cmatrix(a.KL + a.LD, a.N, complex_double(std::numeric_limits<double>::quiet_NaN()));
+        PAPT = cmatrix::view(LU.data() + a.KL, a.LD, a.N, a.KL + a.LD);
+        PX = cmatrix::view(PB.data(), a.N, nrhs, a.N);
     }
 
 protected:
@@ -221,15 +271,14 @@ public:
     std::vector<stat> stats;
 
     bsmbsm_solver_zgbsvx(const suzerain_bsmbsm &a, const specification_zgbsv &s, int nrhs)
-        : bsmbsm_solver(a, s, nrhs), papt_((size_t) a.LD * a.N), px_((size_t) a.N * nrhs),
-          r_(a.N), c_(a.N), rwork_(a.N), ferr_(nrhs), berr_(nrhs), work_((size_t) 2 * a.N)
+        : bsmbsm_solver(a, s, nrhs), r_(a.N), c_(a.N), rwork_(a.N), ferr_(nrhs), berr_(nrhs),
+          work_((size_t) 2 * a.N)
     {
         if (s.method() != SGB_METHOD_ZGBSVX)
             throw std::invalid_argument("Invalid method in bsmbsm_solver_zgbsvx");
-        LU.assign((size_t) (2 * a.KL + a.KU + 1) * a.N, complex_double(0));
-        ld_PAPT_ = a.LD;
-        PAPT_ = papt_.data();
-        PX_ = px_.data();
+        LU = cmatrix(2 * a.KL + a.KU + 1, a.N);
+        PAPT = cmatrix(a.LD, a.N);
+        PX = cmatrix(a.N, nrhs);
     }
     char equed() const { return equed_; }
     double rcond() const { return rcond_; }
@@ -255,9 +304,10 @@ public:
 protected:
     int solve_hook(char trans, int nrhs) override
     {
-        const int info = suzerain_lapack_zgbsvx(fact_, trans, A.N, A.KL, A.KU, nrhs, PAPT_, A.LD,
-                                                LU.data(), 2 * A.KL + A.KU + 1, ipiv.data(), &equed_,
-                                                r_.data(), c_.data(), PB.data(), A.N, PX_, A.N,
+        const int info = suzerain_lapack_zgbsvx(fact_, trans, A.N, A.KL, A.KU, nrhs, PAPT.data(),
+                                                A.LD, LU.data(), 2 * A.KL + A.KU + 1, ipiv.data(),
+                                                &equed_, r_.data(), c_.data(), PB.data(), A.N,
+                                                PX.data(), A.N,
                                                 &rcond_, ferr_.data(), berr_.data(), work_.data(),
                                                 rwork_.data());
         fact_ = 'F';
@@ -266,7 +316,6 @@ protected:
     }
 
 private:
-    std::vector<complex_double> papt_, px_;
     std::vector<double> r_, c_, rwork_, ferr_, berr_;
     std::vector<complex_double> work_;
     char equed_ = 'N';
@@ -283,14 +332,13 @@ public:
     std::vector<stat> stats;
 
     bsmbsm_solver_zcgbsvx(const suzerain_bsmbsm &a, const specification_zgbsv &s, int nrhs)
-        : bsmbsm_solver(a, s, nrhs), papt_((size_t) a.LD * a.N), px_((size_t) a.N * nrhs), r_(a.N)
+        : bsmbsm_solver(a, s, nrhs), r_(a.N)
     {
         if (s.method() != SGB_METHOD_ZCGBSVX)
             throw std::invalid_argument("Invalid method in bsmbsm_solver_zcgbsvx");
-        LU.assign((size_t) (2 * a.KL + a.KU + 1) * a.N, complex_double(0));
-        ld_PAPT_ = a.LD;
-        PAPT_ = papt_.data();
-        PX_ = px_.data();
+        LU = cmatrix(2 * a.KL + a.KU + 1, a.N);
+        PAPT = cmatrix(a.LD, a.N);
+        PX = cmatrix(a.N, nrhs);
     }
     bsmbsm_solver &supplied_PAPT() override
     {
@@ -320,9 +368,9 @@ protected:
             int siter = spec.siter(), diter = spec.diter();
             double tolsc = spec.tolsc(), res = 0;
             info = suzerain_lapackext_zcgbsvx(&fact_, &apprx_, spec.aiter(), trans, A.N, A.KL, A.KU,
-                                              PAPT_, &afrob_, LU.data(), ipiv.data(),
+                                              PAPT.data(), &afrob_, LU.data(), ipiv.data(),
                                               PB.data() + (size_t) j * A.N,
-                                              PX_ + (size_t) j * A.N, &siter, &diter, &tolsc,
+                                              PX.data() + (size_t) j * A.N, &siter, &diter, &tolsc,
                                               r_.data(), &res);
             stats.push_back({fact_, apprx_, afrob_, siter, diter, tolsc, res});
         }
@@ -330,7 +378,7 @@ protected:
     }
 
 private:
-    std::vector<complex_double> papt_, px_, r_;
+    std::vector<complex_double> r_;
     double afrob_ = -1;
 };
 

@@ -475,3 +475,110 @@ def rel_resid(A_apply, x, b):
     apply, anorm = A_apply
     r = b - apply(x)
     return np.max(np.abs(r)) / (anorm * np.max(np.abs(x)) + np.max(np.abs(b)))
+
+
+# --------------------------------------------------------------------------
+# Band assembly helpers of blas_et_al (numpy restatements, pinned against the
+# reference build in tests/test_oracle.py)
+# --------------------------------------------------------------------------
+def gb_diag_scale_acc(side, m, n, kl, ku, alphas, ds, ldds, a, inca, lda, beta, b, incb, ldb):
+    """B <- A (sum_k alpha_k D_k) + beta B ('R') or (sum_k alpha_k D_k) A +
+    beta B ('L') on flat band storage, element (i, j) at (ku+i-j) inc + j ld
+    (suzerain/blas_et_al/blasext.c:2070-2500).  Returns the new b."""
+    b = np.array(b, dtype=np.complex128, copy=True)
+    beta = complex(beta)
+    if all(complex(al) == 0 for al in alphas) and beta == 1 or m <= 0 or n <= 0:
+        return b
+    # side 'L' walks rows 0..n-1 and columns 0..m-1 (the reference recasts a
+    # left scaling as a traversal by rows without exchanging m and n)
+    rows, cols = (n, m) if side.upper() == "L" else (m, n)
+    for j in range(cols):
+        for i in range(max(0, j - ku), min(rows, j + kl + 1)):
+            s = i if side.upper() == "L" else j
+            tmp = sum(complex(al) * d[s * l] for al, d, l in zip(alphas, ds, ldds))
+            av = a[(ku + i - j) * inca + j * lda]
+            ib = (ku + i - j) * incb + j * ldb
+            if beta == 1:
+                b[ib] += tmp * av
+            elif beta == 0:
+                b[ib] = tmp * av
+            else:
+                b[ib] = b[ib] * beta + tmp * av
+    return b
+
+
+def gbnorm1(m, n, kl, ku, a, lda):
+    """Maximum column sum of |a_ij| of a complex band (blasext.c:2741-2778)."""
+    best = 0.0
+    for j in range(n):
+        lo, hi = max(0, ku - j), ku + min(kl + 1, m - j)
+        best = max(best, float(np.sum(np.abs(a[j * lda + lo:j * lda + hi]))))
+    return best
+
+
+def zcgbsvx_call(fn, ab, n, kl, ku, b, state, trans="N", aiter=5, siter=25, diter=5,
+                 tolsc=1.0):
+    """One call of any zcgbsvx implementation with the reference's 18
+    arguments (this restatement's orc_zcgbsvx, the reference build's
+    suzerain_lapackext_zcgbsvx, or a drop-in of it), carrying the caller's
+    state across calls the way bsmbsm_solver_zcgbsvx does
+    (suzerain/bsmbsm_solver.cpp:377-414): state holds fact, apprx, afb and
+    ipiv and is updated in place.  Returns the call's outputs."""
+    ldafb = 2 * kl + ku + 1
+    if "afb" not in state:
+        state.update(fact="N", apprx=0, afb=np.zeros(ldafb * n, np.complex128),
+                     ipiv=np.zeros(n, np.int32))
+    fact = C.create_string_buffer(state["fact"].encode(), 1)
+    apprx = C.c_int(int(state["apprx"]))
+    afrob = C.c_double(-1)
+    x = np.zeros(n, np.complex128)
+    r = np.zeros(n, np.complex128)
+    si, di = C.c_int(siter), C.c_int(diter)
+    ts, res = C.c_double(tolsc), C.c_double(0)
+    abc = np.ascontiguousarray(ab, dtype=np.complex128).copy()
+    bb = np.ascontiguousarray(b, dtype=np.complex128).copy()
+    info = fn(C.addressof(fact), C.addressof(apprx), C.c_int(aiter), C.c_char(trans.encode()),
+              C.c_int(n), C.c_int(kl), C.c_int(ku), C.c_void_p(abc.ctypes.data),
+              C.addressof(afrob), C.c_void_p(state["afb"].ctypes.data),
+              C.c_void_p(state["ipiv"].ctypes.data), C.c_void_p(bb.ctypes.data),
+              C.c_void_p(x.ctypes.data), C.addressof(si), C.addressof(di), C.addressof(ts),
+              C.c_void_p(r.ctypes.data), C.addressof(res))
+    state["fact"] = fact.raw.decode()
+    state["apprx"] = apprx.value
+    return dict(info=info, fact=state["fact"], apprx=apprx.value, siter=si.value,
+                diter=di.value, tolsc=ts.value, res=res.value, x=x)
+
+
+def reuse_sequence(fn, n=120, kl=7, ku=5, seed=77):
+    """A series of slightly (then strongly) changed bands solved with the
+    factor of the first reused as an approximate factor, as a solver with
+    the reuse=true specification does: call 0 factors (fact 'N'), calls 1-2
+    reuse it for perturbed bands (apprx set), call 3 perturbs enough that
+    refinement stalls and the approximate factor is replaced, call 4
+    supplies the complex128 factor of a call that ran with siter < 0
+    (fact 'D').  Returns the per-call outputs."""
+    rng = np.random.default_rng(seed)
+    ld = kl + ku + 1
+    base = np.zeros(ld * n, np.complex128)
+    for j in range(n):
+        for i in range(max(0, j - ku), min(n, j + kl + 1)):
+            base[ku + i - j + j * ld] = complex(rng.normal(), rng.normal())
+        base[ku + j * ld] += 3 * ld
+    noise = rng.normal(size=ld * n) + 1j * rng.normal(size=ld * n)
+    mask = base != 0
+    bands = [base, base + 1e-3 * noise * mask, base + 3e-3 * noise * mask,
+             base + 0.6 * ld * noise * mask]
+    rhs = [rng.normal(size=n) + 1j * rng.normal(size=n) for _ in range(5)]
+    state = {}
+    out = []
+    for k, (band, b) in enumerate(zip(bands, rhs)):
+        if k > 0:
+            state["apprx"] = 1                    # the factor is of an earlier band
+        out.append(zcgbsvx_call(fn, band, n, kl, ku, b, state, aiter=3, siter=25, diter=5,
+                                tolsc=1.0))
+    # fact 'D': factor in complex128 (siter < 0), then reuse that factor
+    dstate = {}
+    out.append(zcgbsvx_call(fn, bands[1], n, kl, ku, rhs[4], dstate, siter=-1, diter=5))
+    dstate["apprx"] = 1
+    out.append(zcgbsvx_call(fn, bands[2], n, kl, ku, rhs[4], dstate, siter=-1, diter=5))
+    return out

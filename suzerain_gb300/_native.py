@@ -184,6 +184,24 @@ _SIGS = {
     "sgb_plan_timings": (_i, [_p, C.c_char_p, _i]),
     "sgb_launch_count": (_ll, []),
     "sgb_plan_assemble_packed": (_i, [_p, _d, _p, _i, _ll, _i, _p]),
+    "suzerain_blasext_zgb_diag_scale_acc_d": (_i, [C.c_char, _i, _i, _i, _i] + [ZC, _p, _i]
+                                              + [_p, _i, _i, ZC, _p, _i, _i]),
+    "suzerain_blasext_zgb_ddiag_scale_acc_d": (_i, [C.c_char, _i, _i, _i, _i] + [ZC, _p, _i] * 2
+                                               + [_p, _i, _i, ZC, _p, _i, _i]),
+    "suzerain_blasext_zgb_dddiag_scale_acc_d": (_i, [C.c_char, _i, _i, _i, _i] + [ZC, _p, _i] * 3
+                                                + [_p, _i, _i, ZC, _p, _i, _i]),
+    "suzerain_blasext_zgb_ddddiag_scale_acc_d": (_i, [C.c_char, _i, _i, _i, _i]
+                                                 + [ZC, _p, _i] * 4
+                                                 + [_p, _i, _i, ZC, _p, _i, _i]),
+    "suzerain_blasext_zgb_dddddiag_scale_acc_d": (_i, [C.c_char, _i, _i, _i, _i]
+                                                  + [ZC, _p, _i] * 5
+                                                  + [_p, _i, _i, ZC, _p, _i, _i]),
+    "suzerain_blas_zgb_acc_d": (_i, [_i, _i, _i, _i, ZC, _p, _i, ZC, _p, _i]),
+    "suzerain_blasext_zdemote": (_i, [_i, _p]),
+    "suzerain_blasext_zpromote": (_i, [_i, _p]),
+    "suzerain_blasext_ddemote": (_i, [_i, _p]),
+    "suzerain_blasext_dpromote": (_i, [_i, _p]),
+    "suzerain_blasext_zgbnorm1": (_i, [_i, _i, _i, _i, _p, _i, _p]),
     "sgb_rholut_create": (_p, [_p, _p, _p, C.POINTER(BsplineopWorkspace), _p, _p, _p, _p]),
     "sgb_rholut_destroy": (_i, [_p]),
     "sgb_rholut_geometry": (_i, [_p, _p]),

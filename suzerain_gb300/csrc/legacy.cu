@@ -17,49 +17,7 @@
 
 using namespace sgb;
 
-namespace {
-
-bool is_device_ptr(const void *p)
-{
-    if (!p) return false;
-    cudaPointerAttributes a;
-    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) { cudaGetLastError(); return false; }
-    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
-}
-
-// A user buffer mirrored in device memory for the duration of one call.
-struct Stage {
-    void *user = nullptr, *dev = nullptr;
-    size_t bytes = 0;
-    bool owned = false;
-    cudaError_t err = cudaSuccess;
-    Stage(const void *u, size_t b, bool copy_in) : user(const_cast<void *>(u)), bytes(b)
-    {
-        if (!u || b == 0) return;
-        if (is_device_ptr(u)) { dev = user; return; }
-        err = cudaMalloc(&dev, b);
-        if (err != cudaSuccess) { dev = nullptr; return; }
-        owned = true;
-        if (copy_in) err = cudaMemcpy(dev, u, b, cudaMemcpyHostToDevice);
-    }
-    cudaError_t back()
-    {
-        if (owned && err == cudaSuccess) return cudaMemcpy(user, dev, bytes, cudaMemcpyDeviceToHost);
-        return err;
-    }
-    ~Stage() { if (owned && dev) cudaFree(dev); }
-    Stage(const Stage &) = delete;
-    Stage &operator=(const Stage &) = delete;
-};
-
-size_t span_bytes(int n, int inc, size_t el) { return n <= 0 ? 0 : ((size_t) (n - 1) * std::abs(inc) + 1) * el; }
-
-int err_of(cudaError_t e, const char *what)
-{
-    return e == cudaSuccess ? 0 : sgb_set_error(e, what, __FILE__, __LINE__);
-}
-
-}  // namespace
+#include "sgb_stage.h"
 
 // ---------------------------------------------------------------------------
 // BSMBSM geometry and permutation
@@ -849,6 +807,12 @@ extern "C" int suzerain_lapack_zgbsvx(const char fact_in, const char trans_in, c
 // ---------------------------------------------------------------------------
 // zcgbsvx (one system through the batched driver)
 // ---------------------------------------------------------------------------
+extern "C" int suzerain_blas_zgbmv(const char trans_, const int m, const int n, const int kl,
+                                   const int ku, const sgb_complex_double alpha,
+                                   const sgb_complex_double *a, const int lda,
+                                   const sgb_complex_double *x, const int incx,
+                                   const sgb_complex_double beta, sgb_complex_double *y,
+                                   const int incy);
 namespace {
 struct ZcWork {
     std::mutex mu;
@@ -857,6 +821,220 @@ struct ZcWork {
     double2 *bx = nullptr; size_t bx_n = 0;   // b, x staging
 };
 ZcWork g_zcw;
+
+// Small single-system vector kernels of the supplied-factor path.
+__global__ void k_nrm2_1(int n, const double2 *__restrict__ v, double *__restrict__ out)
+{
+    __shared__ double part[256];
+    double s = 0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s = fma(v[i].x, v[i].x, fma(v[i].y, v[i].y, s));
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w; w >>= 1) {
+        if ((int) threadIdx.x < w) part[threadIdx.x] += part[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = sqrt(part[0]);
+}
+__global__ void k_band_frob_1(int n, int kl, int ku, const double2 *__restrict__ ab, int ldab,
+                              double *__restrict__ out)
+{
+    __shared__ double part[256];
+    double s = 0;
+    for (long long t = threadIdx.x; t < (long long) n * ldab; t += blockDim.x) {
+        const int j = (int) (t / ldab), r = (int) (t - (long long) j * ldab), i = j + r - ku;
+        if (r <= kl + ku && i >= 0 && i < n) s = fma(ab[t].x, ab[t].x, fma(ab[t].y, ab[t].y, s));
+    }
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w; w >>= 1) {
+        if ((int) threadIdx.x < w) part[threadIdx.x] += part[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = sqrt(part[0]);
+}
+__global__ void k_vec_op(int n, int op, const double2 *__restrict__ a, double2 *__restrict__ y,
+                         float2 *__restrict__ f)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    switch (op) {
+    case 0: y[i] = make_double2(0, 0); break;                              // y = 0
+    case 1: y[i] = a[i]; break;                                           // y = a
+    case 2: y[i] = make_double2(y[i].x + a[i].x, y[i].y + a[i].y); break; // y += a
+    case 3: f[i] = make_float2((float) a[i].x, (float) a[i].y); break;    // f = (float) a
+    case 4: y[i] = make_double2(f[i].x, f[i].y); break;                   // y = (double) f
+    default: y[i] = make_double2(NAN, NAN); break;                        // y = NaN
+    }
+}
+// afb rows kl.. <- the band ab (rows 0..kl+ku), rows 0..kl-1 <- 0: the
+// reference's DLACPY('F', ldab, n, ab, ldab, afb + kl, ldafb) before gbtrf
+__global__ void k_band_to_afb(int n, int kl, int ku, const double2 *__restrict__ ab,
+                              double2 *__restrict__ afb)
+{
+    const int ldab = kl + ku + 1, ldafb = 2 * kl + ku + 1;
+    const long long t = (long long) blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long) n * ldafb) return;
+    const int j = (int) (t / ldafb), r = (int) (t - (long long) j * ldafb);
+    afb[t] = r >= kl ? ab[(long long) j * ldab + r - kl] : make_double2(0, 0);
+}
+
+// *fact 'S' or 'D': refinement with the caller's factor in afb (complex64
+// LAPACK storage at the start of afb for 'S', complex128 for 'D') and its
+// pivots, the control flow of suzerain/blas_et_al/dsgbsvx.def:130-313: with
+// *apprx set, a stall blames the factor and the call starts over with a
+// fresh factorization (fact 'N', the full iteration budgets).
+int zcgbsvx_supplied(char *const fact, int *const apprx, const int aiter, char trans, const int n,
+                     const int kl, const int ku, sgb_complex_double *const ab, double *const afrob,
+                     sgb_complex_double *const afb, int *const ipiv,
+                     sgb_complex_double *const b, sgb_complex_double *const x,
+                     int *const siter, int *const diter, double *const tolsc,
+                     sgb_complex_double *const r, double *const res)
+{
+    const int ldab = kl + ku + 1, ldafb = 2 * kl + ku + 1;
+    if (!afb || !ipiv) return err_of(cudaErrorInvalidValue, "zcgbsvx: a supplied factor needs afb and ipiv");
+    Stage sab(ab, (size_t) ldab * n * sizeof(double2), true);
+    Stage sb(b, (size_t) n * sizeof(double2), true);
+    Stage sx(x, (size_t) n * sizeof(double2), false);
+    Stage sf(afb, (size_t) ldafb * n * sizeof(double2), true);
+    Stage sp(ipiv, (size_t) n * sizeof(int), true);
+    for (Stage *st : {&sab, &sb, &sx, &sf, &sp})
+        if (st->err != cudaSuccess) return err_of(st->err, "zcgbsvx staging");
+    double2 *A = (double2 *) sab.dev, *B = (double2 *) sb.dev, *X = (double2 *) sx.dev;
+    double2 *R = nullptr, *Y = nullptr;
+    double *dn = nullptr;
+    cudaError_t e = cudaMalloc(&R, 2 * (size_t) n * sizeof(double2));
+    if (e == cudaSuccess) e = cudaMalloc(&dn, sizeof(double));
+    if (e != cudaSuccess) { cudaFree(R); return err_of(e, "zcgbsvx scratch"); }
+    Y = R + n;                                   // complex64 copy of r lives in Y's bytes
+    float2 *F = reinterpret_cast<float2 *>(Y);
+    const unsigned EB = (unsigned) ((n + 255) / 256);
+    auto vec = [&](int op, const double2 *a, double2 *y) {
+        k_vec_op<<<EB, 256>>>(n, op, a, y, F);
+        return cudaGetLastError();
+    };
+    auto nrm2 = [&](const double2 *v, double &out) {
+        k_nrm2_1<<<1, 256>>>(n, v, dn);
+        cudaError_t ee = cudaGetLastError();
+        if (ee == cudaSuccess) ee = cudaMemcpy(&out, dn, sizeof(double), cudaMemcpyDeviceToHost);
+        return ee;
+    };
+    const sgb_complex_double one(1.0), mone(-1.0);
+    // r = b - op(A) x and ||r||_2
+    auto residual = [&](double &rn) -> cudaError_t {
+        cudaError_t ee = vec(1, B, R);
+        if (ee != cudaSuccess) return ee;
+        if (suzerain_blas_zgbmv(trans, n, n, kl, ku, mone, (sgb_complex_double *) A, ldab,
+                                (sgb_complex_double *) X, 1, one, (sgb_complex_double *) R, 1))
+            return cudaErrorUnknown;
+        return nrm2(R, rn);
+    };
+    const double eps = 1.1102230246251565e-16;   // dlamch('E')
+    int info = 0;
+    double rn = 0, xn = 0;
+    e = vec(0, nullptr, X);                      // x = 0, r = b
+    if (e == cudaSuccess) e = vec(1, B, R);
+    if (e == cudaSuccess) e = nrm2(R, rn);
+    const double resdecay = 2;
+    double lastres = (resdecay + 1) * (rn + 1);
+    const bool use_eps = (*tolsc == 0.0);
+    double tolconst = 1, tol = eps;
+    if (e == cudaSuccess && !use_eps) {
+        if (*afrob < 0) {
+            k_band_frob_1<<<1, 256>>>(n, kl, ku, A, ldab, dn);
+            e = cudaGetLastError();
+            if (e == cudaSuccess) e = cudaMemcpy(afrob, dn, sizeof(double), cudaMemcpyDeviceToHost);
+        }
+        tolconst = *afrob * eps * std::sqrt((double) n) * (*tolsc);
+        tol = 0;
+    }
+    const int smax = *siter, dmax = *diter;
+    *siter = -1; *diter = -1;
+    bool restart = false;
+    if (e == cudaSuccess && smax >= 0 && *fact != 'D' && rn > tol) {      // single, supplied
+        while (e == cudaSuccess && *siter < smax && rn > tol) {
+            *siter += 1;
+            e = vec(3, R, nullptr);
+            if (e == cudaSuccess &&
+                suzerain_lapack_cgbtrs(trans, n, kl, ku, 1, (const sgb_complex_float *) sf.dev,
+                                       ldafb, (const int *) sp.dev, (sgb_complex_float *) F, n))
+                e = cudaErrorUnknown;
+            if (e == cudaSuccess) e = vec(4, nullptr, R);
+            if (e == cudaSuccess) e = vec(2, R, X);
+            if (e == cudaSuccess && !use_eps) e = nrm2(X, xn);
+            tol = (use_eps ? eps : xn) * tolconst;
+            if (e == cudaSuccess) e = residual(rn);
+            if (e != cudaSuccess) break;
+            if (std::isnan(rn)) { info = -1; break; }
+            if (*siter >= aiter && lastres < rn * resdecay) {
+                if (*apprx) { restart = true; break; }   // blame the approximate factor
+                break;                                   // blame single precision
+            }
+            lastres = rn;
+        }
+    } else if (e == cudaSuccess) {
+        *siter = 0;
+    }
+    if (e == cudaSuccess && !restart && !info && dmax >= 0 && rn > tol) {  // double
+        if (*fact != 'D') {
+            *fact = 'D';
+            *apprx = 0;
+            k_band_to_afb<<<(unsigned) (((long long) n * ldafb + 255) / 256), 256>>>(
+                n, kl, ku, A, (double2 *) sf.dev);
+            e = cudaGetLastError();
+            if (e == cudaSuccess) {
+                const int fi = suzerain_lapack_zgbtrf(n, n, kl, ku, (sgb_complex_double *) sf.dev,
+                                                      ldafb, (int *) sp.dev);
+                if (fi > 0) info = fi;
+                else if (fi < 0) e = cudaErrorUnknown;
+            }
+        }
+        while (e == cudaSuccess && !info && *diter < dmax && rn > tol) {
+            *diter += 1;
+            if (suzerain_lapack_zgbtrs(trans, n, kl, ku, 1, (const sgb_complex_double *) sf.dev,
+                                       ldafb, (const int *) sp.dev, (sgb_complex_double *) R, n))
+                e = cudaErrorUnknown;
+            if (e == cudaSuccess) e = vec(2, R, X);
+            if (e == cudaSuccess && !use_eps) e = nrm2(X, xn);
+            tol = (use_eps ? eps : xn) * tolconst;
+            if (e == cudaSuccess) e = residual(rn);
+            if (e != cudaSuccess) break;
+            if (std::isnan(rn)) { info = -1; break; }
+            if (*diter >= aiter && lastres < rn * resdecay) {
+                if (*apprx) { restart = true; break; }   // blame the approximate factor
+                break;                                   // blame the problem
+            }
+            lastres = rn;
+        }
+    } else if (e == cudaSuccess && !restart && !info) {
+        *diter = 0;
+    }
+    if (e == cudaSuccess && !restart && std::isnan(rn)) e = vec(5, nullptr, X);
+    if (e == cudaSuccess && r && !restart) {
+        Stage sr(r, (size_t) n * sizeof(double2), false);
+        e = sr.err;
+        if (e == cudaSuccess) e = cudaMemcpy(sr.dev, R, n * sizeof(double2), cudaMemcpyDeviceToDevice);
+        if (e == cudaSuccess) e = sr.back();
+    }
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    cudaFree(R);
+    cudaFree(dn);
+    if (e != cudaSuccess) return err_of(e, "suzerain_lapackext_zcgbsvx (supplied factor)");
+    if (restart) {
+        *fact = 'N';
+        *siter = smax;
+        *diter = dmax;
+        return suzerain_lapackext_zcgbsvx(fact, apprx, aiter, trans, n, kl, ku, ab, afrob, afb,
+                                          ipiv, b, x, siter, diter, tolsc, r, res);
+    }
+    e = sx.back();
+    if (e == cudaSuccess) e = sf.back();
+    if (e == cudaSuccess) e = sp.back();
+    if (e != cudaSuccess) return err_of(e, "zcgbsvx outputs");
+    *res = rn;
+    *tolsc = rn == 0 ? 0 : rn / tol;
+    return info;
+}
 }  // namespace
 
 extern "C" int suzerain_lapackext_zcgbsvx(char *const fact, int *const apprx, const int aiter,
@@ -880,10 +1058,9 @@ extern "C" int suzerain_lapackext_zcgbsvx(char *const fact, int *const apprx, co
     else if (*tolsc < 0) info = -16;
     else if (*siter < 0 && *diter < 0) info = -99;
     if (info) return info;
-    if (*fact != 'N') {
-        sgb_set_error(cudaErrorNotSupported, "suzerain_lapackext_zcgbsvx: a supplied factor (fact 'S'/'D') is refactored", __FILE__, __LINE__);
-        *fact = 'N';
-    }
+    if (*fact != 'N' && n > 0)                   // the caller's factor (reuse)
+        return zcgbsvx_supplied(fact, apprx, aiter, trans, n, kl, ku, ab, afrob, afb, ipiv, b, x,
+                                siter, diter, tolsc, r, res);
     *apprx = 0;
     if (n == 0) { *siter = 0; *diter = 0; *tolsc = 0; *res = 0; return 0; }
     if (kl + 1 > 64 || kl + ku + 1 > 192) return -6;

@@ -43,7 +43,8 @@ int main()
             for (int j = 0; j < S; ++j) {
                 const int rc = spec.in_place()
                     ? suzerain_bsmbsm_zpackf(&A, i, j, cd(1), B[i * S + j].data(), solver->LU.data())
-                    : suzerain_bsmbsm_zpackc(&A, i, j, cd(1), B[i * S + j].data(), solver->PAPT());
+                    : suzerain_bsmbsm_zpackc(solver.get(), i, j, cd(1), B[i * S + j].data(),
+                                             solver->PAPT.data());
                 if (rc) { std::printf("FAIL pack %d\n", rc); return 1; }
             }
         solver->supplied_PAPT();
@@ -71,6 +72,64 @@ int main()
         }
     }
     if (worst > 1e-13) { std::printf("FAIL berr %.3e\n", worst); return 1; }
+
+    // The production operator the way apps/perfect/operator_hybrid_isothermal.cpp
+    // drives the solver (:636-661): pack (M + phi L)^T with the rholut drop-ins
+    // straight into the solver's storage through solver.get() as the geometry
+    // and LU.data() / PAPT.data(), supplied_PAPT(), solve with trans 'T';
+    // the solution satisfies the operator's own accumulate.
+    {
+        const double bp[] = {0.0, 0.5, 1.5, 2.25, 2.5, 3.0, 3.35};
+        suzerain_bsplineop_workspace *w = sgb_bsplineop_alloc_breakpoints(6, 7, bp, 2);
+        const int nn = w->n, NN = 5 * nn;
+        suzerain_rholut_imexop_scenario sc{3000, 0.7, 1.5, 3, 1.4};
+        std::vector<double> prof(26 * nn);
+        for (auto &v : prof) v = 0.5 + std::abs(nd(rng)) * 0.2;
+        suzerain_rholut_imexop_ref ref;
+        suzerain_rholut_imexop_refld rld;
+        for (int k = 0; k < 26; ++k) {
+            reinterpret_cast<double **>(&ref)[k] = prof.data() + k * nn;
+            reinterpret_cast<int *>(&rld)[k] = 1;
+        }
+        const cd phi(0.02, 0.01);
+        const double km = 2.5, kn = -1.5;
+        std::vector<cd> u(NN), y(NN), xs(NN), y2(NN);
+        for (auto &v : u) v = cd(nd(rng), nd(rng));
+        suzerain_rholut_imexop_accumulate(phi, km, kn, &sc, &ref, &rld, w, &u[0], &u[nn], &u[2 * nn],
+                                          &u[3 * nn], &u[4 * nn], cd(0), &y[0], &y[nn], &y[2 * nn],
+                                          &y[3 * nn], &y[4 * nn], nullptr, nullptr, nullptr);
+        const suzerain_bsmbsm AA = suzerain_bsmbsm_construct(5, nn, w->max_kl, w->max_ku);
+        std::vector<cd> buf((size_t) std::max(75, nn * (w->max_kl + 1 + w->max_ku)));
+        for (const char *text : {"zgbsv", "zcgbsvx,aiter=5,siter=25,diter=5,tolsc=0"}) {
+            suzerain_gb300::specification_zgbsv spec(text);
+            auto solver = suzerain_gb300::bsmbsm_solver::build(AA, spec, 1);
+            if (solver->spec.in_place())
+                suzerain_rholut_imexop_packf(phi, km, kn, &sc, &ref, &rld, w, 0, 1, 2, 3, 4,
+                                             buf.data(), solver.get(), solver->LU.data(),
+                                             nullptr, nullptr, nullptr);
+            else
+                suzerain_rholut_imexop_packc(phi, km, kn, &sc, &ref, &rld, w, 0, 1, 2, 3, 4,
+                                             buf.data(), solver.get(), solver->PAPT.data(),
+                                             nullptr, nullptr, nullptr);
+            if (solver->PAPT.colStride() != (solver->spec.in_place() ? AA.KL + AA.LD : AA.LD)) {
+                std::printf("FAIL PAPT colStride\n");
+                return 1;
+            }
+            solver->supplied_PAPT();
+            solver->supply_b(y.data(), 0);
+            solver->solve('T');
+            solver->demand_x(xs.data(), 0);
+            suzerain_rholut_imexop_accumulate(phi, km, kn, &sc, &ref, &rld, w, &xs[0], &xs[nn],
+                                              &xs[2 * nn], &xs[3 * nn], &xs[4 * nn], cd(0),
+                                              &y2[0], &y2[nn], &y2[2 * nn], &y2[3 * nn],
+                                              &y2[4 * nn], nullptr, nullptr, nullptr);
+            double r = 0, ym = 0;
+            for (int i = 0; i < NN; ++i) { r = std::max(r, std::abs(y2[i] - y[i])); ym = std::max(ym, std::abs(y[i])); }
+            std::printf("rholut %s: |A x - y| / |y| = %.3e\n", text, r / ym);
+            if (!(r <= 1e-12 * ym)) { std::printf("FAIL rholut %s\n", text); return 1; }
+        }
+        suzerain_bsplineop_free(w);
+    }
     // an invalid specification is rejected with the reference's message
     try {
         suzerain_gb300::specification_zgbsv bad("zcgbsvx,aiter");

@@ -1059,3 +1059,17 @@ def test_cpp_solver_shim_runs(lib, tmp_path):
     assert r.returncode == 0, r.stderr
     r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
     assert r.returncode == 0 and "OK" in r.stdout, r.stdout + r.stderr
+
+
+def test_dropin_zcgbsvx_factor_reuse_sequence(lib, oracle):
+    """suzerain_lapackext_zcgbsvx with the caller's factor (fact 'S'/'D',
+    apprx): over a series of perturbed bands the GPU drop-in makes the same
+    decisions as the oracle (pinned to the reference build), call for call:
+    reuse of the approximate factor, the restart with a fresh factor when
+    refinement with it stalls, refinement with a supplied complex128 factor."""
+    got = oracle.reuse_sequence(lib.suzerain_lapackext_zcgbsvx)
+    want = oracle.reuse_sequence(oracle.lib().orc_zcgbsvx)
+    for k, (g, w) in enumerate(zip(got, want)):
+        for key in ("info", "fact", "apprx", "siter", "diter"):
+            assert g[key] == w[key], (k, key, g[key], w[key])
+        assert np.max(np.abs(g["x"] - w["x"])) <= 1e-11 * np.max(np.abs(w["x"])), k

@@ -479,3 +479,101 @@ def test_rholut_reference_pack_and_accumulate_agree(oracle):
         A_nat[np.ix_(perm, perm)] = AT.T                 # A = P^T (PATPT)^T P
         want = A_nat @ x + complex(kept["beta"]) * y0
         assert np.max(np.abs(want - y)) <= 1e-12 * np.max(np.abs(y)), name
+
+
+DIAG_NAMES = {1: "zgb_diag_scale_acc_d", 2: "zgb_ddiag_scale_acc_d", 3: "zgb_dddiag_scale_acc_d",
+              4: "zgb_ddddiag_scale_acc_d", 5: "zgb_dddddiag_scale_acc_d"}
+
+
+def ref_diag_scale_acc(R, K, side, m, n, kl, ku, alphas, ds, ldds, a, inca, lda, beta, b, incb,
+                       ldb):
+    """The reference's own suzerain_blasext_zgb_<K>diag_scale_acc_d on copies."""
+    from oracle import oracle
+    f = getattr(R, "suzerain_blasext_" + DIAG_NAMES[K])
+    Z, P, I = oracle._Z, C.c_void_p, C.c_int
+    f.argtypes = [C.c_char, I, I, I, I] + [Z, P, I] * K + [P, I, I, Z, P, I, I]
+    f.restype = I
+    bb = np.array(b, dtype=np.complex128, copy=True)
+    args = []
+    for al, d, l in zip(alphas, ds, ldds):
+        args += [oracle._z(al), d.ctypes.data if d is not None else None, l]
+    rc = f(side.encode(), m, n, kl, ku, *args, a.ctypes.data, inca, lda, oracle._z(beta),
+           bb.ctypes.data, incb, ldb)
+    return rc, bb
+
+
+@pytest.mark.parametrize("K", [1, 2, 3, 4, 5])
+@pytest.mark.parametrize("side", ["R", "L"])
+@pytest.mark.parametrize("beta", [1.0, 0.0, 0.5 - 0.25j])
+def test_diag_scale_acc_restatement_matches_reference(oracle, K, side, beta):
+    """oracle.gb_diag_scale_acc equals the reference's blasext routines
+    (rectangular band, row strides, a constant diagonal)."""
+    R = oracle.ref()
+    if R is None:
+        pytest.skip("no reference build here")
+    rng = np.random.default_rng(K * 10 + (side == "L"))
+    # a rectangular band for side 'R'; the reference walks side 'L' over
+    # rows 0..n-1 and columns 0..m-1, which only a square band keeps inside
+    # its storage
+    m, n, kl, ku, inca, incb = (9, 7, 2, 3, 1, 1) if side == "R" else (8, 8, 2, 3, 1, 1)
+    lda, ldb = kl + ku + 2, kl + ku + 3
+    a = rng.normal(size=lda * n + 4)
+    b = rng.normal(size=ldb * n + 4) + 1j * rng.normal(size=ldb * n + 4)
+    alphas = [complex(rng.normal(), rng.normal()) for _ in range(K)]
+    ds = [rng.normal(size=3 * max(m, n)) for _ in range(K)]
+    ldds = [1, 2, 0, 3, 1][:K]
+    rc, want = ref_diag_scale_acc(R, K, side, m, n, kl, ku, alphas, ds, ldds, a, inca, lda, beta,
+                                  b, incb, ldb)
+    assert rc == 0
+    got = oracle.gb_diag_scale_acc(side, m, n, kl, ku, alphas, ds, ldds, a, inca, lda, beta, b,
+                                   incb, ldb)
+    np.testing.assert_allclose(got, want, rtol=1e-15, atol=1e-15)
+
+
+def test_diag_scale_acc_error_positions_of_reference(oracle):
+    """The argument positions the reference returns, which the GPU drop-ins
+    reproduce (tests/test_gpu_blasext.py): kl 4, ku 5, ldd_k 8 + 3k,
+    inca 7 + 3K, lda 8 + 3K, incb 11 + 3K, ldb (lda for K >= 2) 12 + 3K,
+    side 1."""
+    R = oracle.ref()
+    if R is None:
+        pytest.skip("no reference build here")
+    a = np.zeros(64)
+    b = np.zeros(64, complex)
+    d = np.zeros(16)
+    for K in range(1, 6):
+        base = dict(side="R", m=4, n=4, kl=1, ku=1, alphas=[1] * K, ds=[d] * K, ldds=[1] * K,
+                    inca=1, lda=3, beta=1, incb=1, ldb=3)
+
+        def rc(**over):
+            kw = {**base, **over}
+            return ref_diag_scale_acc(R, K, kw["side"], kw["m"], kw["n"], kw["kl"], kw["ku"],
+                                      kw["alphas"], kw["ds"], kw["ldds"], a, kw["inca"],
+                                      kw["lda"], kw["beta"], b, kw["incb"], kw["ldb"])[0]
+        assert rc(kl=-1) == 4 and rc(ku=-1) == 5
+        for k in range(K):
+            assert rc(ldds=[1] * k + [-1] + [1] * (K - k - 1)) == 8 + 3 * k
+        assert rc(inca=0) == 7 + 3 * K and rc(lda=2) == 8 + 3 * K
+        assert rc(incb=0) == 11 + 3 * K
+        assert rc(ldb=2) == (12 + 3 * K if K == 1 else 0)
+        assert rc(side="X") == 1
+
+
+def test_zcgbsvx_factor_reuse_sequence_matches_reference(oracle):
+    """Factor reuse (fact 'S'/'D' supplied, apprx set) over a series of
+    perturbed bands: the restatement makes the reference's decisions call
+    for call, including the restart with a fresh factor when refinement with
+    the approximate one stalls (suzerain/blas_et_al/dsgbsvx.def:214-227)."""
+    R = oracle.ref()
+    if R is None:
+        pytest.skip("no reference build here")
+    got = oracle.reuse_sequence(oracle.lib().orc_zcgbsvx)
+    want = oracle.reuse_sequence(R.suzerain_lapackext_zcgbsvx)
+    for k, (g, w) in enumerate(zip(got, want)):
+        for key in ("info", "fact", "apprx", "siter", "diter"):
+            assert g[key] == w[key], (k, key, g[key], w[key])
+        assert np.max(np.abs(g["x"] - w["x"])) <= 1e-12 * np.max(np.abs(w["x"])), k
+    # the sequence exercises reuse, the stall restart and a supplied factor
+    assert [g["apprx"] for g in got[:4]] == [0, 1, 1, 0]
+    assert got[1]["siter"] > got[0]["siter"] and got[3]["fact"] == "S"
+    assert got[5]["fact"] == "D" and got[5]["diter"] > 0
