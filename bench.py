@@ -515,6 +515,18 @@ def run_ours(args):
             extras["packed_path"] = run_packed(cfg, cs, kx, kz, u, phi_i, args, peak)
         except Exception as exc:
             extras["packed_path"] = {"error": repr(exc)}
+        # bounded configuration-3 and configuration-4 runs (their own modes,
+        # --config 3 / --config 4, run them at full size)
+        if args.extra_cases > 0:
+            try:
+                extras["batching"] = batching_run(args.extra_cases, 2, 1, 256, local)
+            except Exception as exc:
+                extras["batching"] = {"error": repr(exc)}
+        if args.extra_requests > 0:
+            try:
+                extras["serving"] = serving_run(args.extra_requests, (0.5, 0.9), ("M",))
+            except Exception as exc:
+                extras["serving"] = {"error": repr(exc)}
 
     if rank == 0:
         line = {
@@ -556,29 +568,22 @@ def run_ours(args):
     return 0
 
 
-def run_config3(args) -> int:
-    """Configuration 3: 64 cases of uneven S, Ny, k and wavenumber grid,
-    every case resident (one plan each), factor shapes tuned per geometry,
-    one step = the three SMR91 substeps of every case recorded into one CUDA
-    graph over 8 streams and replayed.  value = system solves per second
-    (each system solved once per substep)."""
+def batching_run(cases: int, steps: int, warmup: int, tune_nsys: int, local: int) -> dict:
+    """Configuration 3's step over `cases` cases: every case resident (one
+    plan each), factor shapes tuned per geometry when tune_nsys > 0, one step
+    = the three SMR91 substeps of every case recorded into one CUDA graph
+    over 8 streams and replayed.  value = system solves per second (each
+    system solved once per substep)."""
     import torch
-    rank, local, world = dist_env()
-    if world > 1 and rank != 0:
-        return 0
-    torch.cuda.set_device(local)
-    from suzerain_gb300 import build as B
-    B.build()
-    from suzerain_gb300 import _native as nat, multicase, plan as P, synth
-    L = nat.load()
-    if L.sgb_device_ok() != 0:
-        raise RuntimeError(nat.last_error())
-    cfgs = synth.config3_cases(args.cases)
+    from suzerain_gb300 import multicase, plan as P, synth
+    cfgs = synth.config3_cases(cases)
+    t0 = time.perf_counter()
     mc = multicase.MultiCase(cfgs, nstreams=8, max_double_slots=128)
-    tuned = mc.tune("C", nsys=512, reps=1)
+    tuned = mc.tune("C", nsys=tune_nsys, reps=1) if tune_nsys > 0 else {}
     spec = P.RefineSpec(**SPEC)
     mc.capture("M", spec)
-    for _ in range(args.warmup):
+    setup_s = time.perf_counter() - t0
+    for _ in range(warmup):
         mc.replay()
     torch.cuda.synchronize()
     stream = torch.cuda.current_stream()
@@ -586,63 +591,47 @@ def run_config3(args) -> int:
     sampler.start()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    for _ in range(args.steps):
+    for _ in range(steps):
         mc.replay()
     e1.record(stream)
     torch.cuda.synchronize()
     clocks = sampler.stop()
     ms = e0.elapsed_time(e1)
     nsys = mc.nsys
-    solves = nsys * mc.nsubsteps * args.steps
+    solves = nsys * mc.nsubsteps * steps
     berr = mc.backward_error()
-    line = {
-        "metric": "system solves/s at rel-resid <=1e-12 (mixed c64 LU + FP64 refinement)",
-        "value": solves / (ms / 1e3), "unit": "systems/s", "n_gpus": 1, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "c64 factor + f64 refinement",
-        "data": "synthetic (seeded generator of the reference's shapes)",
-        "config": {"workload": f"config 3: {len(cfgs)} cases, S in {{5,7}}, k in {{6,8}}, "
-                               f"Ny in 32..256, {nsys} systems, {len(mc.geometries())} geometries; "
-                               f"step = 3 SMR91 substeps of every case, one CUDA graph over "
-                               f"8 streams",
-                   "l2": "inputs larger than L2"},
-        "rel_resid_max": float(berr.max()),
-        "unserved": mc.unserved(),
-        "gpu_launches": int(mc.graph_kernels) * args.steps,
+    out = {
+        "value": solves / (ms / 1e3), "unit": "systems/s", "steps": steps, "warmup": warmup,
+        "ms_per_step": ms / steps,
+        "workload": f"config 3: {len(cfgs)} cases, S in {{5,7}}, k in {{6,8}}, Ny in 32..256, "
+                    f"{nsys} systems, {len(mc.geometries())} geometries; step = 3 SMR91 "
+                    f"substeps of every case, one CUDA graph over 8 streams",
+        "cases": len(cfgs), "systems": nsys, "geometries": len(mc.geometries()),
+        "rel_resid_max": float(berr.max()), "unserved": mc.unserved(),
+        "gpu_launches": int(mc.graph_kernels) * steps,
         "tuned_shapes": {f"{k[0]} N={k[1]} KL={k[2]}": list(v) for k, v in tuned.items()},
-        "clocks": clocks,
-        "e2e": None,
-        "device_bytes": mc.device_bytes(),
+        "setup_s": setup_s, "clocks": clocks, "device_bytes": mc.device_bytes(),
     }
-    print(json.dumps(line))
-    return 0
+    del mc
+    torch.cuda.empty_cache()
+    return out
 
 
-def run_config4(args) -> int:
+def serving_run(requests: int, levels, methods) -> dict:
     """Configuration 4: a Poisson stream of substep-solve requests with case
     shapes drawn as in configuration 3 and lifetimes of 3..30 substeps,
     served by the continuous-batching loop under a 120 GB HBM budget.  The
     capacity (system solves/s with every request present at t = 0) is
-    measured first; then the arrival rate sweeps 10..90 % of it.  Reports
-    p50/p99 per-substep latency and throughput per level, mixed and plain
-    complex128.  Requests per level are bounded (--requests) so the run ends
-    in minutes; the full 10,000-request levels are --requests 10000."""
+    measured first; then the arrival rate runs at the given fractions of it.
+    p50/p99 per-substep latency and throughput per level and method."""
     import torch
-    rank, local, world = dist_env()
-    if world > 1 and rank != 0:
-        return 0
-    torch.cuda.set_device(local)
-    from suzerain_gb300 import build as B
-    B.build()
-    from suzerain_gb300 import _native as nat, plan as P, serve, synth
-    L = nat.load()
-    if L.sgb_device_ok() != 0:
-        raise RuntimeError(nat.last_error())
+    from suzerain_gb300 import plan as P, serve, synth
     spec = P.RefineSpec(**SPEC)
     pool = synth.config3_cases(64, seed=synth.SEED_BASE + 4)
     mean_sys = sum(c.nsys for c in pool) / len(pool)
     out = {}
-    for method, nreq in (("M", args.requests), ("Z", max(4, args.requests // 5))):
+    for method in methods:
+        nreq = requests if method == "M" else max(4, requests // 5)
         srv = serve.Server(budget_bytes=120e9, method=method, spec=spec, nstreams=8)
         # warm-up (kernel attributes, first-touch) and capacity
         srv.run(serve.poisson_trace(4, 1e9, seed=99, configs=pool, life=(3, 3)))
@@ -650,14 +639,65 @@ def run_config4(args) -> int:
         srv.prebuild(tr)
         cap = srv.run(tr)
         cap_sps = cap["throughput"]
-        levels = []
-        for lvl in (0.1, 0.3, 0.5, 0.7, 0.9):
+        lv = []
+        for lvl in levels:
             rate = lvl * cap_sps / (mean_sys * 16.5)      # cases/s
             tr = serve.poisson_trace(nreq, rate, seed=int(lvl * 1000), configs=pool)
             srv.prebuild(tr)
             st = srv.run(tr)
-            levels.append({"load": lvl, "rate_cases_per_s": rate, **st})
-        out[method] = {"capacity_system_solves_per_s": cap_sps, "levels": levels}
+            lv.append({"load": lvl, "rate_cases_per_s": rate, **st})
+        out[method] = {"requests_per_level": nreq, "capacity_system_solves_per_s": cap_sps,
+                       "levels": lv}
+    torch.cuda.empty_cache()
+    return out
+
+
+def run_config3(args) -> int:
+    """Configuration 3 as its own bench line (all 64 cases by default)."""
+    import torch
+    rank, local, world = dist_env()
+    if world > 1 and rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    from suzerain_gb300 import build as B
+    B.build()
+    from suzerain_gb300 import _native as nat
+    L = nat.load()
+    if L.sgb_device_ok() != 0:
+        raise RuntimeError(nat.last_error())
+    r = batching_run(args.cases, args.steps, args.warmup, 512, local)
+    line = {
+        "metric": "system solves/s at rel-resid <=1e-12 (mixed c64 LU + FP64 refinement)",
+        "value": r["value"], "unit": "systems/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c64 factor + f64 refinement",
+        "data": "synthetic (seeded generator of the reference's shapes)",
+        "config": {"workload": r["workload"], "l2": "inputs larger than L2"},
+        "rel_resid_max": r["rel_resid_max"], "unserved": r["unserved"],
+        "gpu_launches": r["gpu_launches"], "tuned_shapes": r["tuned_shapes"],
+        "clocks": r["clocks"], "e2e": None, "device_bytes": r["device_bytes"],
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_config4(args) -> int:
+    """Configuration 4 as its own bench line.  Requests per level are bounded
+    (--requests) so the run ends in minutes; --levels picks the loads."""
+    import torch
+    rank, local, world = dist_env()
+    if world > 1 and rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    from suzerain_gb300 import build as B
+    B.build()
+    from suzerain_gb300 import _native as nat
+    L = nat.load()
+    if L.sgb_device_ok() != 0:
+        raise RuntimeError(nat.last_error())
+    levels = [float(x) for x in args.levels.split(",")]
+    methods = ("M", "Z") if args.fp64_steps > 0 else ("M",)
+    out = serving_run(args.requests, levels, methods)
     best = out["M"]["levels"][-1]
     line = {
         "metric": "system solves/s under Poisson load (serving), p50/p99 per-substep latency",
@@ -668,8 +708,7 @@ def run_config4(args) -> int:
         "data": "synthetic (seeded generator of the reference's shapes)",
         "config": {"workload": f"config 4: Poisson requests, case shapes of config 3, "
                                f"lifetimes 3..30 substeps, 120 GB budget, {args.requests} "
-                               f"requests per level (mixed), {max(4, args.requests // 5)} "
-                               f"(complex128)"},
+                               f"requests per level (mixed), loads {args.levels}"},
         "p50_ms": best["p50_ms"], "p99_ms": best["p99_ms"],
         "serving": out,
         "e2e": None,
@@ -696,7 +735,7 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=0,
                     help="reference arm: systems per step (0: the whole batch)")
     ap.add_argument("--no-extras", action="store_true",
-                    help="skip the literal-mask, stiff and packed-band runs")
+                    help="skip the literal-mask, stiff, packed-band, batching and serving runs")
     ap.add_argument("--variant-steps", type=int, default=2)
     ap.add_argument("--variant-sample", type=int, default=1024)
     ap.add_argument("--packed-steps", type=int, default=2)
@@ -704,6 +743,12 @@ def main():
     ap.add_argument("--cases", type=int, default=64, help="configuration 3: number of cases")
     ap.add_argument("--requests", type=int, default=40,
                     help="configuration 4: requests per load level (mixed)")
+    ap.add_argument("--levels", default="0.1,0.3,0.5,0.7,0.9",
+                    help="configuration 4: loads, fractions of the measured capacity")
+    ap.add_argument("--extra-cases", type=int, default=16,
+                    help="default line: configuration-3 cases of the `batching` key (0: skip)")
+    ap.add_argument("--extra-requests", type=int, default=16,
+                    help="default line: requests per level of the `serving` key (0: skip)")
     ap.add_argument("--nsys", type=int, default=0,
                     help="use only the first NSYS systems of the batch (profiling)")
     args = ap.parse_args()

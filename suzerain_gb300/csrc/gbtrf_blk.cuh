@@ -593,11 +593,28 @@ k_gbtrf_cta(FactorGeom g, int nsys, PackedSource src, ModelSource ms,
                     for (int t = 0; t < MAXTR; ++t) l[t] = win[roff[t] + cm];
 #pragma unroll
                     for (int u = 0; u < TC; ++u) uu[u] = win[rm + coff[u]];
+                    if constexpr (sizeof(R) == 4) {
+                        // complex64: two packed FMAs per complex multiply-add
+                        float2 la[MAXTR], lb[MAXTR], us[TC];
 #pragma unroll
-                    for (int t = 0; t < MAXTR; ++t)
+                        for (int t = 0; t < MAXTR; ++t) {
+                            la[t] = make_float2(-l[t].x, -l[t].x);
+                            lb[t] = make_float2(l[t].y, -l[t].y);
+                        }
 #pragma unroll
-                        for (int u = 0; u < TC; ++u)
-                            acc[t][u] = cfnma(l[t], uu[u], acc[t][u]);
+                        for (int u = 0; u < TC; ++u) us[u] = make_float2(uu[u].y, uu[u].x);
+#pragma unroll
+                        for (int t = 0; t < MAXTR; ++t)
+#pragma unroll
+                            for (int u = 0; u < TC; ++u)
+                                acc[t][u] = cfnma2(la[t], lb[t], uu[u], us[u], acc[t][u]);
+                    } else {
+#pragma unroll
+                        for (int t = 0; t < MAXTR; ++t)
+#pragma unroll
+                            for (int u = 0; u < TC; ++u)
+                                acc[t][u] = cfnma(l[t], uu[u], acc[t][u]);
+                    }
                 }
 #pragma unroll
                 for (int t = 0; t < MAXTR; ++t)

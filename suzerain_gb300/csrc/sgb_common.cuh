@@ -49,6 +49,23 @@ SGB_HD double2 cfma(double2 a, double2 b, double2 c)
     return make_double2(fma(-a.y, b.y, fma(a.x, b.x, c.x)),
                         fma(a.y, b.x, fma(a.x, b.y, c.y)));
 }
+// Two-lane FMA on a pair of floats (fma.rn.f32x2, sm_100 and later): lane k
+// of the result is fma(a_k, b_k, c_k), rounded once, as the scalar fmaf.
+__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c)
+{
+    float2 d;
+    asm("{\n .reg .b64 ra, rb, rc, rd;\n mov.b64 ra, {%2, %3};\n mov.b64 rb, {%4, %5};\n"
+        " mov.b64 rc, {%6, %7};\n fma.rn.f32x2 rd, ra, rb, rc;\n mov.b64 {%0, %1}, rd;\n}"
+        : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+    return d;
+}
+// c - a * b as two packed FMAs with cfnma's roundings in cfnma's order, from
+// the operand forms la = (-a.x, -a.x), lb = (a.y, -a.y), b and bs = (b.y, b.x).
+__device__ __forceinline__ float2 cfnma2(float2 la, float2 lb, float2 b, float2 bs, float2 c)
+{
+    return ffma2(lb, bs, ffma2(la, b, c));
+}
+
 SGB_HD float2  cconj(float2 a)  { return make_float2(a.x, -a.y); }
 SGB_HD double2 cconj(double2 a) { return make_double2(a.x, -a.y); }
 
