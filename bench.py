@@ -717,6 +717,44 @@ def run_config4(args) -> int:
     return 0
 
 
+def run_peaks(args) -> int:
+    """Pipe-throughput microbenchmarks of this GPU (FP64 FMA, FP32 FMA, packed
+    FP32 FMA, shared-memory loads) with the clocks seen meanwhile: the
+    denominators of the compute-pipe fractions quoted for the factor and the
+    FP64 kernels.  One JSON line."""
+    import ctypes as C
+    import torch
+    rank, local, world = dist_env()
+    if world > 1 and rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    from suzerain_gb300 import build as B
+    B.build()
+    from suzerain_gb300 import _native as nat
+    L = nat.load()
+    if L.sgb_device_ok() != 0:
+        raise RuntimeError(nat.last_error())
+    out = (C.c_double * 7)()
+    sampler = ClockSampler(local)
+    sampler.start()
+    runs = []
+    for _ in range(max(1, args.steps)):
+        nat.check(L.sgb_measure_peaks(out, None), "sgb_measure_peaks")
+        runs.append(list(out))
+    clocks = sampler.stop()
+    best = [max(r[i] for r in runs) for i in range(4)]
+    sm = clocks.get("sm_mhz") or out[5]
+    line = {"peaks": {"fp64_fma_tflops": best[0], "fp32_fma_tflops": best[1],
+                      "fp32_ffma2_tflops": best[2], "smem_load_tbs": best[3],
+                      "smem_bytes_per_clk_per_sm": best[3] * 1e12 / out[6] / (sm * 1e6),
+                      "sm_count": int(out[6]), "sm_clock_mhz_used": sm},
+            "method": "8 independent chains per thread, 64 warps per SM, CUDA events; "
+                      "best of the runs; smem: conflict-free 64-bit loads",
+            "runs": len(runs), "clocks": clocks}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -751,7 +789,11 @@ def main():
                     help="default line: requests per level of the `serving` key (0: skip)")
     ap.add_argument("--nsys", type=int, default=0,
                     help="use only the first NSYS systems of the batch (profiling)")
+    ap.add_argument("--peaks", action="store_true",
+                    help="print this GPU's pipe-throughput microbenchmarks and exit")
     args = ap.parse_args()
+    if args.peaks:
+        return run_peaks(args)
     if args.impl == "reference":
         return run_reference(args)
     if args.config == 3:

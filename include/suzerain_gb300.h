@@ -567,6 +567,14 @@ int sgb_gbtrf_phase_cycles(char prec, int nsys, int N, int KL, int KU,
                            void *fac, int *ipiv, int *info, int nb, int nw,
                            unsigned long long *cycles_dev, void *stream);
 
+/** Diagnostics: pipe-throughput microbenchmarks of the current device (the
+ *  denominators the factor and residual kernels are compared with).  out
+ *  (7 host doubles) receives FP64 FMA TFLOP/s, FP32 FMA TFLOP/s, packed
+ *  two-lane FP32 FMA TFLOP/s, shared-memory load bandwidth TB/s, the same in
+ *  bytes per SM per clock at the device's reported maximum SM clock, that
+ *  clock in MHz, and the SM count. */
+int sgb_measure_peaks(double *out, void *stream);
+
 /** Process-wide shape table of the blocked factor, keyed (prec, N, KL, KU):
  *  set records (nb, nw) for every later factorization of that geometry (the
  *  plan and the refinement driver included); get reports the shape in force.

@@ -146,6 +146,7 @@ _SIGS = {
                                   _p, _p, _i, _i, _i, _p]),
     "sgb_gbtrf_phase_cycles": (_i, [C.c_char, _i, _i, _i, _i, _p, _i, _ll, _p,
                                     _p, _p, _i, _i, _p, _p]),
+    "sgb_measure_peaks": (_i, [_p, _p]),
     "sgb_gbtrf_set_shape": (_i, [C.c_char, _i, _i, _i, _i, _i]),
     "sgb_gbtrf_get_shape": (_i, [C.c_char, _i, _i, _i, _p, _p]),
     "sgb_gbtrs_batched": (_i, [C.c_char, C.c_char, _i, _i, _i, _i, _p, _p, _p,

@@ -19,12 +19,12 @@ size_t gbtrf_blk_smem_bytes(int prec_bytes, const FactorGeom &g, int S, int nb, 
         const int WR = g.KL + nb, WC = g.KL + g.KU + nb, P = blk_pitch(WC);
         const size_t stage = nw > 1 ? (size_t) nb * WC + nb : 0;
         return ((size_t) (WR + 1) * P + WR + stage + 3 * (size_t) S * S) * el
-             + (size_t) nb * sizeof(int) + 4 * sizeof(int) + 16;
+             + (size_t) nb * sizeof(int) + 4 * sizeof(int) + 12 * 8 + 16;
     }
     // lookahead: panel J-1's rows and columns stay, plus the staged rows
     const int WR = g.KL + 2 * nb, WC = g.KL + g.KU + 2 * nb, P = blk_pitch(WC);
     return ((size_t) (WR + 1) * P + WR + (size_t) nb * WC + nb + 3 * (size_t) S * S) * el
-         + (size_t) nb * sizeof(int) + 4 * sizeof(int) + 16;
+         + (size_t) nb * sizeof(int) + 4 * sizeof(int) + 12 * 8 + 16;
 }
 
 // Rows of the trailing update per thread: KL <= 4 NW MAXTR (MAXTR 13, 7, 4

@@ -75,6 +75,14 @@ __device__ __forceinline__ cplx_t<R> model_entry(const ModelSource &ms, const cp
     }
 }
 
+
+// Complex64 shared-memory accesses at explicit 32-bit shared-window byte
+// addresses (one integer add per access in the trailing update).
+__device__ __forceinline__ float2 lds_c(unsigned a, float2)
+{ float2 v; asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(a)); return v; }
+__device__ __forceinline__ void sts_c(unsigned a, float2 v)
+{ asm volatile("st.shared.v2.f32 [%0], {%1, %2};" :: "r"(a), "f"(v.x), "f"(v.y) : "memory"); }
+
 // Warp shuffle of a complex value from lane src.
 template <typename R>
 __device__ __forceinline__ cplx_t<R> shfl_c(cplx_t<R> z, int src)
@@ -162,16 +170,20 @@ __device__ __forceinline__ void panel_factor(cplx_t<R> *__restrict__ win, int P,
                                              int j0, int nbk, int N, int KL, int KU,
                                              cplx_t<R> *__restrict__ fl, int *__restrict__ pv,
                                              cplx_t<R> *__restrict__ ys, int lane,
-                                             unsigned long long *__restrict__ prof = nullptr)
+                                             unsigned long long *__restrict__ clk = nullptr)
 {
     using T2 = cplx_t<R>;
     const T2 zero = mk<R>(R(0), R(0));
-    // optional sub-phase cycle counters (diagnostics): pivot search,
-    // reciprocal + scale + L store, rank-1 update of the panel columns
-    unsigned long long sp[3] = {0, 0, 0};
-    long long smark = prof ? clock64() : 0;
+    // optional sub-phase cycle counters (diagnostics, lane 0 with clk set,
+    // in shared memory): pivot search, reciprocal + scale + L store, rank-1
+    // update of the panel columns
+    if (clk && lane == 0) clk[11] = clock64();
     auto stick = [&](int ph) {
-        if (prof) { const long long t = clock64(); sp[ph] += (unsigned long long) (t - smark); smark = t; }
+        if (clk && lane == 0) {
+            const unsigned long long t = clock64();
+            clk[6 + ph] += t - clk[11];
+            clk[11] = t;
+        }
     };
     auto rsl = [&](int i) { int t = rb + i; return t >= WR ? t - WR : t; };
     auto csl = [&](int c) { int t = cb + c; return t >= WC ? t - WC : t; };
@@ -284,8 +296,6 @@ __device__ __forceinline__ void panel_factor(cplx_t<R> *__restrict__ win, int P,
         }
     }
     if (lane == 0) { shv[0] = ju; shv[1] = inf; }
-    if (prof && lane == 0)
-        for (int ph = 0; ph < 3; ++ph) atomicAdd(prof + 6 + ph, sp[ph]);
 }
 
 // Rows r0 .. r0+nr-1 of A (rows outside 0..N-1 read as zero) at columns
@@ -453,13 +463,22 @@ k_gbtrf_cta(FactorGeom g, int nsys, PackedSource src, ModelSource ms,
     int *pv = ipiv + fi * N;
     const T2 zero = mk<R>(R(0), R(0));
 
-    // Optional per-phase cycle counters (diagnostics), read on thread 0:
-    // 0 init, 1 panel (+ staging), 2 interchanges + U12, 3 GEMM + U rows out,
-    // 4 unused, 5 retire/enter.
-    unsigned long long tph[6] = {0, 0, 0, 0, 0, 0};
-    long long tmark = prof ? clock64() : 0;
+    // Optional per-phase cycle counters (diagnostics), kept by thread 0 in
+    // shared memory so that no registers are held for them: 0 init, 1 panel
+    // (+ staging), 2 interchanges + U12, 3 GEMM + U rows out, 5 retire/enter;
+    // 6..8 the panel's sub-phases; 10 and 11 the last marks.
+    unsigned long long *clk = reinterpret_cast<unsigned long long *>(shv + 4);
+    const bool timing = prof && tid == 0;
+    if (timing) {
+        for (int i = 0; i < 12; ++i) clk[i] = 0;
+        clk[10] = clock64();
+    }
     auto tick = [&](int ph) {
-        if (prof) { const long long t = clock64(); tph[ph] += (unsigned long long) (t - tmark); tmark = t; }
+        if (timing) {
+            const unsigned long long t = clock64();
+            clk[ph] += t - clk[10];
+            clk[10] = t;
+        }
     };
 
     if (MODEL) {
@@ -499,7 +518,8 @@ k_gbtrf_cta(FactorGeom g, int nsys, PackedSource src, ModelSource ms,
         // nbk panel columns (row k of step k is row k of slot 0, on lane k).
         if (warp == 0) {
             panel_factor<R, NB, RS, FWD>(win, P, WR, WC, rb, cb, WR, rs, pvoff, shv, j0, nbk, N, KL,
-                                         KU, fl, pv, FWD ? y + s * y_stride : nullptr, lane, prof);
+                                         KU, fl, pv, FWD ? y + s * y_stride : nullptr, lane,
+                                         timing ? clk : nullptr);
         } else if constexpr (STAGE) {
             // the next nbk rows of A, at the next window's columns
             if (more) {
@@ -566,33 +586,47 @@ k_gbtrf_cta(FactorGeom g, int nsys, PackedSource src, ModelSource ms,
         if (ntr > 0) {
             const int rg = tid >> 3, cg = tid & 7;
             const int nrow = imin(KL, N - j0 - nbk);     // rows nbk .. nbk+nrow-1
-            int roff[MAXTR];
+            // complex64: explicit shared-window byte addresses, one integer add
+            // per access; complex128 (larger tiles, more live registers):
+            // element offsets into win
+            constexpr bool BYTE = sizeof(R) == 4;
+            constexpr unsigned ES = BYTE ? sizeof(T2) : 1u;
+            const unsigned wsh = BYTE ? (unsigned) __cvta_generic_to_shared(win) : 0u;
+            auto ld = [&](unsigned a) -> T2 {
+                if constexpr (BYTE) return lds_c(a, T2{});
+                else return win[a];
+            };
+            auto st = [&](unsigned a, T2 v) {
+                if constexpr (BYTE) sts_c(a, v);
+                else win[a] = v;
+            };
+            unsigned rB[MAXTR];                           // address of each row
 #pragma unroll
             for (int t = 0; t < MAXTR; ++t) {
                 const int i = rg + RGN * t;
-                roff[t] = (i < nrow) ? rsl(nbk + i) * P : WR * P;
+                rB[t] = wsh + (unsigned) ((i < nrow) ? rsl(nbk + i) * P : WR * P) * ES;
             }
             for (int c0 = 0; c0 < ntr; c0 += 8 * TC) {
-                int coff[TC];
+                unsigned cB[TC];                          // offset of each column
 #pragma unroll
                 for (int u = 0; u < TC; ++u) {
                     const int c = c0 + cg + 8 * u;
-                    coff[u] = (c < ntr) ? csl(nbk + c) : WC;
+                    cB[u] = (unsigned) ((c < ntr) ? csl(nbk + c) : WC) * ES;
                 }
                 T2 acc[MAXTR][TC];
 #pragma unroll
                 for (int t = 0; t < MAXTR; ++t)
 #pragma unroll
                     for (int u = 0; u < TC; ++u)
-                        acc[t][u] = win[roff[t] + coff[u]];
+                        acc[t][u] = ld(rB[t] + cB[u]);
 #pragma unroll
                 for (int m = 0; m < NB; ++m) {       // nbk == NB here
-                    const int cm = csl(m), rm = rsl(m) * P;
+                    const unsigned cm = (unsigned) csl(m) * ES, rm = wsh + (unsigned) (rsl(m) * P) * ES;
                     T2 l[MAXTR], uu[TC];
 #pragma unroll
-                    for (int t = 0; t < MAXTR; ++t) l[t] = win[roff[t] + cm];
+                    for (int t = 0; t < MAXTR; ++t) l[t] = ld(rB[t] + cm);
 #pragma unroll
-                    for (int u = 0; u < TC; ++u) uu[u] = win[rm + coff[u]];
+                    for (int u = 0; u < TC; ++u) uu[u] = ld(rm + cB[u]);
                     if constexpr (sizeof(R) == 4) {
                         // complex64: two packed FMAs per complex multiply-add
                         float2 la[MAXTR], lb[MAXTR], us[TC];
@@ -620,7 +654,7 @@ k_gbtrf_cta(FactorGeom g, int nsys, PackedSource src, ModelSource ms,
                 for (int t = 0; t < MAXTR; ++t)
 #pragma unroll
                     for (int u = 0; u < TC; ++u)
-                        win[roff[t] + coff[u]] = acc[t][u];
+                        st(rB[t] + cB[u], acc[t][u]);
             }
         }
         for (int k = warp; k < nbk; k += NW) {
@@ -669,8 +703,8 @@ k_gbtrf_cta(FactorGeom g, int nsys, PackedSource src, ModelSource ms,
         cb += NB; if (cb >= WC) cb -= WC;
     }
     if (tid == 0) info[fi] = shv[1];
-    if (prof && tid == 0)
-        for (int ph = 0; ph < 6; ++ph) atomicAdd(prof + ph, tph[ph]);
+    if (timing)
+        for (int ph = 0; ph < 9; ++ph) atomicAdd(prof + ph, clk[ph]);
 }
 
 // Lookahead form (NW >= 2): warp 0 factors panel J while warps 1..NW-1 apply
@@ -731,12 +765,21 @@ k_gbtrf_la(FactorGeom g, int nsys, PackedSource src, ModelSource ms,
     int *pv = ipiv + fi * N;
     const T2 zero = mk<R>(R(0), R(0));
 
-    // Optional per-phase cycle counters (diagnostics), read on thread 0:
-    // 0 init, 1 phase A, 2 phase B, 3 phase C, 4 last U rows.
-    unsigned long long tph[6] = {0, 0, 0, 0, 0, 0};
-    long long tmark = prof ? clock64() : 0;
+    // Optional per-phase cycle counters (diagnostics), kept by thread 0 in
+    // shared memory so that no registers are held for them: 0 init, 1 phase A,
+    // 2 phase B, 3 phase C, 4 last U rows; 10 the last mark.
+    unsigned long long *clk = reinterpret_cast<unsigned long long *>(shv + 4);
+    const bool timing = prof && tid == 0;
+    if (timing) {
+        for (int i = 0; i < 12; ++i) clk[i] = 0;
+        clk[10] = clock64();
+    }
     auto tick = [&](int ph) {
-        if (prof) { const long long t = clock64(); tph[ph] += (unsigned long long) (t - tmark); tmark = t; }
+        if (timing) {
+            const unsigned long long t = clock64();
+            clk[ph] += t - clk[10];
+            clk[10] = t;
+        }
     };
 
     if (MODEL) {
@@ -937,8 +980,8 @@ k_gbtrf_la(FactorGeom g, int nsys, PackedSource src, ModelSource ms,
     }
     tick(4);
     if (tid == 0) info[fi] = shv[1];
-    if (prof && tid == 0)
-        for (int ph = 0; ph < 6; ++ph) atomicAdd(prof + ph, tph[ph]);
+    if (timing)
+        for (int ph = 0; ph < 6; ++ph) atomicAdd(prof + ph, clk[ph]);
 }
 
 template <typename R, int NB, int NW, int MAXTR, bool LA, bool MODEL, bool FWD>
