@@ -426,6 +426,17 @@ def run_ours(args):
     ms = max_over_ranks(e0.elapsed_time(e1), world, "cuda")
     value = nsys * world * args.steps / (ms / 1e3)
 
+    if args.profile_step:
+        # profiling runs: the warm-up and timed substeps only, then exit, so
+        # that a launch list of this command holds exactly those launches
+        if rank == 0:
+            print(json.dumps({"profile_step": True, "steps": args.steps, "warmup": args.warmup,
+                              "launches_before_timed": int(l0),
+                              "gpu_launches": int(launches), "ms_per_step": ms / args.steps,
+                              "launches_per_step": int(launches) // max(1, args.steps)}))
+        runner.close()
+        return 0
+
     # ---- accuracy of the last step (untimed) ------------------------------
     rep = runner.report()
     berr = runner.backward_error()
@@ -789,6 +800,8 @@ def main():
                     help="default line: requests per level of the `serving` key (0: skip)")
     ap.add_argument("--nsys", type=int, default=0,
                     help="use only the first NSYS systems of the batch (profiling)")
+    ap.add_argument("--profile-step", action="store_true",
+                    help="run the warm-up and timed substeps only (launch lists)")
     ap.add_argument("--peaks", action="store_true",
                     help="print this GPU's pipe-throughput microbenchmarks and exit")
     args = ap.parse_args()

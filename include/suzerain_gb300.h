@@ -170,6 +170,15 @@ int suzerain_lapack_cgbtrs(const char trans, const int n, const int kl,
                            const sgb_complex_float *ab, const int ldab,
                            const int *ipiv, sgb_complex_float *b,
                            const int ldb);
+/** LAPACK ZGBCON on a gbtrf factor (suzerain/blas_et_al/lapack.c): the
+ *  reciprocal condition number in the 1-norm ('1' / 'O') or the
+ *  infinity-norm ('I') by Higham's estimator; -i argument errors; work and
+ *  rwork unused (may be NULL).  The estimator's triangular solves are plain
+ *  solves (ZLATBS's rescaling against overflow is not reproduced). */
+int suzerain_lapack_zgbcon(const char norm, const int n, const int kl, const int ku,
+                           const sgb_complex_double *ab, const int ldab, const int *ipiv,
+                           const double anorm, double *rcond, sgb_complex_double *work,
+                           double *rwork);
 
 /** LAPACK's expert driver zgbsvx (equilibration for fact 'E', factor for
  *  'N'/'E', a given factor for 'F', reciprocal condition number, solve,
@@ -270,8 +279,8 @@ sgb_bsplineop_alloc_breakpoints(int k, int nbreak, const double *breakpts,
                                 int nderiv);
 /** suzerain/bsplineop.c:205-219. */
 void suzerain_bsplineop_free(suzerain_bsplineop_workspace *w);
-/** y <- alpha D^nderiv x + beta y per right-hand side;
- *  suzerain/bsplineop.c:261-298. */
+/** y <- alpha D^nderiv x + beta y per right-hand side (complex x, y, alpha,
+ *  beta); suzerain/bsplineop.c:261-298. */
 int suzerain_bsplineop_accumulate_complex(int nderiv, int nrhs,
                                           const sgb_complex_double alpha,
                                           const sgb_complex_double *x,
@@ -280,6 +289,78 @@ int suzerain_bsplineop_accumulate_complex(int nderiv, int nrhs,
                                           sgb_complex_double *y, int incy,
                                           int ldy,
                                           const suzerain_bsplineop_workspace *w);
+
+/** x <- alpha D^nderiv x in place (real and complex coefficients, real
+ *  alpha) and y <- alpha D^nderiv x + beta y (real), per right-hand side;
+ *  suzerain/bsplineop.c:222-400.  Argument errors return SUZERAIN_EINVAL (4)
+ *  (the reference's code after its error handler); increments must be
+ *  positive. */
+int suzerain_bsplineop_apply(int nderiv, int nrhs, double alpha, double *x, int incx, int ldx,
+                             const suzerain_bsplineop_workspace *w);
+int suzerain_bsplineop_accumulate(int nderiv, int nrhs, double alpha, const double *x, int incx,
+                                  int ldx, double beta, double *y, int incy, int ldy,
+                                  const suzerain_bsplineop_workspace *w);
+int suzerain_bsplineop_apply_complex(int nderiv, int nrhs, double alpha, sgb_complex_double *x,
+                                     int incx, int ldx, const suzerain_bsplineop_workspace *w);
+
+/** Operator workspaces of suzerain/bsplineop.h:455-990: the transpose of a
+ *  linear combination of the D^m in LAPACK gbtrf storage (A_T + kl is the
+ *  unfactored band, ld = 2 kl + ku + 1), its pivots, and the state flag
+ *  ipiv[0] < 0 (not factored; -ipiv[0] counts accumulations).  Host memory,
+ *  as the reference allocates it; the operations run on the GPU.  Codes:
+ *  0, SUZERAIN_EINVAL (4) for bad arguments or call order, SUZERAIN_ESANITY
+ *  (7) when the factor, norm or estimate reports an error, SUZERAIN_ENOMEM
+ *  (8).  The real workspace factors, estimates and solves in complex
+ *  arithmetic with zero imaginary parts. */
+typedef struct suzerain_bsplineop_lu_workspace {
+    int n, kl, ku, ld;
+    int *ipiv;
+    double *A_T;
+} suzerain_bsplineop_lu_workspace;
+typedef struct suzerain_bsplineop_luz_workspace {
+    int n, kl, ku, ld;
+    int *ipiv;
+    sgb_complex_double *A_T;
+} suzerain_bsplineop_luz_workspace;
+
+suzerain_bsplineop_lu_workspace *suzerain_bsplineop_lu_alloc(const suzerain_bsplineop_workspace *w);
+void suzerain_bsplineop_lu_free(suzerain_bsplineop_lu_workspace *luw);
+int suzerain_bsplineop_lu_opaccumulate(int ncoefficients, const double *coefficients,
+                                       const suzerain_bsplineop_workspace *w, const double scale,
+                                       suzerain_bsplineop_lu_workspace *luw);
+int suzerain_bsplineop_lu_opnorm(const suzerain_bsplineop_lu_workspace *luw, double *norm);
+int suzerain_bsplineop_lu_factor(suzerain_bsplineop_lu_workspace *luw);
+int suzerain_bsplineop_lu_rcond(const double norm, double *rcond,
+                                const suzerain_bsplineop_lu_workspace *luw);
+int suzerain_bsplineop_lu_solve(int nrhs, double *B, int incb, int ldb,
+                                const suzerain_bsplineop_lu_workspace *luw);
+int suzerain_bsplineop_lu_opform(int ncoefficients, const double *coefficients,
+                                 const suzerain_bsplineop_workspace *w,
+                                 suzerain_bsplineop_lu_workspace *luw);
+int suzerain_bsplineop_lu_opform_mass(const suzerain_bsplineop_workspace *w,
+                                      suzerain_bsplineop_lu_workspace *luw);
+int suzerain_bsplineop_lu_factor_mass(const suzerain_bsplineop_workspace *w,
+                                      suzerain_bsplineop_lu_workspace *luw);
+
+suzerain_bsplineop_luz_workspace *suzerain_bsplineop_luz_alloc(const suzerain_bsplineop_workspace *w);
+void suzerain_bsplineop_luz_free(suzerain_bsplineop_luz_workspace *luzw);
+int suzerain_bsplineop_luz_opaccumulate(int ncoefficients, const sgb_complex_double *coefficients,
+                                        const suzerain_bsplineop_workspace *w,
+                                        const sgb_complex_double scale,
+                                        suzerain_bsplineop_luz_workspace *luzw);
+int suzerain_bsplineop_luz_opnorm(const suzerain_bsplineop_luz_workspace *luzw, double *norm);
+int suzerain_bsplineop_luz_factor(suzerain_bsplineop_luz_workspace *luzw);
+int suzerain_bsplineop_luz_rcond(const double norm, double *rcond,
+                                 const suzerain_bsplineop_luz_workspace *luzw);
+int suzerain_bsplineop_luz_solve(int nrhs, sgb_complex_double *B, int incb, int ldb,
+                                 const suzerain_bsplineop_luz_workspace *luzw);
+int suzerain_bsplineop_luz_opform(int ncoefficients, const sgb_complex_double *coefficients,
+                                  const suzerain_bsplineop_workspace *w,
+                                  suzerain_bsplineop_luz_workspace *luzw);
+int suzerain_bsplineop_luz_opform_mass(const suzerain_bsplineop_workspace *w,
+                                       suzerain_bsplineop_luz_workspace *luzw);
+int suzerain_bsplineop_luz_factor_mass(const suzerain_bsplineop_workspace *w,
+                                       suzerain_bsplineop_luz_workspace *luzw);
 
 /** Non-transposed collocation matrices d^m B_j(xi_i), m = 0..nderiv, as
  *  LAPACK bands with the common trimmed kl/ku; bands may be NULL to query
@@ -338,6 +419,9 @@ int suzerain_blasext_dpromote(const int n, void *x);
  *  suzerain/blas_et_al/blasext.c:2741-2778. */
 int suzerain_blasext_zgbnorm1(const int m, const int n, const int kl, const int ku,
                               const sgb_complex_double *a, const int lda, double *norm1);
+/** The real form, dgbnorm1 (suzerain/blas_et_al/blasext.c:2659-2700). */
+int suzerain_blasext_dgbnorm1(const int m, const int n, const int kl, const int ku,
+                              const double *a, const int lda, double *norm1);
 
 /* ---- The production implicit operator (suzerain/rholut_imexop.h) ------ */
 

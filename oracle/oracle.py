@@ -582,3 +582,50 @@ def reuse_sequence(fn, n=120, kl=7, ku=5, seed=77):
     dstate["apprx"] = 1
     out.append(zcgbsvx_call(fn, bands[2], n, kl, ku, rhs[4], dstate, siter=-1, diter=5))
     return out
+
+
+# ---- B-spline operators and their workspaces (suzerain/bsplineop.c) -------
+
+def bsplineop_transposes(w) -> list[np.ndarray]:
+    """Dense D_m^T, m = 0..nderiv, from a workspace's transposed bands (the
+    layout of suzerain/bsplineop.h:125-180: (i, j) of D_m^T at
+    D_T[m][ku[m] + i - j + j ld])."""
+    ws = w.contents
+    n, ld = ws.n, ws.ld
+    out = []
+    for m in range(ws.nderiv + 1):
+        kl, ku = ws.kl[m], ws.ku[m]
+        t = np.zeros((n, n))
+        for j in range(n):
+            for i in range(max(0, j - ku), min(n, j + kl + 1)):
+                t[i, j] = ws.D_T[m][ku + i - j + j * ld]
+        out.append(t)
+    return out
+
+
+def bsplineop_accumulate(DT: np.ndarray, alpha, x, beta, y):
+    """y <- alpha D x + beta y with D = DT^T ('T' band product of the stored
+    transpose, suzerain/bsplineop.c:222-298); beta 0 ignores y."""
+    ax = alpha * (DT.T @ x)
+    return ax if beta == 0 else beta * y + ax
+
+
+def bsplineop_operator(DTs: list[np.ndarray], coefficients, scale=0.0, prior=None):
+    """The transpose A^T of the operator an opaccumulate call leaves:
+    sum_k c_k D_k^T plus scale times the prior transpose
+    (suzerain/bsplineop.c:976-1040, 1325-1380)."""
+    acc = sum(c * t for c, t in zip(coefficients, DTs))
+    if prior is not None and scale != 0:
+        acc = acc + scale * prior
+    return acc
+
+
+def band_of(A: np.ndarray, kl: int, ku: int, ld: int, off: int = 0) -> np.ndarray:
+    """The (kl, ku) band of a dense matrix in LAPACK storage with leading
+    dimension ld, starting at row off (gbtrf storage: off = kl)."""
+    n = A.shape[1]
+    ab = np.zeros((n, ld), dtype=A.dtype)
+    for j in range(n):
+        for i in range(max(0, j - ku), min(A.shape[0], j + kl + 1)):
+            ab[j, off + ku + i - j] = A[i, j]
+    return ab.reshape(-1)

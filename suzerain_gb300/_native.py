@@ -57,6 +57,20 @@ class BsplineopWorkspace(C.Structure):
                 ("D_T", C.POINTER(C.POINTER(_d)))]
 
 
+class BsplineopLuWorkspace(C.Structure):
+    _fields_ = [("n", _i), ("kl", _i), ("ku", _i), ("ld", _i),
+                ("ipiv", C.POINTER(_i)), ("A_T", C.POINTER(_d))]
+
+
+class BsplineopLuzWorkspace(C.Structure):
+    _fields_ = [("n", _i), ("kl", _i), ("ku", _i), ("ld", _i),
+                ("ipiv", C.POINTER(_i)), ("A_T", C.POINTER(_d))]   # interleaved re, im
+
+
+_BW = C.POINTER(BsplineopWorkspace)
+_LU = C.POINTER(BsplineopLuWorkspace)
+_LUZ = C.POINTER(BsplineopLuzWorkspace)
+
 _SIGS = {
     # drop-ins
     "suzerain_bsmbsm_construct": (Bsmbsm, [_i, _i, _i, _i]),
@@ -124,6 +138,30 @@ _SIGS = {
     "suzerain_bsplineop_accumulate_complex": (
         _i, [_i, _i, ZC, _p, _i, _i, ZC, _p, _i, _i,
              C.POINTER(BsplineopWorkspace)]),
+    "suzerain_bsplineop_apply": (_i, [_i, _i, _d, _p, _i, _i, _BW]),
+    "suzerain_bsplineop_accumulate": (_i, [_i, _i, _d, _p, _i, _i, _d, _p, _i, _i, _BW]),
+    "suzerain_bsplineop_apply_complex": (_i, [_i, _i, _d, _p, _i, _i, _BW]),
+    "suzerain_bsplineop_lu_alloc": (_LU, [_BW]),
+    "suzerain_bsplineop_lu_free": (None, [_LU]),
+    "suzerain_bsplineop_lu_opaccumulate": (_i, [_i, _p, _BW, _d, _LU]),
+    "suzerain_bsplineop_lu_opnorm": (_i, [_LU, _p]),
+    "suzerain_bsplineop_lu_factor": (_i, [_LU]),
+    "suzerain_bsplineop_lu_rcond": (_i, [_d, _p, _LU]),
+    "suzerain_bsplineop_lu_solve": (_i, [_i, _p, _i, _i, _LU]),
+    "suzerain_bsplineop_lu_opform": (_i, [_i, _p, _BW, _LU]),
+    "suzerain_bsplineop_lu_opform_mass": (_i, [_BW, _LU]),
+    "suzerain_bsplineop_lu_factor_mass": (_i, [_BW, _LU]),
+    "suzerain_bsplineop_luz_alloc": (_LUZ, [_BW]),
+    "suzerain_bsplineop_luz_free": (None, [_LUZ]),
+    "suzerain_bsplineop_luz_opaccumulate": (_i, [_i, _p, _BW, ZC, _LUZ]),
+    "suzerain_bsplineop_luz_opnorm": (_i, [_LUZ, _p]),
+    "suzerain_bsplineop_luz_factor": (_i, [_LUZ]),
+    "suzerain_bsplineop_luz_rcond": (_i, [_d, _p, _LUZ]),
+    "suzerain_bsplineop_luz_solve": (_i, [_i, _p, _i, _i, _LUZ]),
+    "suzerain_bsplineop_luz_opform": (_i, [_i, _p, _BW, _LUZ]),
+    "suzerain_bsplineop_luz_opform_mass": (_i, [_BW, _LUZ]),
+    "suzerain_bsplineop_luz_factor_mass": (_i, [_BW, _LUZ]),
+    "suzerain_lapack_zgbcon": (_i, [C.c_char, _i, _i, _i, _p, _i, _p, _d, _p, _p, _p]),
     "sgb_bspline_collocation_bands": (_i, [_i, _i, _p, _i, _p, _p, _p, _p,
                                            _p]),
     "suzerain_htstretch2": (_d, [_d, _d, _d]),
@@ -203,6 +241,7 @@ _SIGS = {
     "suzerain_blasext_ddemote": (_i, [_i, _p]),
     "suzerain_blasext_dpromote": (_i, [_i, _p]),
     "suzerain_blasext_zgbnorm1": (_i, [_i, _i, _i, _i, _p, _i, _p]),
+    "suzerain_blasext_dgbnorm1": (_i, [_i, _i, _i, _i, _p, _i, _p]),
     "sgb_rholut_create": (_p, [_p, _p, _p, C.POINTER(BsplineopWorkspace), _p, _p, _p, _p]),
     "sgb_rholut_destroy": (_i, [_p]),
     "sgb_rholut_geometry": (_i, [_p, _p]),

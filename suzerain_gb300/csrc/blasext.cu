@@ -184,7 +184,11 @@ int convert(const char *who, int n, void *x, void (*kern)(long long, const S *, 
     return err_of(e, who);
 }
 
-__global__ void k_gbnorm1(int m, int n, int kl, int ku, const double2 *__restrict__ a, int lda,
+__device__ __forceinline__ double absval(double v) { return fabs(v); }
+__device__ __forceinline__ double absval(double2 v) { return hypot(v.x, v.y); }
+
+template <typename T>
+__global__ void k_gbnorm1(int m, int n, int kl, int ku, const T *__restrict__ a, int lda,
                           double *__restrict__ colsum)
 {
     const int j = blockIdx.x * blockDim.y + threadIdx.y;
@@ -192,10 +196,7 @@ __global__ void k_gbnorm1(int m, int n, int kl, int ku, const double2 *__restric
     const int ib = ku - j > 0 ? ku - j : 0;
     const int ie = ku + (kl + 1 < m - j ? kl + 1 : m - j);
     double s = 0;
-    for (int i = ib + (int) threadIdx.x; i < ie; i += 32) {
-        const double2 v = a[(long long) j * lda + i];
-        s += hypot(v.x, v.y);
-    }
+    for (int i = ib + (int) threadIdx.x; i < ie; i += 32) s += absval(a[(long long) j * lda + i]);
     for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
     if (threadIdx.x == 0) colsum[j] = s;
 }
@@ -300,12 +301,11 @@ extern "C" int suzerain_blasext_dpromote(const int n, void *x)
     return convert<float, double>(__func__, n, x, k_promote_d);
 }
 
-// Maximum column sum of |a_ij| over the band of an m x n matrix: zlangb('1')
-// for the square case (suzerain/blas_et_al/blasext.c:2741-2778).  |z| is
-// hypot(re, im), the reference's cabs.
-extern "C" int suzerain_blasext_zgbnorm1(const int m, const int n, const int kl, const int ku,
-                                         const sgb_complex_double *a, const int lda,
-                                         double *norm1)
+// Maximum column sum of |a_ij| over the band of an m x n matrix, {z,d}langb
+// ('1') for the square case (suzerain/blas_et_al/blasext.c:2659-2778).  For
+// complex entries |z| is hypot(re, im), the reference's cabs.
+template <typename T>
+int gbnorm1(const char *who, int m, int n, int kl, int ku, const T *a, int lda, double *norm1)
 {
     if (m < 0) return -1;
     if (n < 0) return -2;
@@ -316,22 +316,35 @@ extern "C" int suzerain_blasext_zgbnorm1(const int m, const int n, const int kl,
     if (!norm1) return -7;
     *norm1 = 0;
     if (m == 0 || n == 0) return 0;
-    Stage sa(a, ((size_t) (n - 1) * lda + kl + ku + 1) * sizeof(double2), true);
-    if (sa.err != cudaSuccess) return err_of(sa.err, __func__);
+    Stage sa(a, ((size_t) (n - 1) * lda + kl + ku + 1) * sizeof(T), true);
+    if (sa.err != cudaSuccess) return err_of(sa.err, who);
     double *cs = nullptr;
     cudaError_t e = cudaMalloc(&cs, (size_t) n * sizeof(double));
     if (e == cudaSuccess) {
         count_launch(1);
-        k_gbnorm1<<<(unsigned) ((n + 3) / 4), dim3(32, 4)>>>(
-            m, n, kl, ku, static_cast<const double2 *>(sa.dev), lda, cs);
+        k_gbnorm1<T><<<(unsigned) ((n + 3) / 4), dim3(32, 4)>>>(
+            m, n, kl, ku, static_cast<const T *>(sa.dev), lda, cs);
         e = cudaGetLastError();
     }
     std::vector<double> h(n);
     if (e == cudaSuccess) e = cudaMemcpy(h.data(), cs, (size_t) n * sizeof(double), cudaMemcpyDeviceToHost);
     if (cs) cudaFree(cs);
-    if (e != cudaSuccess) return err_of(e, __func__);
+    if (e != cudaSuccess) return err_of(e, who);
     double mx = 0;
     for (double v : h) mx = std::fmax(mx, v);   // NaN columns: fmax keeps the other value
     *norm1 = mx;
     return 0;
+}
+
+extern "C" int suzerain_blasext_zgbnorm1(const int m, const int n, const int kl, const int ku,
+                                         const sgb_complex_double *a, const int lda,
+                                         double *norm1)
+{
+    return gbnorm1(__func__, m, n, kl, ku, reinterpret_cast<const double2 *>(a), lda, norm1);
+}
+
+extern "C" int suzerain_blasext_dgbnorm1(const int m, const int n, const int kl, const int ku,
+                                         const double *a, const int lda, double *norm1)
+{
+    return gbnorm1(__func__, m, n, kl, ku, a, lda, norm1);
 }

@@ -758,9 +758,134 @@ int zgbsvx_batched(const GbsvxArgs &A, cudaStream_t st)
     return 0;
 }
 
+// ZGBCON alone: the reciprocal condition number in the 1-norm (norm '1' or
+// 'O') or the infinity-norm ('I') from a factor in LAPACK gbtrf storage
+// (device afb, ipiv) and the norm of the unfactored matrix (host anorm, one
+// per system); rcond out on the host.  The same estimator loop as the
+// expert driver's condition estimate.
+int zgbcon_batched(char norm, int nsys, const FactorGeom &g, const double2 *afb, int ldafb,
+                   long long afb_stride, const int *ipiv, const double *anorm, double *rcond,
+                   cudaStream_t st)
+{
+    const int N = g.N;
+    if (nsys == 0) return 0;
+    const bool onenrm = norm == '1' || norm == 'O';
+    const size_t vec = (size_t) nsys * N;
+    std::vector<void *> tmp;
+    auto take = [&](size_t bytes) -> void * {
+        void *p = nullptr;
+        if (cudaMalloc(&p, bytes) != cudaSuccess) return nullptr;
+        tmp.push_back(p);
+        return p;
+    };
+    auto cleanup = [&]() { for (void *p : tmp) cudaFree(p); tmp.clear(); };
+#define GC_TRY(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) { cleanup(); return sgb_set_error(e_, #x, __FILE__, __LINE__); } } while (0)
+    SysScal *sc = (SysScal *) take(nsys * sizeof(SysScal));
+    double2 *fac = (double2 *) take((size_t) nsys * g.fac_elems() * sizeof(double2));
+    double2 *xe = (double2 *) take(vec * sizeof(double2));
+    double2 *ve = (double2 *) take(vec * sizeof(double2));
+    int *kase = (int *) take(nsys * sizeof(int));
+    int *info = (int *) take(nsys * sizeof(int));
+    if (tmp.size() != 6) {
+        cleanup();
+        return sgb_set_error(cudaErrorMemoryAllocation, "zgbcon_batched workspace", __FILE__, __LINE__);
+    }
+    std::vector<SysScal> hs(nsys);
+    std::memset(hs.data(), 0, nsys * sizeof(SysScal));
+    for (int s = 0; s < nsys; ++s) hs[s].anorm = anorm[s];
+    GC_TRY(cudaMemcpyAsync(sc, hs.data(), nsys * sizeof(SysScal), cudaMemcpyHostToDevice, st));
+    GC_TRY(cudaMemsetAsync(info, 0, nsys * sizeof(int), st));
+    const unsigned cg = (unsigned) ((size_t) nsys * N);
+    count_launch(2);
+    k_afb_to_fac<<<cg, 64, 0, st>>>(nsys, g, afb, ldafb, afb_stride, fac);
+    GC_TRY(cudaGetLastError());
+    const int T = 128, B = (nsys + T - 1) / T;
+    k_start_est<<<B, T, 0, st>>>(nsys, sc, info);
+    GC_TRY(cudaGetLastError());
+    auto apply = [&](char tr, int want) -> cudaError_t {
+        GbtrsArgs a;
+        a.prec = 'Z'; a.trans = tr; a.g = g; a.nsys = nsys; a.fac = fac;
+        a.fac_stride = g.fac_elems(); a.ipiv = ipiv; a.b = xe; a.b_stride = N;
+        a.x = xe; a.x_stride = N; a.status = kase; a.status_want = want;
+        count_launch(1);
+        return launch_gbtrs(a, st);
+    };
+    // kase 1 applies A^{-1} for the 1-norm and A^{-H} for the infinity-norm
+    const char op1 = onenrm ? 'N' : 'C', op2 = onenrm ? 'C' : 'N';
+    std::vector<int> hk(nsys);
+    for (int round = 0; round < 16; ++round) {
+        count_launch(1);
+        k_lacn2<<<nsys, 32, 0, st>>>(nsys, N, xe, ve, sc, kase);
+        GC_TRY(cudaGetLastError());
+        GC_TRY(cudaMemcpyAsync(hk.data(), kase, nsys * sizeof(int), cudaMemcpyDeviceToHost, st));
+        GC_TRY(cudaStreamSynchronize(st));
+        bool any = false;
+        for (int k : hk) any |= k != 0;
+        if (!any) break;
+        GC_TRY(apply(op1, 1));
+        GC_TRY(apply(op2, 2));
+    }
+    GC_TRY(cudaMemcpyAsync(hs.data(), sc, nsys * sizeof(SysScal), cudaMemcpyDeviceToHost, st));
+    GC_TRY(cudaStreamSynchronize(st));
+    for (int s = 0; s < nsys; ++s)
+        rcond[s] = (anorm[s] == 0 || hs[s].est == 0) ? 0.0 : (1.0 / hs[s].est) / anorm[s];
+    cleanup();
+#undef GC_TRY
+    return 0;
+}
+
 }  // namespace sgb
 
 using namespace sgb;
+
+// LAPACK ZGBCON (the routine suzerain_lapack_zgbcon forwards to,
+// suzerain/blas_et_al/lapack.c): argument errors as LAPACK's -i, n = 0 gives
+// rcond 1, anorm = 0 gives 0.  ab is the gbtrf factor (ld >= 2 kl + ku + 1),
+// host or device; work and rwork are not used.
+extern "C" int suzerain_lapack_zgbcon(const char norm_in, const int n, const int kl, const int ku,
+                                      const sgb_complex_double *ab, const int ldab,
+                                      const int *ipiv, const double anorm, double *rcond,
+                                      sgb_complex_double *work, double *rwork)
+{
+    (void) work; (void) rwork;
+    const char norm = (char) std::toupper((unsigned char) norm_in);
+    if (norm != '1' && norm != 'O' && norm != 'I') return -1;
+    if (n < 0) return -2;
+    if (kl < 0) return -3;
+    if (ku < 0) return -4;
+    if (ldab < 2 * kl + ku + 1) return -6;
+    if (anorm < 0) return -8;
+    if (!rcond) return -9;
+    *rcond = 0;
+    if (n == 0) { *rcond = 1; return 0; }
+    if (anorm == 0) return 0;
+    if (kl + 1 > 64 || kl + ku + 1 > 192)
+        return sgb_set_error(cudaErrorNotSupported, "suzerain_lapack_zgbcon: bandwidth beyond KL < 64, KL + KU < 192", __FILE__, __LINE__);
+    const size_t fb = (size_t) ldab * n * sizeof(double2), pb = (size_t) n * sizeof(int);
+    void *dab = nullptr, *dpv = nullptr;
+    cudaPointerAttributes at;
+    const bool dev_ab = cudaPointerGetAttributes(&at, ab) == cudaSuccess &&
+                        (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged);
+    cudaGetLastError();
+    const bool dev_pv = cudaPointerGetAttributes(&at, ipiv) == cudaSuccess &&
+                        (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged);
+    cudaGetLastError();
+    cudaError_t e = cudaSuccess;
+    if (dev_ab) dab = (void *) ab;
+    else if ((e = cudaMalloc(&dab, fb)) == cudaSuccess) e = cudaMemcpy(dab, ab, fb, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        if (dev_pv) dpv = (void *) ipiv;
+        else if ((e = cudaMalloc(&dpv, pb)) == cudaSuccess) e = cudaMemcpy(dpv, ipiv, pb, cudaMemcpyHostToDevice);
+    }
+    int rc = 0;
+    if (e == cudaSuccess)
+        rc = zgbcon_batched(norm, 1, FactorGeom{n, kl, ku}, (const double2 *) dab, ldab,
+                            (long long) ldab * n, (const int *) dpv, &anorm, rcond, 0);
+    if (!dev_ab && dab) cudaFree(dab);
+    if (!dev_pv && dpv) cudaFree(dpv);
+    if (e != cudaSuccess) return sgb_set_error(e, "suzerain_lapack_zgbcon", __FILE__, __LINE__);
+    return rc;
+}
 
 extern "C" int sgb_zgbsvx_batched(char fact, char trans, int nsys, int n, int kl, int ku,
                                   sgb_complex_double *ab, int ldab, long long ab_stride,

@@ -1214,51 +1214,6 @@ extern "C" int suzerain_blas_zgbmv(const char trans_, const int m, const int n, 
     return err_of(e, "suzerain_blas_zgbmv");
 }
 
-// y <- alpha D^m x + beta y via the stored transpose D_T ('T' gbmv with a
-// real band, suzerain/bsplineop.c:261-298).
-extern "C" int suzerain_bsplineop_accumulate_complex(int nderiv, int nrhs,
-                                                     const sgb_complex_double alpha,
-                                                     const sgb_complex_double *x, int incx, int ldx,
-                                                     const sgb_complex_double beta,
-                                                     sgb_complex_double *y, int incy, int ldy,
-                                                     const suzerain_bsplineop_workspace *w)
-{
-    if (!w || nderiv < 0 || w->nderiv < nderiv) return -1;
-    if (nrhs > 1 && ldx < w->n) return -1;
-    if (nrhs > 1 && ldy < w->n) return -1;
-    if ((const void *) x == (const void *) y) return -1;
-    const int n = w->n;
-    double2 al, be;
-    std::memcpy(&al, &alpha, sizeof al);
-    std::memcpy(&be, &beta, sizeof be);
-    // D_T[nderiv] with its own kl/ku is offset inside storage of leading dim ld
-    const double *band = w->D_T[nderiv];
-    double *dband = nullptr;
-    cudaError_t e = cudaMalloc(&dband, (size_t) w->ld * n * sizeof(double));
-    if (e != cudaSuccess) return err_of(e, "cudaMalloc(bsplineop band)");
-    // copy the operator's own view: rows 0..kl+ku of each column
-    std::vector<double> hb((size_t) w->ld * n, 0.0);
-    for (int j = 0; j < n; ++j)
-        for (int r = 0; r < w->kl[nderiv] + 1 + w->ku[nderiv]; ++r)
-            hb[(size_t) j * w->ld + r] = band[(size_t) j * w->ld + r];
-    e = cudaMemcpy(dband, hb.data(), hb.size() * sizeof(double), cudaMemcpyHostToDevice);
-    for (int j = 0; j < nrhs && e == cudaSuccess; ++j) {
-        Stage sx(x + (size_t) j * ldx, span_bytes(n, incx, sizeof(double2)), true);
-        Stage sy(y + (size_t) j * ldy, span_bytes(n, incy, sizeof(double2)), true);
-        if (sx.err || sy.err) { e = cudaErrorMemoryAllocation; break; }
-        const int kx = incx > 0 ? 0 : (1 - n) * incx, ky = incy > 0 ? 0 : (1 - n) * incy;
-        k_gbmv<double><<<(n + 127) / 128, 128>>>(1, n, n, w->kl[nderiv], w->ku[nderiv], al, dband,
-                                                w->ld, (const double2 *) sx.dev, incx, kx, be,
-                                                (double2 *) sy.dev, incy, ky,
-                                                be.x == 1 && be.y == 0, be.x == 0 && be.y == 0);
-        e = cudaGetLastError();
-        if (e == cudaSuccess) e = cudaDeviceSynchronize();
-        if (e == cudaSuccess) e = sy.back();
-    }
-    cudaFree(dband);
-    return err_of(e, "suzerain_bsplineop_accumulate_complex");
-}
-
 // ---------------------------------------------------------------------------
 // diffwave_apply (suzerain/diffwave.c:66-131)
 // ---------------------------------------------------------------------------

@@ -129,5 +129,10 @@ struct GbsvxArgs {
     int *info = nullptr;         // device
 };
 int zgbsvx_batched(const GbsvxArgs &a, cudaStream_t st);
+// Batched ZGBCON from gbtrf storage (device afb, ipiv); anorm and rcond on
+// the host, one per system.
+int zgbcon_batched(char norm, int nsys, const FactorGeom &g, const double2 *afb, int ldafb,
+                   long long afb_stride, const int *ipiv, const double *anorm, double *rcond,
+                   cudaStream_t st);
 
 }  // namespace sgb

@@ -12,6 +12,12 @@ solve path with, and writes it as JSON fixtures:
   bsplineop_kat.json tests/test_bsplineop.cpp
                        transposed mass band of order-3 B-splines on
                        {0,1,2,3} and its complex apply (:465-540).
+  bsplineop_luz_kat.json tests/test_bsplineop.cpp
+                       the complex operator (2-3i) D0 + (7-5i) D1 +
+                       (999-999i) D2 of order-2 B-splines on {0,1,2,3}:
+                       its solves against the unit basis vectors and two
+                       right-hand sides, contiguous and with incb 2
+                       (:340-462, Octave rationals).
 
 Rational entries such as 1024.0/3125.0 are evaluated exactly with
 fractions.Fraction and rounded once to double.  Run from the repository root:
@@ -87,9 +93,36 @@ def bsplineop_kat(ref: str) -> dict:
                                    [7.25, 8.25], [9., 10.]]}
 
 
+def _pairs(sect: str, name: str) -> list[list[float]]:
+    m = re.search(re.escape(name) + r"\[\]\[2\]\s*=\s*\{(.*?)\};", sect, re.S)
+    if not m:
+        raise KeyError(name)
+    body = re.sub(r"//[^\n]*", "", m.group(1))
+    return [[_num(a), _num(b)] for a, b in re.findall(r"\{([^,{}]+),([^,{}]+)\}", body)]
+
+
+def bsplineop_luz_kat(ref: str) -> dict:
+    src = open(os.path.join(ref, "tests", "test_bsplineop.cpp")).read()
+    case = src[src.index("BOOST_AUTO_TEST_CASE( collocation_piecewise_linear )"):
+               src.index("BOOST_AUTO_TEST_CASE( collocation_piecewise_quadratic)")]
+    marks = ['BOOST_TEST_MESSAGE("suzerain_bspline_luz_form")',
+             'BOOST_TEST_MESSAGE("suzerain_bspline_luz_solve contiguous")',
+             'BOOST_TEST_MESSAGE("suzerain_bspline_luz_solve noncontiguous")']
+    sects = [case[case.index(marks[i]):case.index(marks[i + 1]) if i + 1 < 3 else len(case)]
+             for i in range(3)]
+    solves = []
+    for sect, nrhs, incb in zip(sects, (8, 2, 2), (1, 1, 2)):
+        solves.append({"nrhs": nrhs, "incb": incb, "b": _pairs(sect, "b"),
+                       "b_good": _pairs(sect, "b_good"), "tolerance": 1e-5})
+    return {"source": "tests/test_bsplineop.cpp",
+            "k": 2, "breakpoints": [0.0, 1.0, 2.0, 3.0], "nderiv": 2, "n": 4,
+            "coefficients": _pairs(sects[0], "coeff"), "solves": solves}
+
+
 def main(ref: str) -> None:
     for name, fn in (("bsmbsm_kat.json", bsmbsm_kat),
-                     ("bsplineop_kat.json", bsplineop_kat)):
+                     ("bsplineop_kat.json", bsplineop_kat),
+                     ("bsplineop_luz_kat.json", bsplineop_luz_kat)):
         with open(os.path.join(HERE, name), "w") as f:
             json.dump(fn(ref), f, indent=1)
         print("wrote", name)

@@ -116,6 +116,33 @@ def test_bsplineop_workspace_golden_k3(native):
         native.suzerain_bsplineop_free(w)
 
 
+def test_bsplineop_luz_golden_dense(native, oracle):
+    """tests/test_bsplineop.cpp:340-462 restated densely on the host: the
+    operator (2-3i) D0 + (7-5i) D1 + (999-999i) D2 of the order-2 basis on
+    {0,1,2,3}, from this library's collocation bands, solves the reference's
+    right-hand sides to its Octave rationals within its 1e-5 (pins the
+    fixture the GPU luz test uses and the oracle's operator restatement)."""
+    d = json.load(open(os.path.join(GOLD, "bsplineop_luz_kat.json")))
+    bp = np.array(d["breakpoints"])
+    w = native.sgb_bsplineop_alloc_breakpoints(d["k"], len(bp), bp.ctypes.data, d["nderiv"])
+    try:
+        coef = [complex(a, b) for a, b in d["coefficients"]]
+        A = oracle.bsplineop_operator(oracle.bsplineop_transposes(w), coef).T
+        n = d["n"]
+        assert A.shape == (n, n)
+        for sv in d["solves"]:
+            b = np.array([complex(a, c) for a, c in sv["b"]])
+            good = np.array([complex(a, c) for a, c in sv["b_good"]])
+            ldb, inc = len(b) // sv["nrhs"], sv["incb"]
+            x = b.copy()
+            for c in range(sv["nrhs"]):
+                s = slice(c * ldb, c * ldb + n * inc, inc)
+                x[s] = np.linalg.solve(A, b[s])
+            assert np.abs(x - good).max() <= sv["tolerance"]
+    finally:
+        native.suzerain_bsplineop_free(w)
+
+
 @pytest.mark.parametrize("Ny,k", [(48, 8), (192, 8), (32, 6), (256, 6)])
 def test_collocation_matches_scipy(native, Ny, k):
     interp = pytest.importorskip("scipy.interpolate")
