@@ -425,6 +425,7 @@ def run_ours(args):
     clocks = sampler.stop()
     ms = max_over_ranks(e0.elapsed_time(e1), world, "cuda")
     value = nsys * world * args.steps / (ms / 1e3)
+    async_faults = L.sgb_async_faults()
 
     if args.profile_step:
         # profiling runs: the warm-up and timed substeps only, then exit, so
@@ -552,7 +553,8 @@ def run_ours(args):
                        "parallelism": f"wavenumber blocks x{world}",
                        "parts": parts,
                        "l2": "inputs larger than L2 (u 380 MB, factors 20 GB)"},
-            "rel_resid_max": float(berr.max()), "all_converged": ok,
+            "rel_resid_max": float(berr.max()), "all_converged": ok and async_faults == 0,
+            "async_faults": async_faults,
             "fact_double": rep["fact"].count("D"),
             "siter_mean": float(rep["siter"].mean()),
             "gpu_launches": int(launches),

@@ -713,6 +713,16 @@ int sgb_zgbsvx_batched(char fact, char trans, int nsys, int n, int kl, int ku,
  *  keeps the current value; defaults 2 and 2).  Returns -1 for other values.
  *  Process-wide; results do not depend on it. */
 int sgb_gbtrs_set_quad_depth(int fwd, int bwd);
+/** Backward quad-lane solve, rows per factor record: 2 (the default), 4 or
+ *  8 consecutive U rows arrive by one bulk copy (1-D TMA, completion on an
+ *  mbarrier) per record and system; 0 or 1: one row by 16-byte cp.async
+ *  spread over the system's four lanes.  Results are identical. */
+int sgb_gbtrs_set_quad_bulk(int rows);
+/** Kernels that wait on asynchronous copies bound every wait; one whose
+ *  wait ran out records a fault (its results are invalid).  Returns the
+ *  number recorded since the last call (0 or 1) and clears the record; -1
+ *  if the device cannot be read. */
+int sgb_async_faults(void);
 
 /** Row-panel factor -> LAPACK gbtrf storage ((2KL+KU+1) x N per system). */
 int sgb_factor_to_lapack(char prec, int nsys, int N, int KL, int KU,

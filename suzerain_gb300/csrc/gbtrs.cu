@@ -10,8 +10,10 @@
 // optionally scattered to natural order x[q(i)] (suzerain_bsmbsm_zaPxpby 'T').
 //
 // The sweeps are sequential in j, so each step's factor row (or column, and
-// its pivot) must not wait on HBM: a ring of PD rows in shared memory is
-// filled by cp.async PD steps ahead of its use.
+// its pivot) must not wait on HBM: a ring of PD records in shared memory is
+// filled PD records ahead of its use, by cp.async or, for the backward
+// quad solve, by one bulk copy (1-D TMA) of two consecutive U rows per
+// record completing on an mbarrier.
 #include "sgb_internal.h"
 
 #include <algorithm>
@@ -37,6 +39,40 @@ __device__ __forceinline__ void cp_int(int *dst, const int *src)
 __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// One-dimensional bulk copy (TMA) of `bytes` (a multiple of 16, both
+// addresses 16-byte aligned) from global into this CTA's shared memory,
+// completing on the mbarrier at `bar` (the issuing lane declares the bytes).
+__device__ __forceinline__ void bulk_to_smem(void *dst, const void *src, unsigned bytes, unsigned bar)
+{
+    const unsigned d = (unsigned) __cvta_generic_to_shared(dst);
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(bytes)
+                 : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n"
+                 ::"r"(d), "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+}
+__device__ __forceinline__ void mbar_init(unsigned bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(bar), "r"(count) : "memory");
+}
+// Waits for phase `parity` of the mbarrier, at most `limit` polls; false on
+// time-out (the caller records a fault and stops).
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity, int limit = 1 << 20)
+{
+    for (int i = 0; i < limit; ++i) {
+        unsigned done;
+        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                     " selp.u32 %0, 1, 0, p;\n}\n"
+                     : "=r"(done) : "r"(bar), "r"(parity) : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// Set by a kernel whose bounded wait on an asynchronous copy ran out (its
+// results are then invalid); read and cleared by sgb_async_faults().
+__device__ int g_async_fault = 0;
 
 // Prefetch depth (sweep steps in flight) per precision.
 template <typename R> __host__ __device__ constexpr int gbtrs_depth() { return sizeof(R) == 8 ? 4 : 8; }
@@ -236,6 +272,13 @@ __host__ __device__ inline int quad_pad(int e) { return e + ((4 - e % 16) + 16) 
 // forward + backward 4.6 ms at depth 2, 6.3 ms at 8 / 4, 8.6 ms at 16 / 8).
 static int g_qdepth[2] = {2, 2};
 static bool quad_depth_ok(int d) { return d == 2 || d == 4 || d == 8 || d == 16; }
+// Backward quad solve: records of 1 row by 16-byte cp.async over the
+// system's four lanes (g_qbulk 0 or 1), or of 2, 4 or 8 consecutive rows by
+// one bulk copy (TMA) per record and system.  Measured on the GB300 at
+// N = 960, KL = KU = 34, complex64, 24,768 systems (backsolve / correction
+// solve): 1 row 2.83 / 4.75 ms, 2 rows 2.72 / 4.65 ms, 4 rows 3.25 / 5.21 ms,
+// 8 rows 6.06 / 8.34 ms (larger records leave fewer warps per SM).
+static int g_qbulk = 2;
 
 // A factor segment of n complex elements starting at element e (from the
 // base pointer `base`) is copied with 16-byte cp.async: complex128 element by
@@ -281,13 +324,14 @@ struct QuadFwdLayout {
         SE = quad_pad((bytes + EB - 1) / EB);
     }
 };
-template <typename R, int PD>
+template <typename R, int PD, int RB = 1>
 struct QuadBwdLayout {
-    int XW, RP, SE;       // mirrored window (2 x (KV+3) ring), record, stride
+    int XW, SPAN, RP, SE; // mirrored window (2 x (KV+3) ring), rows' span, record, stride
     __host__ __device__ QuadBwdLayout(const FactorGeom &g)
     {
         XW = g.UW() + 2;
-        RP = quad_span<R>(g.UW()) + 1;      // U row span, then y_j
+        SPAN = quad_span<R>(RB * g.UW());   // RB consecutive U rows, then their y
+        RP = SPAN + RB;
         RP += RP & 1;
         SE = quad_pad(2 * XW + PD * RP);
     }
@@ -376,13 +420,18 @@ k_gbtrs_fwd_quad(FactorGeom g, int nsys, const cplx_t<R> *__restrict__ fac, long
     if (act && q == 0) ys[N - 1] = xw[(N - 1) & m];
 }
 
-template <typename R, bool ACCUM, int PD>
+template <typename R, bool ACCUM, int PD, int RB>
 __global__ void __launch_bounds__(32)
 k_gbtrs_bwd_quad(FactorGeom g, int nsys, const cplx_t<R> *__restrict__ fac, long long fac_stride,
                  cplx_t<R> *__restrict__ yw, double2 *__restrict__ x, long long x_stride,
                  const int *__restrict__ sys_list, int nlist, const int *__restrict__ d_count,
                  bool slot_mode, const int *__restrict__ status, int status_want, int unS, int unn)
 {
+    // RB == 1: each record (one U row and its y) by 16-byte cp.async over the
+    // system's four lanes; RB > 1: each record holds RB consecutive rows,
+    // fetched by one bulk copy (1-D TMA) issued by the system's lane 0 and
+    // completing on the record slot's mbarrier, and their y by cp.async.
+    constexpr bool BULK = RB > 1;
     using T2 = cplx_t<R>;
     const int lane = threadIdx.x, sub = lane >> 2, q = lane & 3;
     const int pos = blockIdx.x * QSYS + sub;
@@ -391,36 +440,80 @@ k_gbtrs_bwd_quad(FactorGeom g, int nsys, const cplx_t<R> *__restrict__ fac, long
     if (!__any_sync(0xffffffffu, act)) return;
     const long long fi = slot_mode ? (long long) pos : (long long) s;
     const int N = g.N, UW = g.UW(), KV = UW - 1;
-    const QuadBwdLayout<R, PD> L(g);
+    const QuadBwdLayout<R, PD, RB> L(g);
     const int XW = L.XW;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     // x window: ring of XW = KV+3 slots (row r at r mod XW), stored twice so
     // that rows j+1 .. j+KV+3 are contiguous from slot(j+1)
     T2 *xw = reinterpret_cast<T2 *>(smem_raw) + sub * L.SE;
     T2 *rec = xw + 2 * XW;                                        // PD x RP
+    // BULK: one mbarrier per record slot of each system, after the systems' areas
+    unsigned long long *mb = reinterpret_cast<unsigned long long *>(
+        reinterpret_cast<T2 *>(smem_raw) + QSYS * L.SE) + sub * PD;
+    const unsigned mb0 = (unsigned) __cvta_generic_to_shared(mb);
     const long long ubase = fi * fac_stride;
     T2 *ys = act ? yw + (long long) s * N : nullptr;
     const T2 zero = mk<R>(R(0), R(0));
+    // offset of element e within its record: complex64 copies start at the
+    // aligned pair holding e
+    auto el_off = [&](long long e) { return (int) (e & (sizeof(R) == 8 ? 0 : 1)); };
 
-    auto fetch = [&](int j) {
-        if (act && j >= 0) {
-            T2 *d = rec + (j % PD) * L.RP;
-            quad_copy<R>(d, fac, ubase + (long long) j * UW, UW, q);
-            if (q == 3) cp_el<R>(d + L.RP - 1, ys + j);
+    // record b: rows hi = N-1-b RB down to lo = max(0, hi-RB+1), into slot
+    // b % PD; the rows' elements from offset el_off(e0), then y_lo .. y_hi
+    auto fetch = [&](int b) {
+        const int hi = N - 1 - b * RB, lo = imax(0, hi - RB + 1);
+        if (act && hi >= 0) {
+            T2 *d = rec + (b % PD) * L.RP;
+            const long long e0 = ubase + (long long) lo * UW;
+            const int cnt = (hi - lo + 1) * UW;
+            if constexpr (BULK) {
+                if (q == 0) {
+                    const int off = el_off(e0);
+                    const unsigned bytes = sizeof(R) == 8 ? (unsigned) cnt * 16u
+                                                          : (unsigned) ((cnt + off + 1) >> 1) * 16u;
+                    bulk_to_smem(d, fac + (e0 - off), bytes, mb0 + 8u * (unsigned) (b % PD));
+                }
+            } else {
+                quad_copy<R>(d, fac, e0, cnt, q);
+            }
+            for (int r = q; r <= hi - lo; r += 4) cp_el<R>(d + L.SPAN + r, ys + lo + r);
         }
         cp_commit();
     };
+    if constexpr (BULK) {
+        if (q == 0)
+            for (int p = 0; p < PD; ++p) mbar_init(mb0 + 8u * p, 1);
+        __syncwarp();
+    }
     // rows >= N (and never-written slots) read as zeros
     for (int i = q; i < 2 * XW; i += 4) xw[i] = zero;
 #pragma unroll 1
-    for (int t = 0; t < PD; ++t) fetch(N - 1 - t);
+    for (int b = 0; b < PD; ++b) fetch(b);
     const int T = (KV + 3) >> 2;          // terms per lane; only the last may pass KV
+    const int nblk = (N + RB - 1) / RB;
     int slot = (N - 1) % XW;              // slot of row j
     for (int j = N - 1; j >= 0; --j) {
-        cp_wait<PD - 1>();
-        __syncwarp();
-        const T2 *rj = rec + (j % PD) * L.RP;
-        const T2 *ur = rj + (int) ((ubase + (long long) j * UW) & (sizeof(R) == 8 ? 0 : 1));
+        const int tj = N - 1 - j, b = tj / RB, hi = N - 1 - b * RB, lo = imax(0, hi - RB + 1);
+        if (j == hi) {                    // first row of record b: wait for it
+            cp_wait<PD - 1>();
+            if constexpr (BULK) {
+                const bool ok = !act || mbar_wait(mb0 + 8u * (unsigned) (b % PD), (unsigned) ((b / PD) & 1));
+                if (__any_sync(0xffffffffu, !ok)) {
+                    // a copy did not complete: record the fault, let the
+                    // copies still in flight land (bounded), and stop
+                    if (lane == 0) atomicExch(&g_async_fault, 1);
+                    if (act && q == 0)
+                        for (int p = 1; p < PD && b + p < nblk; ++p)
+                            mbar_wait(mb0 + 8u * (unsigned) ((b + p) % PD), (unsigned) (((b + p) / PD) & 1));
+                    cp_wait<0>();
+                    return;
+                }
+            }
+            __syncwarp();
+        }
+        const T2 *rb = rec + (b % PD) * L.RP;
+        const T2 *rj = rb + L.SPAN + (j - lo) - (L.RP - 1);   // rj[L.RP - 1] = y_j
+        const T2 *ur = rb + el_off(ubase + (long long) lo * UW) + (j - lo) * UW;
         const int s1 = slot + 1 == XW ? 0 : slot + 1;
         const T2 *xr = xw + s1 - 1;                   // xr[k] = x_{j+k}, k = 1 .. KV+3
         T2 a0 = zero, a1 = zero, a2 = zero, a3 = zero;
@@ -448,7 +541,7 @@ k_gbtrs_bwd_quad(FactorGeom g, int nsys, const cplx_t<R> *__restrict__ fac, long
             if (act) ys[j] = xj;
         }
         __syncwarp();
-        fetch(j - PD);
+        if (j == lo) fetch(b + PD);       // record b consumed: its slot takes b + PD
         slot = slot == 0 ? XW - 1 : slot - 1;
     }
     cp_wait<0>();
@@ -466,6 +559,21 @@ k_gbtrs_bwd_quad(FactorGeom g, int nsys, const cplx_t<R> *__restrict__ fac, long
             else *dst = v;
         }
     }
+}
+
+template <typename R, int PB, int RB>
+static cudaError_t launch_quad_bwd(const GbtrsArgs &a, cplx_t<R> *yw, int grid, cudaStream_t st)
+{
+    using T2 = cplx_t<R>;
+    const QuadBwdLayout<R, PB, RB> L(a.g);
+    const size_t smem = (size_t) QSYS * L.SE * sizeof(T2) + (size_t) QSYS * PB * 8;
+    auto kern = a.accumulate ? k_gbtrs_bwd_quad<R, true, PB, RB> : k_gbtrs_bwd_quad<R, false, PB, RB>;
+    cudaError_t e = smem_attr((const void *) kern, smem);
+    if (e != cudaSuccess) return e;
+    kern<<<grid, 32, smem, st>>>(a.g, a.nsys, reinterpret_cast<const T2 *>(a.fac), a.fac_stride, yw,
+                                 a.x, a.x_stride, a.sys_list, a.nlist, a.d_count, a.slot_mode,
+                                 a.status, a.status_want, a.unpermute_S, a.unpermute_n);
+    return cudaGetLastError();
 }
 
 template <typename R, int PF, int PB>
@@ -489,15 +597,12 @@ static cudaError_t launch_quad_d(const GbtrsArgs &a, cudaStream_t st)
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
-    const QuadBwdLayout<R, PB> L(a.g);
-    const size_t smem = (size_t) QSYS * L.SE * sizeof(T2);
-    auto kern = a.accumulate ? k_gbtrs_bwd_quad<R, true, PB> : k_gbtrs_bwd_quad<R, false, PB>;
-    e = smem_attr((const void *) kern, smem);
-    if (e != cudaSuccess) return e;
-    kern<<<grid, 32, smem, st>>>(a.g, a.nsys, reinterpret_cast<const T2 *>(a.fac), a.fac_stride, yw,
-                                 a.x, a.x_stride, a.sys_list, a.nlist, a.d_count, a.slot_mode,
-                                 a.status, a.status_want, a.unpermute_S, a.unpermute_n);
-    return cudaGetLastError();
+    switch (g_qbulk) {
+    case 2: return launch_quad_bwd<R, PB, 2>(a, yw, grid, st);
+    case 4: return launch_quad_bwd<R, PB, 4>(a, yw, grid, st);
+    case 8: return launch_quad_bwd<R, PB, 8>(a, yw, grid, st);
+    default: return launch_quad_bwd<R, PB, 1>(a, yw, grid, st);
+    }
 }
 
 template <typename R, int PF>
@@ -532,14 +637,24 @@ static size_t quad_fwd_se(const FactorGeom &g)
     default: return QuadFwdLayout<R, 2>(g).SE;
     }
 }
+template <typename R, int RB>
+static size_t quad_bwd_se_rb(const FactorGeom &g)
+{
+    switch (g_qdepth[1]) {
+    case 4: return QuadBwdLayout<R, 4, RB>(g).SE;
+    case 8: return QuadBwdLayout<R, 8, RB>(g).SE;
+    case 16: return QuadBwdLayout<R, 16, RB>(g).SE;
+    default: return QuadBwdLayout<R, 2, RB>(g).SE;
+    }
+}
 template <typename R>
 static size_t quad_bwd_se(const FactorGeom &g)
 {
-    switch (g_qdepth[1]) {
-    case 4: return QuadBwdLayout<R, 4>(g).SE;
-    case 8: return QuadBwdLayout<R, 8>(g).SE;
-    case 16: return QuadBwdLayout<R, 16>(g).SE;
-    default: return QuadBwdLayout<R, 2>(g).SE;
+    switch (g_qbulk) {
+    case 2: return quad_bwd_se_rb<R, 2>(g);
+    case 4: return quad_bwd_se_rb<R, 4>(g);
+    case 8: return quad_bwd_se_rb<R, 8>(g);
+    default: return quad_bwd_se_rb<R, 1>(g);
     }
 }
 
@@ -552,7 +667,7 @@ static bool quad_ok(const GbtrsArgs &a)
     const size_t el = a.prec == 'Z' ? 16 : 8;
     const size_t fwd = a.prec == 'Z' ? quad_fwd_se<double>(a.g) : quad_fwd_se<float>(a.g);
     const size_t bwd = a.prec == 'Z' ? quad_bwd_se<double>(a.g) : quad_bwd_se<float>(a.g);
-    return (size_t) QSYS * std::max(fwd, bwd) * el <= 227 * 1024;
+    return (size_t) QSYS * std::max(fwd, bwd) * el + (size_t) QSYS * 16 * 8 <= 227 * 1024;
 }
 
 template <typename R, int TRANS, bool FWD_DONE, bool ACCUM>
@@ -594,6 +709,29 @@ cudaError_t launch_gbtrs(const GbtrsArgs &a, cudaStream_t st)
 }
 
 }  // namespace sgb
+
+// Tuning knob: rows per record of the backward quad solve; 0 or 1: one row
+// by 16-byte cp.async, 2 (the default), 4 or 8: that many rows by one bulk
+// copy (TMA).
+extern "C" int sgb_gbtrs_set_quad_bulk(int rows)
+{
+    if (rows != 0 && rows != 1 && rows != 2 && rows != 4 && rows != 8) return -1;
+    sgb::g_qbulk = rows;
+    return 0;
+}
+
+// Faults recorded by kernels whose bounded waits on asynchronous copies ran
+// out since the last call (0 when none); clears the record.
+extern "C" int sgb_async_faults(void)
+{
+    int h = 0;
+    if (cudaMemcpyFromSymbol(&h, sgb::g_async_fault, sizeof h) != cudaSuccess) return -1;
+    if (h) {
+        const int z = 0;
+        cudaMemcpyToSymbol(sgb::g_async_fault, &z, sizeof z);
+    }
+    return h;
+}
 
 // Tuning knob: records in flight per system of the quad-lane solves
 // (2, 4, 8 or 16; 0 keeps the current value).

@@ -531,6 +531,45 @@ def test_plan_result_independent_of_factor_shape(lib, torch_cuda):
             assert np.array_equal(row[m], results[0][m])
 
 
+@pytest.mark.parametrize("config", [0, 2])
+def test_quad_solve_bulk_copies_match_cp_async(lib, torch_cuda, config):
+    """The backward quad solve fetching records of 2, 4 or 8 factor rows by
+    one bulk copy (TMA) per system gives the bits of the one-row 16-byte
+    cp.async form, for both methods and both precisions' factors
+    (configuration 0's geometry and a 512-system sample of configuration 2),
+    and records no wait time-out."""
+    torch = torch_cuda
+    from suzerain_gb300 import plan as P, synth
+    if config == 0:
+        c, cs, kx, kz, u = config0()
+    else:
+        c = synth.CONFIGS[2]
+        cs, kx, kz, u = c.batch()
+        kx, kz, u = kx[:512], kz[:512], u[:512]
+    assert lib.sgb_async_faults() == 0
+    out = {}
+    try:
+        for bulk in (1, 2, 4, 8):
+            assert lib.sgb_gbtrs_set_quad_bulk(bulk) == 0
+            pl = P.Plan(cs, kx, kz)
+            for method in ("Z", "M"):
+                a = torch.zeros(u.shape, dtype=torch.complex128, device="cuda")
+                pl.substep(method, 0.0, -c.phi, dev(torch, u), a, P.RefineSpec(tolsc=145.0))
+                b = torch.zeros_like(a)
+                pl.substep_capturable(method, 0.0, -c.phi, dev(torch, u), b, P.RefineSpec(tolsc=145.0))
+                torch.cuda.synchronize()
+                out[(bulk, method)] = (a.cpu().numpy(), b.cpu().numpy())
+            pl.close()
+    finally:
+        lib.sgb_gbtrs_set_quad_bulk(2)
+    assert lib.sgb_async_faults() == 0
+    for bulk in (2, 4, 8):
+        for method in ("Z", "M"):
+            for i in range(2):
+                assert np.array_equal(out[(bulk, method)][i], out[(1, method)][i]), (bulk, method)
+    assert lib.sgb_gbtrs_set_quad_bulk(3) != 0
+
+
 def test_plan_memory_reuse_waits_for_issued_work(lib, torch_cuda):
     """Plans take device memory from a pool that keeps freed blocks.  A plan
     destroyed right after issuing a substep on a side stream must not hand
