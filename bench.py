@@ -730,6 +730,89 @@ def run_config4(args) -> int:
     return 0
 
 
+def run_profile_kernels(args) -> int:
+    """Profiling runs of the kernels beside the headline substep, on the
+    first --nsys systems (default 4096) of configuration 2: the packed-band
+    assembly (sgb_plan_assemble_packed), the caller-packed mixed solve
+    (sgb_zcgbsvx_batched: factor from the packed band, packed FP64
+    residual), the FP64 backward-error check, and the production operator
+    (rholut_imexop, k = 8, Ny = 192, N = 960) packed and applied for as many
+    wavenumber pairs.  Each runs twice; prints one JSON line of CUDA-event
+    times and exits."""
+    import ctypes as C
+    import torch
+    rank, local, world = dist_env()
+    if world > 1 and rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    from suzerain_gb300 import build as B
+    B.build()
+    from suzerain_gb300 import _native as nat, plan as P, rholut, synth
+    L = nat.load()
+    if L.sgb_device_ok() != 0:
+        raise RuntimeError(nat.last_error())
+    nsys = args.nsys or 4096
+    cfg = synth.CONFIGS[2]
+    cs, kx, kz, u = cfg.batch()
+    kx, kz, u = kx[:nsys], kz[:nsys], u[:nsys]
+    phi_e, phi_i = synth.smr91_phis(cfg.phi)
+    N, LD = cs.N, cs.LD
+    stream = torch.cuda.current_stream()
+    out = {}
+
+    def ev(fn, reps=2):
+        fn()
+        torch.cuda.synchronize()
+        return timed(fn, reps, stream) / reps
+
+    pl = P.Plan(cs, kx, kz, max_double_slots=256)
+    ab = torch.empty((nsys, N * LD), dtype=torch.complex128, device="cuda")
+    out["assemble_packed_ms"] = ev(lambda: pl.assemble_packed(phi_i, ab, LD, 0, stream=stream.cuda_stream))
+    q = np.array([(i % cs.S) * cs.n + i // cs.S for i in range(N)])
+    b = torch.from_numpy(u).cuda()[:, torch.from_numpy(q).cuda()].contiguous()
+    x = torch.empty_like(b)
+    rep = {k: torch.zeros(nsys, dtype=t, device="cuda") for k, t in
+           (("info", torch.int32), ("siter", torch.int32), ("diter", torch.int32),
+            ("res", torch.float64), ("tolsc", torch.float64), ("fact", torch.uint8))}
+    R = nat.RefineReport(*(rep[k].data_ptr() for k in ("info", "siter", "diter", "res",
+                                                         "tolsc", "fact")))
+    S = nat.RefineSpec(SPEC["aiter"], SPEC["siter"], SPEC["diter"], cfg.tolsc)
+    out["packed_zcgbsvx_ms"] = ev(lambda: nat.check(L.sgb_zcgbsvx_batched(
+        nsys, N, cs.KL, cs.KU, b"N", ab.data_ptr(), LD, LD * N, b.data_ptr(), x.data_ptr(),
+        C.byref(S), C.byref(R), stream.cuda_stream), "sgb_zcgbsvx_batched"))
+    del ab, b, x
+    du = torch.from_numpy(u).cuda()
+    dout = torch.empty_like(du)
+    pl.substep("M", phi_e, phi_i, du, dout, P.RefineSpec(**{**SPEC, "tolsc": cfg.tolsc}),
+               stream=stream.cuda_stream)
+    out["backward_error_ms"] = ev(lambda: pl.backward_error(stream=stream.cuda_stream))
+    pl.close()
+    del du, dout
+    torch.cuda.empty_cache()
+    # production operator on the configuration-2 wall-normal geometry
+    Ny, k = 192, 8
+    x01 = np.linspace(0, 1, Ny - k + 2)
+    bp = np.array([2 * L.suzerain_htstretch2(2.0, 1.0, float(t)) for t in x01])
+    w = L.sgb_bsplineop_alloc_breakpoints(k, len(bp), bp.ctypes.data, 2)
+    y = np.linspace(0, 2, Ny)
+    prof = {nm: 0.2 * (1 + 0.3 * np.sin((i + 1) * y)) for i, nm in enumerate(rholut.PROFILES)}
+    prof["nu"] = 1 + 0.1 * np.cos(y)
+    op = rholut.Operator(dict(Re=3000.0, Pr=0.7, Ma=1.5, alpha=3.0, gamma=1.4), prof, w)
+    g = op.geometry
+    km = torch.from_numpy(np.asarray(kx, dtype=np.float64)).cuda()
+    kn = torch.from_numpy(np.asarray(kz, dtype=np.float64)).cuda()
+    pab = torch.empty((nsys, g.N * g.LD), dtype=torch.complex128, device="cuda")
+    out["rholut_pack_ms"] = ev(lambda: op.pack(complex(phi_i, 0), km, kn, pab, stream=stream.cuda_stream))
+    xt = torch.from_numpy(u).cuda()
+    yt = torch.empty_like(xt)
+    out["rholut_accumulate_ms"] = ev(lambda: op.accumulate(complex(phi_e, 0), km, kn, xt, 0, yt,
+                                                           stream=stream.cuda_stream))
+    op.close()
+    L.suzerain_bsplineop_free(w)
+    print(json.dumps({"profile_kernels": True, "nsys": nsys, "N": N, **out}))
+    return 0
+
+
 def run_peaks(args) -> int:
     """Pipe-throughput microbenchmarks of this GPU (FP64 FMA, FP32 FMA, packed
     FP32 FMA, shared-memory loads) with the clocks seen meanwhile: the
@@ -806,9 +889,13 @@ def main():
                     help="run the warm-up and timed substeps only (launch lists)")
     ap.add_argument("--peaks", action="store_true",
                     help="print this GPU's pipe-throughput microbenchmarks and exit")
+    ap.add_argument("--profile-kernels", action="store_true",
+                    help="run the kernels beside the headline substep once each (profiling)")
     args = ap.parse_args()
     if args.peaks:
         return run_peaks(args)
+    if args.profile_kernels:
+        return run_profile_kernels(args)
     if args.impl == "reference":
         return run_reference(args)
     if args.config == 3:

@@ -844,7 +844,8 @@ extern "C" int sgb_plan_report(const sgb_plan *p, int *info, int *siter, int *di
     return 0;
 }
 
-// Normwise backward error per system: one warp per system, lanes over rows.
+// Normwise backward error per system: one warp per system, lanes over rows;
+// the S x S block coefficients of the system in shared memory (3 S^2 <= 192).
 __global__ void k_backward_error(int nsys, ModelSource ms, const double2 *__restrict__ b,
                                  const double2 *__restrict__ x, double *__restrict__ out)
 {
@@ -854,11 +855,11 @@ __global__ void k_backward_error(int nsys, ModelSource ms, const double2 *__rest
     const int S = cs.S, n = cs.n, N = S * n;
     const double2 *xs = x + (long long) s * N, *bs = b + (long long) s * N;
     double anorm = 0, rmax = 0, xmax = 0, bmax = 0;
-    sgb_coef cf[3][64];
-    for (int e = 0; e < S; ++e)
-        for (int f = 0; f < S; ++f)
-            sgb_block_coefs(&cs, e, f, ms.phi, ms.kx[s], ms.kz[s], &cf[0][e * S + f],
-                            &cf[1][e * S + f], &cf[2][e * S + f]);
+    __shared__ sgb_coef cf[3][64];
+    for (int ef = threadIdx.x; ef < S * S; ef += 32)
+        sgb_block_coefs(&cs, ef / S, ef % S, ms.phi, ms.kx[s], ms.kz[s], &cf[0][ef], &cf[1][ef],
+                        &cf[2][ef]);
+    __syncwarp();
     for (int I = threadIdx.x; I < N; I += 32) {
         const int p = I / S, e = I % S;
         double2 ax = make_double2(0, 0);
@@ -1139,29 +1140,41 @@ extern "C" int sgb_batch_unserved(sgb_batch *b, int *count)
 // rows off .. off + KL + KU hold A(r, c), r = c + i - off - KU, the others
 // and every position outside the matrix are zero (what suzerain_bsmbsm_zpack
 // leaves around the band, suzerain/bsmbsm_pack.def:66-119).
+// Packed band of every system (ldab x N per system, band rows off ..
+// off + KL + KU).  Block (x, s): columns 4x .. 4x+3 of system s, threads
+// over (row, column); the system's S x S block coefficients are formed once
+// per block in shared memory.
 __global__ void k_assemble_packed(int nsys, ModelSource ms, int KL, int KU, double2 *__restrict__ ab,
                                   int ldab, long long ab_stride, int off)
 {
     const int s = blockIdx.y;
     const sgb_case &cs = ms.cs;
     const int S = cs.S, N = S * cs.n;
-    const long long t = (long long) blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= nsys || t >= (long long) ldab * N) return;
-    const int c = (int) (t / ldab), i = (int) (t - (long long) c * ldab);
-    const int r = c + i - off - KU;
-    double2 v = make_double2(0.0, 0.0);
-    if (i >= off && i <= off + KL + KU && r >= 0 && r < N) {
-        const int p = r / S, e = r - p * S, q = c / S, f = c - q * S;
-        if (sgb_is_dirichlet_row(&cs, r)) {
-            v.x = (r == c) ? 1.0 : 0.0;
-        } else if (p - q <= cs.kl && q - p <= cs.ku) {
-            sgb_coef cM, cD1, cD2;
-            sgb_block_coefs(&cs, e, f, ms.phi, ms.kx[s], ms.kz[s], &cM, &cD1, &cD2);
-            const int k = cs.ku + p - q + q * cs.ld;
-            sgb_block_entry(cM, cD1, cD2, cs.M[k], cs.D1[k], cs.D2[k], &v.x, &v.y);
+    if (s >= nsys) return;
+    __shared__ sgb_coef cf[3][64];
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    for (int ef = tid; ef < S * S; ef += blockDim.x * blockDim.y)
+        sgb_block_coefs(&cs, ef / S, ef % S, ms.phi, ms.kx[s], ms.kz[s], &cf[0][ef], &cf[1][ef],
+                        &cf[2][ef]);
+    __syncthreads();
+    const int c = blockIdx.x * blockDim.y + threadIdx.y;
+    if (c >= N) return;
+    const int q = c / S, f = c - q * S;
+    double2 *col = ab + s * ab_stride + (long long) c * ldab;
+    for (int i = threadIdx.x; i < ldab; i += blockDim.x) {
+        const int r = c + i - off - KU;
+        double2 v = make_double2(0.0, 0.0);
+        if (i >= off && i <= off + KL + KU && r >= 0 && r < N) {
+            const int p = r / S, e = r - p * S;
+            if (sgb_is_dirichlet_row(&cs, r)) {
+                v.x = (r == c) ? 1.0 : 0.0;
+            } else if (p - q <= cs.kl && q - p <= cs.ku) {
+                const int k = cs.ku + p - q + q * cs.ld, ef = e * S + f;
+                sgb_block_entry(cf[0][ef], cf[1][ef], cf[2][ef], cs.M[k], cs.D1[k], cs.D2[k], &v.x, &v.y);
+            }
         }
+        col[i] = v;
     }
-    ab[s * ab_stride + t] = v;
 }
 
 extern "C" int sgb_plan_assemble_packed(sgb_plan *p, double phi, void *ab, int ldab,
@@ -1171,11 +1184,11 @@ extern "C" int sgb_plan_assemble_packed(sgb_plan *p, double phi, void *ab, int l
     if (off < 0 || ldab < off + p->KL + p->KU + 1 || ab_stride < (long long) ldab * p->N)
         return fail("sgb_plan_assemble_packed: ldab must be >= off + KL + KU + 1 and "
                     "ab_stride >= ldab * N");
+    if (p->hc.S * p->hc.S > 64) return fail("sgb_plan_assemble_packed: S too large");
     std::lock_guard<std::mutex> lk(p->mu);
-    const long long per = (long long) ldab * p->N;
-    dim3 grd((unsigned) ((per + 255) / 256), (unsigned) p->nsys);
+    dim3 grd((unsigned) ((p->N + 3) / 4), (unsigned) p->nsys);
     count_launch(1);
-    k_assemble_packed<<<grd, 256, 0, (cudaStream_t) stream>>>(
+    k_assemble_packed<<<grd, dim3(64, 4), 0, (cudaStream_t) stream>>>(
         p->nsys, p->ms(phi), p->KL, p->KU, reinterpret_cast<double2 *>(ab), ldab, ab_stride, off);
     SGB_CUDA_TRY(cudaGetLastError());
     p->note((cudaStream_t) stream);

@@ -597,12 +597,18 @@ static cudaError_t launch_quad_d(const GbtrsArgs &a, cudaStream_t st)
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
+    // multi-row records where the shared memory holds them, else one row
+    // (the same results either way)
+    auto fits = [&](size_t se) {
+        return (size_t) QSYS * se * sizeof(T2) + (size_t) QSYS * PB * 8 <= 227 * 1024;
+    };
     switch (g_qbulk) {
-    case 2: return launch_quad_bwd<R, PB, 2>(a, yw, grid, st);
-    case 4: return launch_quad_bwd<R, PB, 4>(a, yw, grid, st);
-    case 8: return launch_quad_bwd<R, PB, 8>(a, yw, grid, st);
-    default: return launch_quad_bwd<R, PB, 1>(a, yw, grid, st);
+    case 2: if (fits(QuadBwdLayout<R, PB, 2>(a.g).SE)) return launch_quad_bwd<R, PB, 2>(a, yw, grid, st); break;
+    case 4: if (fits(QuadBwdLayout<R, PB, 4>(a.g).SE)) return launch_quad_bwd<R, PB, 4>(a, yw, grid, st); break;
+    case 8: if (fits(QuadBwdLayout<R, PB, 8>(a.g).SE)) return launch_quad_bwd<R, PB, 8>(a, yw, grid, st); break;
+    default: break;
     }
+    return launch_quad_bwd<R, PB, 1>(a, yw, grid, st);
 }
 
 template <typename R, int PF>
@@ -647,16 +653,10 @@ static size_t quad_bwd_se_rb(const FactorGeom &g)
     default: return QuadBwdLayout<R, 2, RB>(g).SE;
     }
 }
+// the one-row layout: the backward solve falls back to it when larger
+// records do not fit
 template <typename R>
-static size_t quad_bwd_se(const FactorGeom &g)
-{
-    switch (g_qbulk) {
-    case 2: return quad_bwd_se_rb<R, 2>(g);
-    case 4: return quad_bwd_se_rb<R, 4>(g);
-    case 8: return quad_bwd_se_rb<R, 8>(g);
-    default: return quad_bwd_se_rb<R, 1>(g);
-    }
-}
+static size_t quad_bwd_se(const FactorGeom &g) { return quad_bwd_se_rb<R, 1>(g); }
 
 // The quad path needs a writable y buffer (nsys x N, complex of prec) and,
 // when forward elimination is already done, y already in it.
