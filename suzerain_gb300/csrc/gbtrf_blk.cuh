@@ -860,11 +860,28 @@ k_gbtrf_la(FactorGeom g, int nsys, PackedSource src, ModelSource ms,
                                 for (int t = 0; t < MT; ++t) l[t] = win[roff[t] + cm];
 #pragma unroll
                                 for (int u = 0; u < TC; ++u) uu[u] = win[rm + coff[u]];
+                                if constexpr (sizeof(R) == 4) {
+                                    // complex64: two packed FMAs per complex multiply-add
+                                    float2 la[MT], lb[MT], us[TC];
 #pragma unroll
-                                for (int t = 0; t < MT; ++t)
+                                    for (int t = 0; t < MT; ++t) {
+                                        la[t] = make_float2(-l[t].x, -l[t].x);
+                                        lb[t] = make_float2(l[t].y, -l[t].y);
+                                    }
 #pragma unroll
-                                    for (int u = 0; u < TC; ++u)
-                                        acc[t][u] = cfnma(l[t], uu[u], acc[t][u]);
+                                    for (int u = 0; u < TC; ++u) us[u] = make_float2(uu[u].y, uu[u].x);
+#pragma unroll
+                                    for (int t = 0; t < MT; ++t)
+#pragma unroll
+                                        for (int u = 0; u < TC; ++u)
+                                            acc[t][u] = cfnma2(la[t], lb[t], uu[u], us[u], acc[t][u]);
+                                } else {
+#pragma unroll
+                                    for (int t = 0; t < MT; ++t)
+#pragma unroll
+                                        for (int u = 0; u < TC; ++u)
+                                            acc[t][u] = cfnma(l[t], uu[u], acc[t][u]);
+                                }
                             }
                         }
 #pragma unroll
@@ -899,29 +916,41 @@ k_gbtrf_la(FactorGeom g, int nsys, PackedSource src, ModelSource ms,
         tick(1);
 
         // ---------------- B. interchanges and U12 of panel J ---------------
+        // Trailing columns exist only when column j0 + nbk does, so then the
+        // panel is full (nbk == NB).  The interchange offsets, row offsets
+        // and L11 are read once into registers; per column the interchanges
+        // are applied in order and U12 solved in registers (the order of
+        // multiply-adds of a column-by-column sweep).
         const int ju = shv[0];
         const int ce = ju - (j0 - NB);       // last trailing column, logical (< WC)
-        for (int c = NB + nbk + tid; c <= ce; c += NT) {
-            const int cc = csl(c);
-            for (int k = 0; k < nbk; ++k) {
-                const int bt = pvoff[k];
-                if (bt) {
-                    T2 &a = win[rsl(NB + k) * P + cc], &b = win[rsl(NB + k + bt) * P + cc];
-                    const T2 t = a; a = b; b = t;
-                }
-            }
-            T2 u[NB];
+        if (ce >= NB + nbk) {
+            int bts[NB], ro[NB];
+            T2 l11[NB][NB];
 #pragma unroll
             for (int k = 0; k < NB; ++k) {
-                if (k < nbk) {
-                    const int ro = rsl(NB + k) * P;
-                    T2 v = win[ro + cc];
+                bts[k] = pvoff[k];
+                ro[k] = rsl(NB + k) * P;
 #pragma unroll
-                    for (int m = 0; m < NB; ++m)
-                        if (m < k) v = cfnma(win[ro + csl(NB + m)], u[m], v);
-                    u[k] = v;
-                    win[ro + cc] = v;
+                for (int m = 0; m < NB; ++m) l11[k][m] = m < k ? win[ro[k] + csl(NB + m)] : zero;
+            }
+            for (int c = NB + nbk + tid; c <= ce; c += NT) {
+                const int cc = csl(c);
+#pragma unroll
+                for (int k = 0; k < NB; ++k) {
+                    if (bts[k]) {
+                        T2 &a = win[ro[k] + cc], &b = win[rsl(NB + k + bts[k]) * P + cc];
+                        const T2 t = a; a = b; b = t;
+                    }
                 }
+                T2 u[NB];
+#pragma unroll
+                for (int k = 0; k < NB; ++k) u[k] = win[ro[k] + cc];
+#pragma unroll
+                for (int k = 1; k < NB; ++k)
+#pragma unroll
+                    for (int m = 0; m < k; ++m) u[k] = cfnma(l11[k][m], u[m], u[k]);
+#pragma unroll
+                for (int k = 0; k < NB; ++k) win[ro[k] + cc] = u[k];
             }
         }
         __syncthreads();
