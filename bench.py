@@ -581,17 +581,19 @@ def run_ours(args):
     return 0
 
 
-def batching_run(cases: int, steps: int, warmup: int, tune_nsys: int, local: int) -> dict:
+def batching_run(cases: int, steps: int, warmup: int, tune_nsys: int, local: int,
+                 ragged: bool = True) -> dict:
     """Configuration 3's step over `cases` cases: every case resident (one
     plan each), factor shapes tuned per geometry when tune_nsys > 0, one step
     = the three SMR91 substeps of every case recorded into one CUDA graph
-    over 8 streams and replayed.  value = system solves per second (each
-    system solved once per substep)."""
+    over 8 streams and replayed.  ragged: one persistent complex64 factor
+    launch per substep over every case instead of one per case.  value =
+    system solves per second (each system solved once per substep)."""
     import torch
     from suzerain_gb300 import multicase, plan as P, synth
     cfgs = synth.config3_cases(cases)
     t0 = time.perf_counter()
-    mc = multicase.MultiCase(cfgs, nstreams=8, max_double_slots=128)
+    mc = multicase.MultiCase(cfgs, nstreams=8, max_double_slots=128, ragged=ragged)
     tuned = mc.tune("C", nsys=tune_nsys, reps=1) if tune_nsys > 0 else {}
     spec = P.RefineSpec(**SPEC)
     mc.capture("M", spec)
@@ -618,13 +620,15 @@ def batching_run(cases: int, steps: int, warmup: int, tune_nsys: int, local: int
         "ms_per_step": ms / steps,
         "workload": f"config 3: {len(cfgs)} cases, S in {{5,7}}, k in {{6,8}}, Ny in 32..256, "
                     f"{nsys} systems, {len(mc.geometries())} geometries; step = 3 SMR91 "
-                    f"substeps of every case, one CUDA graph over 8 streams",
+                    f"substeps of every case, one CUDA graph over 8 streams"
+                    + (", ragged factor" if ragged else ""),
         "cases": len(cfgs), "systems": nsys, "geometries": len(mc.geometries()),
         "rel_resid_max": float(berr.max()), "unserved": mc.unserved(),
         "gpu_launches": int(mc.graph_kernels) * steps,
         "tuned_shapes": {f"{k[0]} N={k[1]} KL={k[2]}": list(v) for k, v in tuned.items()},
         "setup_s": setup_s, "clocks": clocks, "device_bytes": mc.device_bytes(),
     }
+    mc.close()
     del mc
     torch.cuda.empty_cache()
     return out
@@ -678,7 +682,8 @@ def run_config3(args) -> int:
     L = nat.load()
     if L.sgb_device_ok() != 0:
         raise RuntimeError(nat.last_error())
-    r = batching_run(args.cases, args.steps, args.warmup, 512, local)
+    r = batching_run(args.cases, args.steps, args.warmup, 512, local,
+                     ragged=not args.per_case_factor)
     line = {
         "metric": "system solves/s at rel-resid <=1e-12 (mixed c64 LU + FP64 refinement)",
         "value": r["value"], "unit": "systems/s", "n_gpus": 1, "steps": args.steps,
@@ -875,6 +880,9 @@ def main():
     ap.add_argument("--packed-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cases", type=int, default=64, help="configuration 3: number of cases")
+    ap.add_argument("--per-case-factor", action="store_true",
+                    help="configuration 3: one complex64 factor launch per case instead of "
+                         "the ragged launch over all cases")
     ap.add_argument("--requests", type=int, default=40,
                     help="configuration 4: requests per load level (mixed)")
     ap.add_argument("--levels", default="0.1,0.3,0.5,0.7,0.9",

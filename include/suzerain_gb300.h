@@ -832,6 +832,30 @@ int sgb_plan_unserved(sgb_plan *plan, int *count);
  *  would, so that every substep can then take the capturable form. */
 int sgb_plan_prepare(sgb_plan *plan, char method);
 
+/** The capturable mixed substep (method 'M', siter >= 0) in two stages
+ *  around an external complex64 factor: stage 1 runs the explicit operator
+ *  and the refinement's initial state, stage 2 everything after the factor.
+ *  Stage 1 of every plan of a ragged batch, sgb_ragged_factor, then stage 2
+ *  of every plan give sgb_plan_substep_capturable's results bit for bit.
+ *  Replaces, for a batch of wavenumber sets, the per-set factor loop of the
+ *  reference's implicit solve (suzerain/bsmbsm_solver.cpp:443 and
+ *  suzerain/bsmbsm_solver.cpp:1009, zgbtrf of each set's packed band). */
+int sgb_plan_substep_stage(sgb_plan *plan, int stage, char method, double phi_exp,
+                           double phi_imp, const void *u_in, void *u_out,
+                           const sgb_refine_spec *spec, void *stream);
+
+/** A ragged batch: the complex64 factors of several plans' mixed substeps
+ *  (each plan at its own phi_imp, up to KL = 56, S <= 8) as one launch per
+ *  row-tile class (KL <= 40, KL <= 56), the systems of the largest plans
+ *  first.  Every plan needs its mixed workspace (one
+ *  sgb_plan_substep with 'M', or sgb_plan_prepare) before creation; the
+ *  batch reads the plans' workspaces, so the plans outlive it. */
+typedef struct sgb_ragged sgb_ragged;
+sgb_ragged *sgb_ragged_create(sgb_plan *const *plans, int nplans, const double *phi_imp,
+                              const sgb_refine_spec *spec);
+int sgb_ragged_factor(sgb_ragged *batch, void *stream);
+void sgb_ragged_destroy(sgb_ragged *batch);
+
 /** Same, from and to host memory (copies inside the call). */
 int sgb_plan_substep_host(sgb_plan *p, char method, double phi_exp,
                           double phi_imp, const void *u_in_host,

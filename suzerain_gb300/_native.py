@@ -215,6 +215,11 @@ _SIGS = {
                                          C.POINTER(RefineSpec), _p]),
     "sgb_plan_unserved": (_i, [_p, _p]),
     "sgb_plan_prepare": (_i, [_p, C.c_char]),
+    "sgb_plan_substep_stage": (_i, [_p, _i, C.c_char, _d, _d, _p, _p,
+                                    C.POINTER(RefineSpec), _p]),
+    "sgb_ragged_create": (_p, [_p, _i, _p, C.POINTER(RefineSpec)]),
+    "sgb_ragged_factor": (_i, [_p, _p]),
+    "sgb_ragged_destroy": (None, [_p]),
     "sgb_solver_spec_default": (None, [_p]),
     "sgb_solver_spec_parse": (_i, [C.c_char_p, _p, _p, C.c_size_t]),
     "sgb_solver_spec_format": (_i, [_p, _p, C.c_size_t]),

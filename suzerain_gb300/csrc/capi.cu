@@ -634,18 +634,27 @@ static int plan_alloc_m(sgb_plan *p)
     return 0;
 }
 
+// The refinement problem of the mixed method's capturable or host-driven
+// substep of plan p at phi_imp.
+static RefineProblem plan_refine_problem(sgb_plan *p, double phi_imp, const sgb_refine_spec *spec,
+                                         bool capturable);
+
 // capturable: no host synchronization, no allocation, no host-to-device copy
 // (the refinement runs its device-counted form), so the call can be
 // recorded into a CUDA graph after one ordinary call of the same method.
+// stage 1 / 2: the two halves of the capturable mixed substep around an
+// external complex64 factor (sgb_plan_substep_stage).
+
 static int plan_substep(sgb_plan *p, char method, double phi_exp, double phi_imp,
                         const void *u_in, void *u_out, const sgb_refine_spec *spec,
-                        cudaStream_t st, bool capturable = false)
+                        cudaStream_t st, bool capturable = false, int stage = 0)
 {
     const int nsys = p->nsys, N = p->N, S = p->hc.S, n = p->hc.n;
     const long long tot = (long long) nsys * N;
     const unsigned EB = (unsigned) ((tot + 255) / 256);
     PhaseTimer nop;
     PhaseTimer &tm = capturable ? nop : p->timer;
+    if (stage == 2) goto refine;      // stage 1 ran the explicit operator and the init
     // 1. explicit operator (or plain permutation) into b
     tm.begin(phi_exp != 0.0 ? "explicit_apply_f64" : "permute_in", st);
     count_launch(1);
@@ -660,6 +669,8 @@ static int plan_substep(sgb_plan *p, char method, double phi_exp, double phi_imp
         SGB_CUDA_TRY(cudaGetLastError());
     }
     tm.end(st);
+refine:
+    {
     FactorGeom g{N, p->KL, p->KU};
     p->phi_imp_last = phi_imp;
     if (method == 'Z') {
@@ -687,19 +698,8 @@ static int plan_substep(sgb_plan *p, char method, double phi_exp, double phi_imp
         SGB_CUDA_TRY(launch_gbtrs(sa, st));
         tm.end(st);
     } else if (method == 'M') {
-        RefineProblem P;
-        P.nsys = nsys; P.g = g; P.trans = 'N'; P.resid_trans = 'N'; P.model = true;
-        P.ms = p->ms(phi_imp); P.gram = p->gram; P.b = p->b; P.b_stride = N;
-        P.x = p->x; P.x_stride = N;
-        P.aiter = spec ? spec->aiter : 5; P.siter = spec ? spec->siter : 25;
-        P.diter = spec ? spec->diter : 5; P.tolsc = spec ? spec->tolsc : 1.0;
-        P.nslot64 = p->nslot64; P.host_count = p->hcount;
-        P.timer = capturable ? nullptr : &p->timer;
-        if (capturable) {
-            P.graph = true;
-            P.graph_siter = P.siter < 0 ? 0 : P.siter + 1;
-            P.graph_diter = P.diter + 2;
-        }
+        RefineProblem P = plan_refine_problem(p, phi_imp, spec, capturable);
+        P.stage = stage;
         const size_t need = refine_workspace_bytes(P);
         if (need > p->rws_bytes && capturable)
             return fail("sgb_plan_substep_capturable: run sgb_plan_substep or sgb_plan_prepare "
@@ -710,8 +710,10 @@ static int plan_substep(sgb_plan *p, char method, double phi_exp, double phi_imp
         }
         int rc = refine_batched(P, p->rws, p->rws_bytes, p->last, st);
         if (rc) return sgb_set_error((cudaError_t) rc, "refine_batched", __FILE__, __LINE__);
+        if (stage == 1) return 0;
     } else {
         return fail("sgb_plan_substep: method must be 'Z' or 'M'");
+    }
     }
     p->last_method = method;
     tm.begin("permute_out", st);
@@ -770,6 +772,152 @@ extern "C" int sgb_plan_substep_capturable(sgb_plan *p, char method, double phi_
                                 (cudaStream_t) stream, true);
     p->note((cudaStream_t) stream);
     return rc;
+}
+
+static RefineProblem plan_refine_problem(sgb_plan *p, double phi_imp, const sgb_refine_spec *spec,
+                                         bool capturable)
+{
+    RefineProblem P;
+    const int N = p->N;
+    P.nsys = p->nsys; P.g = FactorGeom{N, p->KL, p->KU}; P.trans = 'N'; P.resid_trans = 'N';
+    P.model = true;
+    P.ms = p->ms(phi_imp); P.gram = p->gram; P.b = p->b; P.b_stride = N;
+    P.x = p->x; P.x_stride = N;
+    P.aiter = spec ? spec->aiter : 5; P.siter = spec ? spec->siter : 25;
+    P.diter = spec ? spec->diter : 5; P.tolsc = spec ? spec->tolsc : 1.0;
+    P.nslot64 = p->nslot64; P.host_count = p->hcount;
+    P.timer = capturable ? nullptr : &p->timer;
+    if (capturable) {
+        P.graph = true;
+        P.graph_siter = P.siter < 0 ? 0 : P.siter + 1;
+        P.graph_diter = P.diter + 2;
+    }
+    return P;
+}
+
+// The capturable mixed substep in two stages around an external complex64
+// factor (a ragged batch over many plans): stage 1 runs the explicit operator
+// and the refinement's initial state, stage 2 everything from the factor's
+// results on.  Stage 1, the ragged factor, then stage 2 give the results of
+// sgb_plan_substep_capturable bit for bit.
+extern "C" int sgb_plan_substep_stage(sgb_plan *p, int stage, char method, double phi_exp,
+                                      double phi_imp, const void *u_in, void *u_out,
+                                      const sgb_refine_spec *spec, void *stream)
+{
+    if (!p || !u_in || !u_out) return fail("sgb_plan_substep_stage: null argument");
+    if (stage != 1 && stage != 2) return fail("sgb_plan_substep_stage: stage must be 1 or 2");
+    if (toupper(method) != 'M') return fail("sgb_plan_substep_stage: method must be 'M'");
+    if (spec && spec->siter < 0) return fail("sgb_plan_substep_stage: needs siter >= 0");
+    std::lock_guard<std::mutex> lk(p->mu);
+    const int rc = plan_substep(p, 'M', phi_exp, phi_imp, u_in, u_out, spec, (cudaStream_t) stream,
+                                true, stage);
+    p->note((cudaStream_t) stream);
+    return rc;
+}
+
+// A ragged batch: the complex64 factors of many plans' substeps (each at its
+// own phi_imp) as one launch per row-tile class (KL <= 40 and KL <= 56), one
+// CTA per system position, the largest plans' systems first.
+struct sgb_ragged {
+    struct Class {
+        RaggedDesc *descs = nullptr;
+        int2 *items = nullptr;
+        int nitems = 0, maxtr = 5;
+        size_t smem = 0;
+    } cls[2];
+    std::vector<sgb_plan *> plans;
+    std::vector<void *> rws;      // each plan's workspace when the batch was made
+};
+
+extern "C" void sgb_ragged_destroy(sgb_ragged *r);
+
+extern "C" sgb_ragged *sgb_ragged_create(sgb_plan *const *plans, int nplans, const double *phi_imp,
+                                         const sgb_refine_spec *spec)
+{
+    if (!plans || nplans <= 0 || !phi_imp) { fail("sgb_ragged_create: bad arguments"); return nullptr; }
+    if (spec && spec->siter < 0) { fail("sgb_ragged_create: needs siter >= 0"); return nullptr; }
+    auto *r = new (std::nothrow) sgb_ragged;
+    if (!r) { fail("sgb_ragged_create: out of memory"); return nullptr; }
+    std::vector<RaggedDesc> hd[2];
+    std::vector<std::pair<long long, int>> order[2];   // (cost, plan) per class
+    std::vector<int> where(nplans);
+    for (int i = 0; i < nplans; ++i) {
+        sgb_plan *p = plans[i];
+        if (!p || p->KL > 56 || p->hc.S > 8) {
+            sgb_ragged_destroy(r);
+            fail("sgb_ragged_create: a plan is null or has KL > 56 or S > 8");
+            return nullptr;
+        }
+        std::lock_guard<std::mutex> lk(p->mu);
+        RefineProblem P = plan_refine_problem(p, phi_imp[i], spec, true);
+        if (refine_workspace_bytes(P) > p->rws_bytes) {
+            sgb_ragged_destroy(r);
+            fail("sgb_ragged_create: run a mixed substep (or sgb_plan_prepare 'M') of every plan first");
+            return nullptr;
+        }
+        RaggedDesc d;
+        refine_ragged_desc(P, p->rws, d);
+        const int c = p->KL <= 40 ? 0 : 1;
+        where[i] = (int) hd[c].size();
+        hd[c].push_back(d);
+        order[c].push_back({(long long) p->N * p->KL * (p->KL + p->KU), i});
+        const size_t sm = gbtrf_blk_smem_bytes(sizeof(float), d.g, p->hc.S, 4, 2);
+        r->cls[c].smem = std::max(r->cls[c].smem, sm);
+        r->plans.push_back(p);
+        r->rws.push_back(p->rws);
+    }
+    cudaError_t e = cudaSuccess;
+    for (int c = 0; c < 2; ++c) {
+        sgb_ragged::Class &k = r->cls[c];
+        k.maxtr = c == 0 ? 5 : 7;
+        if (hd[c].empty()) continue;
+        std::sort(order[c].begin(), order[c].end(),
+                  [](const std::pair<long long, int> &a, const std::pair<long long, int> &b) {
+                      return a.first > b.first;
+                  });
+        std::vector<int2> it;
+        for (auto &o : order[c])
+            for (int k2 = 0; k2 < plans[o.second]->nsys; ++k2) it.push_back(make_int2(where[o.second], k2));
+        k.nitems = (int) it.size();
+        if ((e = cudaMalloc(&k.descs, hd[c].size() * sizeof(RaggedDesc))) != cudaSuccess) break;
+        if ((e = cudaMemcpy(k.descs, hd[c].data(), hd[c].size() * sizeof(RaggedDesc),
+                            cudaMemcpyHostToDevice)) != cudaSuccess) break;
+        if ((e = cudaMalloc(&k.items, it.size() * sizeof(int2))) != cudaSuccess) break;
+        if ((e = cudaMemcpy(k.items, it.data(), it.size() * sizeof(int2), cudaMemcpyHostToDevice)) != cudaSuccess)
+            break;
+    }
+    if (e != cudaSuccess) {
+        sgb_ragged_destroy(r);
+        sgb_set_error(e, "sgb_ragged_create", __FILE__, __LINE__);
+        return nullptr;
+    }
+    return r;
+}
+
+extern "C" void sgb_ragged_destroy(sgb_ragged *r)
+{
+    if (!r) return;
+    for (auto &k : r->cls) { cudaFree(k.descs); cudaFree(k.items); }
+    delete r;
+}
+
+// The ragged factor launch(es), after every plan's stage 1 and before its
+// stage 2 (on the stream given, capturable).
+extern "C" int sgb_ragged_factor(sgb_ragged *r, void *stream)
+{
+    if (!r) return fail("sgb_ragged_factor: null batch");
+    cudaStream_t st = (cudaStream_t) stream;
+    for (size_t i = 0; i < r->plans.size(); ++i)
+        if (r->plans[i]->rws != r->rws[i])
+            return fail("sgb_ragged_factor: a plan's workspace moved since the batch was made");
+    for (int c = 0; c < 2; ++c) {
+        const auto &k = r->cls[c];
+        if (k.nitems == 0) continue;
+        count_launch(1);
+        SGB_CUDA_TRY(launch_gbtrf_ragged(k.descs, k.items, k.nitems, k.maxtr, k.smem, st));
+    }
+    for (sgb_plan *p : r->plans) p->note(st);
+    return 0;
 }
 
 extern "C" int sgb_plan_prepare(sgb_plan *p, char method)

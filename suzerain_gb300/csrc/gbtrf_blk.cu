@@ -4,6 +4,7 @@
 // compiled once per (precision, NB, warp family), instantiates it.
 #include "gbtrf_blk.cuh"
 
+#include <algorithm>
 #include <mutex>
 #include <map>
 #include <tuple>
@@ -80,6 +81,18 @@ cudaError_t launch_nb(const GbtrfArgs &a, int nw, cudaStream_t st)
     return launch_blk_fam<R, NB, 4>(a, nw, st);
 }
 }  // namespace
+
+cudaError_t launch_gbtrf_ragged(const RaggedDesc *descs, const int2 *items, int nitems, int maxtr,
+                                size_t smem, cudaStream_t st)
+{
+    if (nitems <= 0) return cudaSuccess;
+    if (maxtr != 5 && maxtr != 7) return cudaErrorInvalidValue;
+    auto kern = maxtr == 5 ? k_gbtrf_ragged<5> : k_gbtrf_ragged<7>;
+    cudaError_t e = smem_attr((const void *) kern, smem);
+    if (e != cudaSuccess) return e;
+    kern<<<nitems, 64, smem, st>>>(descs, items);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_gbtrf_blk(const GbtrfArgs &a, int nb, int nw, cudaStream_t st)
 {

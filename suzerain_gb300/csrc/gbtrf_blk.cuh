@@ -417,15 +417,16 @@ __device__ __forceinline__ void assemble_rows(const PackedSource &src, const Mod
 template <typename R, int NW>
 constexpr int blk_min_blocks() { return sizeof(R) == 8 ? (NW == 4 ? 3 : 4) : (NW == 4 ? 4 : 8); }
 
-template <typename R, int NB, int NW, int MAXTR, bool MODEL, bool FWD>
-__global__ void __launch_bounds__(32 * NW, (blk_min_blocks<R, NW>()))
-k_gbtrf_cta(FactorGeom g, int nsys, PackedSource src, ModelSource ms,
-            cplx_t<R> *__restrict__ fac, long long fac_stride,
-            int *__restrict__ ipiv, int *__restrict__ info,
-            const double2 *__restrict__ rhs, long long rhs_stride,
-            cplx_t<R> *__restrict__ y, long long y_stride,
-            const int *__restrict__ sys_list, const int *__restrict__ d_count,
-            bool slot_mode, unsigned long long *__restrict__ prof)
+// The factor of one system s (factor, pivots and info at index fi) by the
+// CTA: the body of the phased kernel below and of the ragged kernel.
+template <typename R, int NB, int NW, int MAXTR, bool MODEL, bool FWD, typename MST = ModelSource>
+__device__ __forceinline__ void
+gbtrf_cta_system(const FactorGeom g, int s, long long fi, const PackedSource src,
+                 MST ms, cplx_t<R> *__restrict__ fac, long long fac_stride,
+                 int *__restrict__ ipiv, int *__restrict__ info,
+                 const double2 *__restrict__ rhs, long long rhs_stride,
+                 cplx_t<R> *__restrict__ y, long long y_stride,
+                 unsigned long long *__restrict__ prof)
 {
     using T2 = cplx_t<R>;
     constexpr int NT = 32 * NW;
@@ -436,10 +437,6 @@ k_gbtrf_cta(FactorGeom g, int nsys, PackedSource src, ModelSource ms,
     constexpr int RS = RGN * MAXTR > 48 ? 3 : 2;      // panel rows per lane: WR <= 32 RS
     static_assert((1 << LNB) == NB, "NB must be 4, 8 or 16");
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    if (d_count && (int) blockIdx.x >= *d_count) return;
-    const int s = sys_list ? sys_list[blockIdx.x] : (int) blockIdx.x;
-    if (s < 0 || s >= nsys) return;
-    const long long fi = slot_mode ? (long long) blockIdx.x : (long long) s;
 
     const int N = g.N, KL = g.KL, KU = g.KU, UW = g.UW();
     const int WR = KL + NB, WC = KL + KU + NB, P = blk_pitch(WC);
@@ -705,6 +702,46 @@ k_gbtrf_cta(FactorGeom g, int nsys, PackedSource src, ModelSource ms,
     if (tid == 0) info[fi] = shv[1];
     if (timing)
         for (int ph = 0; ph < 9; ++ph) atomicAdd(prof + ph, clk[ph]);
+}
+
+template <typename R, int NB, int NW, int MAXTR, bool MODEL, bool FWD>
+__global__ void __launch_bounds__(32 * NW, (blk_min_blocks<R, NW>()))
+k_gbtrf_cta(FactorGeom g, int nsys, PackedSource src, ModelSource ms,
+            cplx_t<R> *__restrict__ fac, long long fac_stride,
+            int *__restrict__ ipiv, int *__restrict__ info,
+            const double2 *__restrict__ rhs, long long rhs_stride,
+            cplx_t<R> *__restrict__ y, long long y_stride,
+            const int *__restrict__ sys_list, const int *__restrict__ d_count,
+            bool slot_mode, unsigned long long *__restrict__ prof)
+{
+    if (d_count && (int) blockIdx.x >= *d_count) return;
+    const int s = sys_list ? sys_list[blockIdx.x] : (int) blockIdx.x;
+    if (s < 0 || s >= nsys) return;
+    const long long fi = slot_mode ? (long long) blockIdx.x : (long long) s;
+    gbtrf_cta_system<R, NB, NW, MAXTR, MODEL, FWD>(g, s, fi, src, ms, fac, fac_stride, ipiv, info, rhs,
+                                                   rhs_stride, y, y_stride, prof);
+}
+
+// Ragged factor: one CTA per work item (plan d, list position k), the
+// items in the order given (the largest plans' systems first, which the
+// block scheduler dispatches first); each item is one system of one plan,
+// of that plan's own geometry (KL <= 8 MAXTR), or nothing when k is beyond
+// the plan's active count.  The plan's descriptor is read once into shared
+// memory (fewer registers than a copy in registers; no spills at MAXTR 5).
+// The shared memory is sized for the largest window of the batch.
+template <int MAXTR>
+__global__ void __launch_bounds__(64, (blk_min_blocks<float, 2>()))
+k_gbtrf_ragged(const RaggedDesc *__restrict__ descs, const int2 *__restrict__ items)
+{
+    __shared__ RaggedDesc sd;
+    const int2 w = items[blockIdx.x];
+    if (threadIdx.x == 0) sd = descs[w.x];
+    __syncthreads();
+    if (w.y >= *sd.d_count) return;
+    const int s = sd.sys_list[w.y];
+    gbtrf_cta_system<float, 4, 2, MAXTR, true, true, const ModelSource &>(
+        sd.g, s, s, PackedSource{}, sd.ms, sd.fac, sd.fac_stride, sd.ipiv, sd.info, sd.rhs,
+        sd.rhs_stride, sd.y, sd.y_stride, nullptr);
 }
 
 // Lookahead form (NW >= 2): warp 0 factors panel J while warps 1..NW-1 apply

@@ -323,6 +323,20 @@ size_t refine_workspace_bytes(const RefineProblem &P)
     return carve_layout(P, nullptr, Lo);
 }
 
+// The complex64 factor of a model problem (trans 'N') as one plan of a
+// ragged batch: its outputs and active list in the refinement workspace.
+int refine_ragged_desc(const RefineProblem &P, void *workspace, RaggedDesc &d)
+{
+    if (!P.model || P.trans != 'N' || P.siter < 0) return (int) cudaErrorInvalidValue;
+    RefineLayout Lo;
+    carve_layout(P, reinterpret_cast<char *>(workspace), Lo);
+    d.g = P.g; d.ms = P.ms;
+    d.fac = Lo.fac32; d.fac_stride = P.g.fac_elems(); d.ipiv = Lo.ipiv32; d.info = Lo.info32;
+    d.rhs = P.b; d.rhs_stride = P.b_stride; d.y = Lo.y32; d.y_stride = P.g.N;
+    d.sys_list = Lo.listS; d.d_count = Lo.cnt + 0;
+    return 0;
+}
+
 __global__ void k_fill(int n, double *__restrict__ p, double v)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -364,6 +378,7 @@ int refine_batched(const RefineProblem &P, void *workspace, size_t workspace_byt
     const unsigned EB = (unsigned) ((tot + 255) / 256);
     cudaError_t e;
 #define TRY(x) do { e = (x); if (e != cudaSuccess) return (int) e; } while (0)
+    if (P.stage != 2) {
     TRY(cudaMemsetAsync(cnt, 0, 16 * sizeof(int), st));
 
     // r = b, x = 0, ||b||, ||A||_F
@@ -381,6 +396,8 @@ int refine_batched(const RefineProblem &P, void *workspace, size_t workspace_byt
                                    listS, cnt + 0, listD, cnt + 2);
     TRY(cudaGetLastError());
     tm.end(st);
+    }
+    if (P.stage == 1) return 0;   // the caller factors (ragged factor), then stage 2
 
     ResidualArgs ra;
     ra.trans = P.resid_trans; ra.nsys = nsys; ra.N = N; ra.KL = P.g.KL; ra.KU = P.g.KU;
@@ -397,10 +414,13 @@ int refine_batched(const RefineProblem &P, void *workspace, size_t workspace_byt
         fa.ms = P.ms; fa.fac = fac32; fa.fac_stride = P.g.fac_elems(); fa.ipiv = ipiv32;
         fa.info = info32; fa.sys_list = listS; fa.nlist = nsys; fa.d_count = cnt + 0;
         if (fuse) { fa.rhs = P.b; fa.rhs_stride = P.b_stride; fa.y = y32; fa.y_stride = N; }
-        tm.begin("factor_c64", st);
-        count_launch(2);
-        TRY(launch_gbtrf(fa, st));
-        tm.end(st);
+        if (P.stage != 2) {
+            tm.begin("factor_c64", st);
+            count_launch(1);
+            TRY(launch_gbtrf(fa, st));
+            tm.end(st);
+        }
+        count_launch(1);
         k_refine_after_sfactor<<<B, T, 0, st>>>(rs, info32, listS, cnt + 0, P.diter, listD, cnt + 2);
         GbtrsArgs sa;
         sa.prec = 'C'; sa.trans = P.trans; sa.g = P.g; sa.nsys = nsys; sa.fac = fac32;

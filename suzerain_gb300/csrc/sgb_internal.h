@@ -34,6 +34,28 @@ struct GbtrfArgs {
     int nw = 0;                      // warps per system of the blocked kernel (1, 2, 4; 0 = default)
     unsigned long long *prof = nullptr;  // optional per-phase cycle counters (6)
 };
+// One system of a ragged batch: the factor inputs and outputs of the plan
+// it belongs to (complex64, assembled from the plan's model operator, the
+// forward elimination of its right-hand side fused).
+struct RaggedDesc {
+    FactorGeom g;
+    ModelSource ms;
+    float2 *fac;
+    long long fac_stride;
+    int *ipiv, *info;
+    const double2 *rhs;
+    long long rhs_stride;
+    float2 *y;
+    long long y_stride;
+    const int *sys_list;       // the plan's active list and its device count
+    const int *d_count;
+};
+// The ragged factor over descriptors and (descriptor, list position) items
+// in device memory, one CTA per item; maxtr 5 for KL <= 40, 7 for KL <= 56;
+// smem the largest window's bytes.
+cudaError_t launch_gbtrf_ragged(const RaggedDesc *descs, const int2 *items, int nitems, int maxtr,
+                                size_t smem, cudaStream_t st);
+
 cudaError_t launch_gbtrf(const GbtrfArgs &a, cudaStream_t st);
 cudaError_t launch_gbtrf_blk(const GbtrfArgs &a, int nb, int nw, cudaStream_t st);
 bool gbtrf_blk_supported(const FactorGeom &g, int nb, int nw);

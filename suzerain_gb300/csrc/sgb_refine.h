@@ -42,6 +42,10 @@ struct RefineProblem {
     // complex128".
     bool graph = false;
     int graph_siter = 0, graph_diter = 0;
+    // 0: the whole solve; 1: up to the complex64 factor (initial state,
+    // norms, active list); 2: from the factor's results on (the caller ran
+    // the factor, e.g. as part of a ragged batch)
+    int stage = 0;
 };
 
 struct RefineOutputs {
@@ -63,5 +67,9 @@ int zcgbsvx_batched_check(const char *who, int nsys, int N, int KL, int KU, char
                           const sgb_refine_spec *spec);
 int refine_batched(const RefineProblem &P, void *workspace, size_t workspace_bytes,
                    RefineOutputs &out, cudaStream_t st);
+struct RaggedDesc;
+// Fills d with the complex64 factor's inputs and outputs of problem P in its
+// workspace (model operator, trans 'N', siter >= 0 only).
+int refine_ragged_desc(const RefineProblem &P, void *workspace, RaggedDesc &d);
 
 }  // namespace sgb

@@ -140,6 +140,17 @@ class Plan:
                                                 C.byref(sp), _ptr(stream))
         nat.check(rc, "sgb_plan_substep_capturable")
 
+    def substep_stage(self, stage: int, phi_exp: float, phi_imp: float, u_in, u_out,
+                      spec: RefineSpec | None = None, stream=0) -> None:
+        """One of the two stages of the capturable mixed substep around an
+        external complex64 factor (a RaggedFactor over several plans):
+        stage 1 the explicit operator and the refinement's initial state,
+        stage 2 everything after the factor."""
+        sp = (spec or RefineSpec()).ctypes()
+        rc = self.L.sgb_plan_substep_stage(self.handle, int(stage), b"M", phi_exp, phi_imp,
+                                           _ptr(u_in), _ptr(u_out), C.byref(sp), _ptr(stream))
+        nat.check(rc, "sgb_plan_substep_stage")
+
     def prepare(self, method: str = "M") -> None:
         """Allocate what the first substep of `method` would (then every
         substep may take the capturable form)."""
@@ -205,6 +216,36 @@ class Plan:
                                                  _ptr(stream)),
                   "sgb_plan_backward_error")
         return out
+
+
+class RaggedFactor:
+    """The complex64 factors of several plans' mixed substeps, each plan at
+    its own implicit coefficient, as one launch per row-tile class (the
+    systems of the largest plans first).  Between stage 1 and
+    stage 2 of every plan's substep_stage; the plans must outlive it and
+    hold their mixed workspace (a substep with 'M', or prepare('M'))."""
+
+    def __init__(self, plans: list, phi_imp: list, spec: RefineSpec | None = None):
+        self.L = nat.load()
+        self.plans = list(plans)
+        n = len(self.plans)
+        arr = (C.c_void_p * n)(*[p.handle for p in self.plans])
+        phis = (C.c_double * n)(*[float(v) for v in phi_imp])
+        sp = (spec or RefineSpec()).ctypes()
+        h = self.L.sgb_ragged_create(arr, n, phis, C.byref(sp))
+        if not h:
+            raise RuntimeError(f"sgb_ragged_create failed: {nat.last_error()}")
+        self.handle = h
+
+    def factor(self, stream=0) -> None:
+        nat.check(self.L.sgb_ragged_factor(self.handle, _ptr(stream)), "sgb_ragged_factor")
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.L.sgb_ragged_destroy(self.handle)
+            self.handle = None
+
+    __del__ = close
 
 
 class BatchPlan:

@@ -1054,6 +1054,46 @@ def test_multicase_graph_matches_eager(lib, torch_cuda):
     assert mc2.backward_error().max() <= 1e-12 and mc2.unserved() == 0
 
 
+def test_ragged_factor_matches_per_case(lib, torch_cuda):
+    """One complex64 factor launch per row-tile class over every case of a
+    substep (KL = 24, 48 and 39: both classes) gives the per-case step's
+    bits, replayed from a CUDA graph and issued directly."""
+    torch = torch_cuda
+    from suzerain_gb300 import multicase, plan as P, synth
+    cfgs = [synth.Config("a", 5, 48, 6, 8, 8, synth.FOURPI, synth.FOURPI / 3, 1e-3, seed=11),
+            synth.Config("b", 7, 64, 8, 8, 6, synth.FOURPI, synth.FOURPI / 3, 1e-3, seed=12),
+            synth.Config("c", 5, 96, 9, 16, 8, synth.FOURPI, synth.FOURPI / 3, 1e-3, seed=13)]
+    spec = P.RefineSpec(aiter=5, siter=3, diter=5, tolsc=145.0)
+    ref = multicase.MultiCase(cfgs, nstreams=2)
+    ref.capture("M", spec)
+    ref.reset()
+    ref.replay()
+    torch.cuda.synchronize()
+    want = [ref.result(i).cpu().numpy() for i in range(len(cfgs))]
+    kls = sorted(cs.KL for cs in ref.cases)
+    assert kls[0] <= 40 < kls[-1] <= 56, kls
+    rg = multicase.MultiCase(cfgs, nstreams=2, ragged=True)
+    rg.capture("M", spec)
+    rg.reset()
+    rg.replay()
+    torch.cuda.synchronize()
+    for i in range(len(cfgs)):
+        assert np.array_equal(rg.result(i).cpu().numpy(), want[i]), i
+    assert rg.unserved() == 0 and rg.backward_error().max() <= 1e-12
+    # issued directly, without the graph
+    rg.reset()
+    rg.step_capturable("M", spec)
+    torch.cuda.synchronize()
+    for i in range(len(cfgs)):
+        assert np.array_equal(rg.result(i).cpu().numpy(), want[i]), i
+    rg.close()
+    # the creation checks: a plan without its mixed workspace
+    bare = P.Plan(*cfgs[0].batch()[:3])
+    with pytest.raises(RuntimeError, match="sgb_ragged_create"):
+        P.RaggedFactor([bare], [1e-3], spec)
+    bare.close()
+
+
 def test_serving_result_same_alone_and_in_the_mix(lib, torch_cuda):
     """Continuous batching: requests that arrive while others run are
     admitted under the memory budget and overlap on the device; each
