@@ -206,6 +206,7 @@ _SIGS = {
     "sgb_plan_pool_trim": (_i, [_sz]),
     "sgb_gbtrs_set_quad_depth": (_i, [_i, _i]),
     "sgb_gbtrs_set_quad_bulk": (_i, [_i]),
+    "sgb_gbtrf_set_specialized": (_i, [_i]),
     "sgb_async_faults": (_i, []),
     "sgb_plan_substep": (_i, [_p, C.c_char, _d, _d, _p, _p,
                               C.POINTER(RefineSpec), _p]),

@@ -38,6 +38,8 @@ def sources() -> list[str]:
 BLK_INST = "gbtrf_blk_inst.cu"
 BLK_VARIANTS = [(p, nb, fam) for nb in (16, 8, 4) for p in ("z", "c")
                 for fam in (0, 1, 2, 4)]
+# and once per bandwidth of the compile-time complex64 instances
+BLK_SPEC_BANDS = (24, 34, 48)
 
 
 def jobs() -> list[tuple[str, str, list[str]]]:
@@ -50,6 +52,8 @@ def jobs() -> list[tuple[str, str, list[str]]]:
                 out.append((src, f"gbtrf_blk_{p}{nb}_f{fam}",
                             [f"-DSGB_BLK_R={r}", f"-DSGB_BLK_NB={nb}",
                              f"-DSGB_BLK_FAM={fam}"]))
+            for kb in BLK_SPEC_BANDS:
+                out.append((src, f"gbtrf_blk_spec{kb}", [f"-DSGB_BLK_SPEC={kb}"]))
         else:
             out.append((src, os.path.basename(src), []))
     return out

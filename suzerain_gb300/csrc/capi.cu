@@ -816,15 +816,18 @@ extern "C" int sgb_plan_substep_stage(sgb_plan *p, int stage, char method, doubl
 }
 
 // A ragged batch: the complex64 factors of many plans' substeps (each at its
-// own phi_imp) as one launch per row-tile class (KL <= 40 and KL <= 56), one
-// CTA per system position, the largest plans' systems first.
+// own phi_imp) as one launch per kernel kind (the compile-time bandwidth
+// instances, else the generic ones for KL <= 40 and KL <= 56), one CTA per
+// system position, the largest plans' systems first.
 struct sgb_ragged {
     struct Class {
+        int kind = 0;             // ragged_kind of its plans' geometry
         RaggedDesc *descs = nullptr;
         int2 *items = nullptr;
-        int nitems = 0, maxtr = 5;
+        int nitems = 0;
         size_t smem = 0;
-    } cls[2];
+    };
+    std::vector<Class> cls;
     std::vector<sgb_plan *> plans;
     std::vector<void *> rws;      // each plan's workspace when the batch was made
 };
@@ -838,8 +841,12 @@ extern "C" sgb_ragged *sgb_ragged_create(sgb_plan *const *plans, int nplans, con
     if (spec && spec->siter < 0) { fail("sgb_ragged_create: needs siter >= 0"); return nullptr; }
     auto *r = new (std::nothrow) sgb_ragged;
     if (!r) { fail("sgb_ragged_create: out of memory"); return nullptr; }
-    std::vector<RaggedDesc> hd[2];
-    std::vector<std::pair<long long, int>> order[2];   // (cost, plan) per class
+    struct Acc {
+        std::vector<RaggedDesc> descs;
+        std::vector<std::pair<long long, int>> order;   // (cost, plan)
+        size_t smem = 0;
+    };
+    std::map<int, Acc> acc;
     std::vector<int> where(nplans);
     for (int i = 0; i < nplans; ++i) {
         sgb_plan *p = plans[i];
@@ -857,30 +864,31 @@ extern "C" sgb_ragged *sgb_ragged_create(sgb_plan *const *plans, int nplans, con
         }
         RaggedDesc d;
         refine_ragged_desc(P, p->rws, d);
-        const int c = p->KL <= 40 ? 0 : 1;
-        where[i] = (int) hd[c].size();
-        hd[c].push_back(d);
-        order[c].push_back({(long long) p->N * p->KL * (p->KL + p->KU), i});
-        const size_t sm = gbtrf_blk_smem_bytes(sizeof(float), d.g, p->hc.S, 4, 2);
-        r->cls[c].smem = std::max(r->cls[c].smem, sm);
+        Acc &a = acc[ragged_kind(d.g)];
+        where[i] = (int) a.descs.size();
+        a.descs.push_back(d);
+        a.order.push_back({(long long) p->N * p->KL * (p->KL + p->KU), i});
+        a.smem = std::max(a.smem, gbtrf_blk_smem_bytes(sizeof(float), d.g, p->hc.S, 4, 2));
         r->plans.push_back(p);
         r->rws.push_back(p->rws);
     }
     cudaError_t e = cudaSuccess;
-    for (int c = 0; c < 2; ++c) {
-        sgb_ragged::Class &k = r->cls[c];
-        k.maxtr = c == 0 ? 5 : 7;
-        if (hd[c].empty()) continue;
-        std::sort(order[c].begin(), order[c].end(),
-                  [](const std::pair<long long, int> &a, const std::pair<long long, int> &b) {
-                      return a.first > b.first;
+    for (auto &kv : acc) {
+        Acc &a = kv.second;
+        r->cls.emplace_back();
+        sgb_ragged::Class &k = r->cls.back();
+        k.kind = kv.first;
+        k.smem = a.smem;
+        std::sort(a.order.begin(), a.order.end(),
+                  [](const std::pair<long long, int> &x, const std::pair<long long, int> &y) {
+                      return x.first > y.first;
                   });
         std::vector<int2> it;
-        for (auto &o : order[c])
+        for (auto &o : a.order)
             for (int k2 = 0; k2 < plans[o.second]->nsys; ++k2) it.push_back(make_int2(where[o.second], k2));
         k.nitems = (int) it.size();
-        if ((e = cudaMalloc(&k.descs, hd[c].size() * sizeof(RaggedDesc))) != cudaSuccess) break;
-        if ((e = cudaMemcpy(k.descs, hd[c].data(), hd[c].size() * sizeof(RaggedDesc),
+        if ((e = cudaMalloc(&k.descs, a.descs.size() * sizeof(RaggedDesc))) != cudaSuccess) break;
+        if ((e = cudaMemcpy(k.descs, a.descs.data(), a.descs.size() * sizeof(RaggedDesc),
                             cudaMemcpyHostToDevice)) != cudaSuccess) break;
         if ((e = cudaMalloc(&k.items, it.size() * sizeof(int2))) != cudaSuccess) break;
         if ((e = cudaMemcpy(k.items, it.data(), it.size() * sizeof(int2), cudaMemcpyHostToDevice)) != cudaSuccess)
@@ -901,7 +909,7 @@ extern "C" void sgb_ragged_destroy(sgb_ragged *r)
     delete r;
 }
 
-// The ragged factor launch(es), after every plan's stage 1 and before its
+// The ragged factor launches, after every plan's stage 1 and before its
 // stage 2 (on the stream given, capturable).
 extern "C" int sgb_ragged_factor(sgb_ragged *r, void *stream)
 {
@@ -910,13 +918,20 @@ extern "C" int sgb_ragged_factor(sgb_ragged *r, void *stream)
     for (size_t i = 0; i < r->plans.size(); ++i)
         if (r->plans[i]->rws != r->rws[i])
             return fail("sgb_ragged_factor: a plan's workspace moved since the batch was made");
-    for (int c = 0; c < 2; ++c) {
-        const auto &k = r->cls[c];
+    for (const auto &k : r->cls) {
         if (k.nitems == 0) continue;
         count_launch(1);
-        SGB_CUDA_TRY(launch_gbtrf_ragged(k.descs, k.items, k.nitems, k.maxtr, k.smem, st));
+        SGB_CUDA_TRY(launch_gbtrf_ragged(k.descs, k.items, k.nitems, k.kind, k.smem, st));
     }
     for (sgb_plan *p : r->plans) p->note(st);
+    return 0;
+}
+
+// Compile-time bandwidth instances of the complex64 factor on (1, the
+// default) or off; both give the same bits.
+extern "C" int sgb_gbtrf_set_specialized(int on)
+{
+    gbtrf_set_specialized(on);
     return 0;
 }
 

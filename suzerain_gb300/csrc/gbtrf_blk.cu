@@ -5,6 +5,7 @@
 #include "gbtrf_blk.cuh"
 
 #include <algorithm>
+#include <atomic>
 #include <mutex>
 #include <map>
 #include <tuple>
@@ -82,12 +83,51 @@ cudaError_t launch_nb(const GbtrfArgs &a, int nw, cudaStream_t st)
 }
 }  // namespace
 
-cudaError_t launch_gbtrf_ragged(const RaggedDesc *descs, const int2 *items, int nitems, int maxtr,
+namespace {
+std::atomic<int> g_spec{1};
+}  // namespace
+
+void gbtrf_set_specialized(int on) { g_spec.store(on ? 1 : 0); }
+
+int gbtrf_spec_band(const FactorGeom &g)
+{
+    if (!g_spec.load() || g.KL != g.KU || g.N % 4 != 0) return 0;
+    for (int kb : kSpecBands)
+        if (g.KL == kb) return kb;
+    return 0;
+}
+
+cudaError_t launch_blk_spec_any(const GbtrfArgs &a, cudaStream_t st, bool *done)
+{
+    *done = false;
+    if (a.prec != 'C') return cudaSuccess;
+    switch (gbtrf_spec_band(a.g)) {
+    case 24: *done = true; return launch_blk_spec<24>(a, st);
+    case 34: *done = true; return launch_blk_spec<34>(a, st);
+    case 48: *done = true; return launch_blk_spec<48>(a, st);
+    default: return cudaSuccess;
+    }
+}
+
+int ragged_kind(const FactorGeom &g)
+{
+    const int kb = gbtrf_spec_band(g);
+    return kb ? kb : (g.KL <= 40 ? -5 : -7);
+}
+
+cudaError_t launch_gbtrf_ragged(const RaggedDesc *descs, const int2 *items, int nitems, int kind,
                                 size_t smem, cudaStream_t st)
 {
     if (nitems <= 0) return cudaSuccess;
-    if (maxtr != 5 && maxtr != 7) return cudaErrorInvalidValue;
-    auto kern = maxtr == 5 ? k_gbtrf_ragged<5> : k_gbtrf_ragged<7>;
+    void (*kern)(const RaggedDesc *, const int2 *) = nullptr;
+    switch (kind) {
+    case -5: kern = k_gbtrf_ragged<5>; break;
+    case -7: kern = k_gbtrf_ragged<7>; break;
+    case 24: kern = k_gbtrf_ragged<5, 24, 24, true>; break;
+    case 34: kern = k_gbtrf_ragged<5, 34, 34, true>; break;
+    case 48: kern = k_gbtrf_ragged<7, 48, 48, true>; break;
+    default: return cudaErrorInvalidValue;
+    }
     cudaError_t e = smem_attr((const void *) kern, smem);
     if (e != cudaSuccess) return e;
     kern<<<nitems, 64, smem, st>>>(descs, items);
@@ -100,6 +140,11 @@ cudaError_t launch_gbtrf_blk(const GbtrfArgs &a, int nb, int nw, cudaStream_t st
         if (nb == 4) return launch_nb<double, 4>(a, nw, st);
         if (nb == 16) return launch_nb<double, 16>(a, nw, st);
         return launch_nb<double, 8>(a, nw, st);
+    }
+    if (nb == 4 && nw == 2 && a.variant != 2) {
+        bool done = false;
+        const cudaError_t e = launch_blk_spec_any(a, st, &done);
+        if (done) return e;
     }
     if (nb == 4) return launch_nb<float, 4>(a, nw, st);
     if (nb == 16) return launch_nb<float, 16>(a, nw, st);

@@ -419,7 +419,13 @@ constexpr int blk_min_blocks() { return sizeof(R) == 8 ? (NW == 4 ? 3 : 4) : (NW
 
 // The factor of one system s (factor, pivots and info at index fi) by the
 // CTA: the body of the phased kernel below and of the ragged kernel.
-template <typename R, int NB, int NW, int MAXTR, bool MODEL, bool FWD, typename MST = ModelSource>
+// CKL, CKU > 0: the bandwidths fixed at compile time (they must equal g.KL,
+// g.KU), so that the window's extents, pitch and wrap-arounds fold into
+// immediates; NFULL: N is a multiple of NB, every panel is full.  Both only
+// change the instruction stream, not the arithmetic: the factors are
+// bit-identical to the generic instance's.
+template <typename R, int NB, int NW, int MAXTR, bool MODEL, bool FWD, typename MST = ModelSource,
+          int CKL = 0, int CKU = 0, bool NFULL = false>
 __device__ __forceinline__ void
 gbtrf_cta_system(const FactorGeom g, int s, long long fi, const PackedSource src,
                  MST ms, cplx_t<R> *__restrict__ fac, long long fac_stride,
@@ -438,7 +444,7 @@ gbtrf_cta_system(const FactorGeom g, int s, long long fi, const PackedSource src
     static_assert((1 << LNB) == NB, "NB must be 4, 8 or 16");
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
-    const int N = g.N, KL = g.KL, KU = g.KU, UW = g.UW();
+    const int N = g.N, KL = CKL ? CKL : g.KL, KU = CKU ? CKU : g.KU, UW = KL + KU + 1;
     const int WR = KL + NB, WC = KL + KU + NB, P = blk_pitch(WC);
     const int S = MODEL ? ms.cs.S : 1;
     const unsigned magic = (MODEL && S > 1) ? (unsigned) ((0x100000000ull + S - 1) / S) : 0u;
@@ -505,7 +511,7 @@ gbtrf_cta_system(const FactorGeom g, int s, long long fi, const PackedSource src
 
     int rb = 0, cb = 0;
     for (int j0 = 0; j0 < N; j0 += NB) {
-        const int nbk = imin(NB, N - j0);
+        const int nbk = NFULL ? NB : imin(NB, N - j0);
         const bool more = j0 + nbk < N;
         auto rsl = [&](int i) { int t = rb + i; return t >= WR ? t - WR : t; };
         auto csl = [&](int c) { int t = cb + c; return t >= WC ? t - WC : t; };
@@ -704,7 +710,8 @@ gbtrf_cta_system(const FactorGeom g, int s, long long fi, const PackedSource src
         for (int ph = 0; ph < 9; ++ph) atomicAdd(prof + ph, clk[ph]);
 }
 
-template <typename R, int NB, int NW, int MAXTR, bool MODEL, bool FWD>
+template <typename R, int NB, int NW, int MAXTR, bool MODEL, bool FWD, int CKL = 0, int CKU = 0,
+          bool NFULL = false>
 __global__ void __launch_bounds__(32 * NW, (blk_min_blocks<R, NW>()))
 k_gbtrf_cta(FactorGeom g, int nsys, PackedSource src, ModelSource ms,
             cplx_t<R> *__restrict__ fac, long long fac_stride,
@@ -718,18 +725,19 @@ k_gbtrf_cta(FactorGeom g, int nsys, PackedSource src, ModelSource ms,
     const int s = sys_list ? sys_list[blockIdx.x] : (int) blockIdx.x;
     if (s < 0 || s >= nsys) return;
     const long long fi = slot_mode ? (long long) blockIdx.x : (long long) s;
-    gbtrf_cta_system<R, NB, NW, MAXTR, MODEL, FWD>(g, s, fi, src, ms, fac, fac_stride, ipiv, info, rhs,
+    gbtrf_cta_system<R, NB, NW, MAXTR, MODEL, FWD, ModelSource, CKL, CKU, NFULL>(g, s, fi, src, ms, fac, fac_stride, ipiv, info, rhs,
                                                    rhs_stride, y, y_stride, prof);
 }
 
 // Ragged factor: one CTA per work item (plan d, list position k), the
 // items in the order given (the largest plans' systems first, which the
 // block scheduler dispatches first); each item is one system of one plan,
-// of that plan's own geometry (KL <= 8 MAXTR), or nothing when k is beyond
+// of that plan's own geometry (KL <= 8 MAXTR; KL = CKL, KU = CKU and N a
+// multiple of 4 in the specialized instances), or nothing when k is beyond
 // the plan's active count.  The plan's descriptor is read once into shared
 // memory (fewer registers than a copy in registers; no spills at MAXTR 5).
 // The shared memory is sized for the largest window of the batch.
-template <int MAXTR>
+template <int MAXTR, int CKL = 0, int CKU = 0, bool NFULL = false>
 __global__ void __launch_bounds__(64, (blk_min_blocks<float, 2>()))
 k_gbtrf_ragged(const RaggedDesc *__restrict__ descs, const int2 *__restrict__ items)
 {
@@ -739,7 +747,7 @@ k_gbtrf_ragged(const RaggedDesc *__restrict__ descs, const int2 *__restrict__ it
     __syncthreads();
     if (w.y >= *sd.d_count) return;
     const int s = sd.sys_list[w.y];
-    gbtrf_cta_system<float, 4, 2, MAXTR, true, true, const ModelSource &>(
+    gbtrf_cta_system<float, 4, 2, MAXTR, true, true, const ModelSource &, CKL, CKU, NFULL>(
         sd.g, s, s, PackedSource{}, sd.ms, sd.fac, sd.fac_stride, sd.ipiv, sd.info, sd.rhs,
         sd.rhs_stride, sd.y, sd.y_stride, nullptr);
 }
@@ -1050,14 +1058,15 @@ k_gbtrf_la(FactorGeom g, int nsys, PackedSource src, ModelSource ms,
         for (int ph = 0; ph < 6; ++ph) atomicAdd(prof + ph, clk[ph]);
 }
 
-template <typename R, int NB, int NW, int MAXTR, bool LA, bool MODEL, bool FWD>
+template <typename R, int NB, int NW, int MAXTR, bool LA, bool MODEL, bool FWD, int CKL = 0,
+          int CKU = 0, bool NFULL = false>
 cudaError_t launch_cta_one(const GbtrfArgs &a, cudaStream_t st)
 {
     const int S = MODEL ? a.ms.cs.S : 1;
     const size_t smem = gbtrf_blk_smem_bytes(sizeof(R), a.g, S, NB, LA ? -NW : NW);
     auto kern = [] {
         if constexpr (LA) return k_gbtrf_la<R, NB, NW, MODEL, FWD>;
-        else return k_gbtrf_cta<R, NB, NW, MAXTR, MODEL, FWD>;
+        else return k_gbtrf_cta<R, NB, NW, MAXTR, MODEL, FWD, CKL, CKU, NFULL>;
     }();
     cudaError_t e = smem_attr((const void *) kern, smem);
     if (e != cudaSuccess) return e;
@@ -1089,5 +1098,17 @@ cudaError_t launch_cta_r(const GbtrfArgs &a, cudaStream_t st)
 // MAXTR rows of the trailing update per thread.
 template <typename R, int NB, int FAM>
 cudaError_t launch_blk_fam(const GbtrfArgs &a, int nw, cudaStream_t st);
+
+// Bandwidths with compile-time instances of the complex64 phased kernel
+// (NB = 4, two warps; N a multiple of 4): the geometries of the B-spline
+// operators with S = 5 or 7 equations and order k = 6 or 8 (KL = KU =
+// S (k - 1) - 1 = 24, 34, 48).  Each has its own translation unit
+// (gbtrf_blk_inst.cu with SGB_BLK_SPEC set).
+constexpr int kSpecBands[] = {24, 34, 48};
+template <int KB>
+cudaError_t launch_blk_spec(const GbtrfArgs &a, cudaStream_t st);
+// The specialized launch for a's geometry when one exists (complex64, NB 4,
+// nw 2, KL = KU in kSpecBands, N % 4 == 0); *done false otherwise.
+cudaError_t launch_blk_spec_any(const GbtrfArgs &a, cudaStream_t st, bool *done);
 
 }  // namespace sgb

@@ -1,7 +1,9 @@
 // Blocked band LU kernels of one (precision, panel width, warp family).
 // The build compiles this file once per triple with -DSGB_BLK_R=float|double
 // -DSGB_BLK_NB=4|8|16 -DSGB_BLK_FAM=0|1|2|4 (24 objects, compiled in
-// parallel); without those definitions it instantiates nothing.
+// parallel), and once per specialized bandwidth with -DSGB_BLK_SPEC=KB (the
+// complex64 phased kernel with KL = KU = KB fixed at compile time); without
+// those definitions it instantiates nothing.
 #include "gbtrf_blk.cuh"
 
 namespace sgb {
@@ -23,6 +25,22 @@ cudaError_t launch_blk_fam(const GbtrfArgs &a, int nw, cudaStream_t st)
         return KL <= 48 ? launch_cta_r<R, NB, 4, 3, false>(a, st)
                         : launch_cta_r<R, NB, 4, 4, false>(a, st);
 }
+
+template <int KB>
+cudaError_t launch_blk_spec(const GbtrfArgs &a, cudaStream_t st)
+{
+    constexpr int MT = KB <= 40 ? 5 : 7;          // the generic family's row tiles
+    const bool fwd = a.rhs != nullptr;
+    if (a.model)
+        return fwd ? launch_cta_one<float, 4, 2, MT, false, true, true, KB, KB, true>(a, st)
+                   : launch_cta_one<float, 4, 2, MT, false, true, false, KB, KB, true>(a, st);
+    return fwd ? launch_cta_one<float, 4, 2, MT, false, false, true, KB, KB, true>(a, st)
+               : launch_cta_one<float, 4, 2, MT, false, false, false, KB, KB, true>(a, st);
+}
+
+#if defined(SGB_BLK_SPEC)
+template cudaError_t launch_blk_spec<SGB_BLK_SPEC>(const GbtrfArgs &, cudaStream_t);
+#endif
 
 #if defined(SGB_BLK_R) && defined(SGB_BLK_NB) && defined(SGB_BLK_FAM)
 template cudaError_t launch_blk_fam<SGB_BLK_R, SGB_BLK_NB, SGB_BLK_FAM>(

@@ -51,10 +51,18 @@ struct RaggedDesc {
     const int *d_count;
 };
 // The ragged factor over descriptors and (descriptor, list position) items
-// in device memory, one CTA per item; maxtr 5 for KL <= 40, 7 for KL <= 56;
-// smem the largest window's bytes.
-cudaError_t launch_gbtrf_ragged(const RaggedDesc *descs, const int2 *items, int nitems, int maxtr,
+// in device memory, one CTA per item; kind (ragged_kind of every item's
+// geometry) 24, 34 or 48 for the compile-time bandwidth instances, -5 for
+// the generic one with KL <= 40, -7 for KL <= 56; smem the largest window's
+// bytes.
+cudaError_t launch_gbtrf_ragged(const RaggedDesc *descs, const int2 *items, int nitems, int kind,
                                 size_t smem, cudaStream_t st);
+int ragged_kind(const FactorGeom &g);
+// The compile-time bandwidth of the complex64 phased factor's instance for
+// g (KL = KU in 24, 34, 48 and N % 4 == 0), or 0 for the generic instance;
+// gbtrf_set_specialized(0) makes every geometry take the generic one.
+int gbtrf_spec_band(const FactorGeom &g);
+void gbtrf_set_specialized(int on);
 
 cudaError_t launch_gbtrf(const GbtrfArgs &a, cudaStream_t st);
 cudaError_t launch_gbtrf_blk(const GbtrfArgs &a, int nb, int nw, cudaStream_t st);

@@ -117,6 +117,66 @@ def test_blocked_factor_equals_unblocked(lib, torch_cuda, n, kl, ku, prec):
         assert np.array_equal(fac.view(fv), outs[0][0].view(fv)), (nb, nw)
 
 
+def test_specialized_factor_matches_generic(lib, torch_cuda):
+    """The complex64 factor's compile-time bandwidth instances (KL = KU = 24,
+    34, 48, N a multiple of 4) give the generic instance's bits: factors,
+    pivots and info of packed bands with frequent pivoting (with and without
+    the fused forward elimination), and the mixed substeps of plans whose
+    operators assemble in the kernel, per case and as one ragged batch."""
+    torch = torch_cuda
+    from suzerain_gb300 import multicase, plan as P, synth
+    rng = np.random.default_rng(77)
+    nsys = 6
+    try:
+        for n, kl in ((240, 24), (480, 34), (192, 48), (97, 34)):
+            ku = kl
+            bands = [rand_band(rng, n, kl, ku)[0] for _ in range(nsys)]
+            for b_ in bands:
+                for j in range(n):
+                    if rng.random() < 0.3:
+                        for i in range(max(0, j - ku), min(n, j + kl + 1)):
+                            b_[ku + i - j + j * (kl + ku + 1)] *= 8.0
+            ld = kl + ku + 1
+            ab = dev(torch, np.stack(bands))
+            fe = lib.sgb_factor_elems(n, kl, ku)
+            outs = []
+            for on in (0, 1):
+                assert lib.sgb_gbtrf_set_specialized(on) == 0
+                fac = torch.full((nsys * fe,), float("nan"), dtype=torch.complex64, device="cuda")
+                ipiv = torch.zeros(nsys * n, dtype=torch.int32, device="cuda")
+                info = torch.zeros(nsys, dtype=torch.int32, device="cuda")
+                assert lib.sgb_gbtrf_batched_ex(b"C", nsys, n, kl, ku, ab.data_ptr(), ld, ld * n,
+                                                fac.data_ptr(), ipiv.data_ptr(), info.data_ptr(), 0,
+                                                4, 2, 0) == 0, lib.sgb_last_error().decode()
+                torch.cuda.synchronize()
+                outs.append((fac.cpu().numpy().view(np.float32), ipiv.cpu().numpy(),
+                             info.cpu().numpy()))
+            for x, y in zip(outs[0], outs[1]):
+                assert np.array_equal(x, y), (n, kl)
+        # plans (model assembly + fused forward elimination), KL = 24, 48, 34
+        cfgs = [synth.Config("a", 5, 48, 6, 8, 8, synth.FOURPI, synth.FOURPI / 3, 1e-3, seed=11),
+                synth.Config("b", 7, 64, 8, 8, 6, synth.FOURPI, synth.FOURPI / 3, 1e-3, seed=12),
+                synth.Config("c", 5, 96, 8, 16, 8, synth.FOURPI, synth.FOURPI / 3, 1e-3, seed=13)]
+        spec = P.RefineSpec(aiter=5, siter=3, diter=5, tolsc=145.0)
+        res = {}
+        for on in (0, 1):
+            assert lib.sgb_gbtrf_set_specialized(on) == 0
+            for ragged in (False, True):
+                mc = multicase.MultiCase(cfgs, nstreams=2, ragged=ragged)
+                mc.capture("M", spec)
+                mc.reset()
+                mc.replay()
+                torch.cuda.synchronize()
+                res[(on, ragged)] = [mc.result(i).cpu().numpy() for i in range(len(cfgs))]
+                mc.close()
+        assert sorted(c.KL for c in mc.cases) == [24, 34, 48]
+        for key, r in res.items():
+            for i in range(len(cfgs)):
+                assert np.array_equal(r[i], res[(0, False)][i]), (key, i)
+    finally:
+        lib.sgb_gbtrf_set_specialized(1)
+
+
 @pytest.mark.parametrize("n,kl,ku", [(40, 3, 5), (240, 34, 34), (97, 48, 48)])
 @pytest.mark.parametrize("trans", ["N", "T", "C"])
 @pytest.mark.parametrize("prec", ["Z", "C"])
