@@ -141,7 +141,7 @@ cudaError_t launch_gbtrf_blk(const GbtrfArgs &a, int nb, int nw, cudaStream_t st
         if (nb == 16) return launch_nb<double, 16>(a, nw, st);
         return launch_nb<double, 8>(a, nw, st);
     }
-    if (nb == 4 && nw == 2 && a.variant != 2) {
+    if (nb == 4 && nw == 2 && a.variant != 2 && !a.prof) {
         bool done = false;
         const cudaError_t e = launch_blk_spec_any(a, st, &done);
         if (done) return e;

@@ -423,9 +423,11 @@ constexpr int blk_min_blocks() { return sizeof(R) == 8 ? (NW == 4 ? 3 : 4) : (NW
 // g.KU), so that the window's extents, pitch and wrap-arounds fold into
 // immediates; NFULL: N is a multiple of NB, every panel is full.  Both only
 // change the instruction stream, not the arithmetic: the factors are
-// bit-identical to the generic instance's.
+// bit-identical to the generic instance's.  PROF: the per-phase cycle
+// counters (diagnostics) are compiled in and kept when prof is set; without
+// it the counting code and its branches are absent.
 template <typename R, int NB, int NW, int MAXTR, bool MODEL, bool FWD, typename MST = ModelSource,
-          int CKL = 0, int CKU = 0, bool NFULL = false>
+          int CKL = 0, int CKU = 0, bool NFULL = false, bool PROF = false>
 __device__ __forceinline__ void
 gbtrf_cta_system(const FactorGeom g, int s, long long fi, const PackedSource src,
                  MST ms, cplx_t<R> *__restrict__ fac, long long fac_stride,
@@ -471,7 +473,7 @@ gbtrf_cta_system(const FactorGeom g, int s, long long fi, const PackedSource src
     // (+ staging), 2 interchanges + U12, 3 GEMM + U rows out, 5 retire/enter;
     // 6..8 the panel's sub-phases; 10 and 11 the last marks.
     unsigned long long *clk = reinterpret_cast<unsigned long long *>(shv + 4);
-    const bool timing = prof && tid == 0;
+    const bool timing = PROF && prof && tid == 0;
     if (timing) {
         for (int i = 0; i < 12; ++i) clk[i] = 0;
         clk[10] = clock64();
@@ -711,7 +713,7 @@ gbtrf_cta_system(const FactorGeom g, int s, long long fi, const PackedSource src
 }
 
 template <typename R, int NB, int NW, int MAXTR, bool MODEL, bool FWD, int CKL = 0, int CKU = 0,
-          bool NFULL = false>
+          bool NFULL = false, bool PROF = false>
 __global__ void __launch_bounds__(32 * NW, (blk_min_blocks<R, NW>()))
 k_gbtrf_cta(FactorGeom g, int nsys, PackedSource src, ModelSource ms,
             cplx_t<R> *__restrict__ fac, long long fac_stride,
@@ -725,7 +727,7 @@ k_gbtrf_cta(FactorGeom g, int nsys, PackedSource src, ModelSource ms,
     const int s = sys_list ? sys_list[blockIdx.x] : (int) blockIdx.x;
     if (s < 0 || s >= nsys) return;
     const long long fi = slot_mode ? (long long) blockIdx.x : (long long) s;
-    gbtrf_cta_system<R, NB, NW, MAXTR, MODEL, FWD, ModelSource, CKL, CKU, NFULL>(g, s, fi, src, ms, fac, fac_stride, ipiv, info, rhs,
+    gbtrf_cta_system<R, NB, NW, MAXTR, MODEL, FWD, ModelSource, CKL, CKU, NFULL, PROF>(g, s, fi, src, ms, fac, fac_stride, ipiv, info, rhs,
                                                    rhs_stride, y, y_stride, prof);
 }
 
@@ -1064,8 +1066,15 @@ cudaError_t launch_cta_one(const GbtrfArgs &a, cudaStream_t st)
 {
     const int S = MODEL ? a.ms.cs.S : 1;
     const size_t smem = gbtrf_blk_smem_bytes(sizeof(R), a.g, S, NB, LA ? -NW : NW);
-    auto kern = [] {
+    // the phase counters: compiled into the generic packed-band instances
+    // only (the diagnostic entry's), absent elsewhere
+    constexpr bool CAN_PROF = LA || (!MODEL && !FWD && CKL == 0);
+    if (!CAN_PROF && a.prof) return cudaErrorInvalidValue;
+    auto kern = [&] {
         if constexpr (LA) return k_gbtrf_la<R, NB, NW, MODEL, FWD>;
+        else if constexpr (CAN_PROF)
+            return a.prof ? k_gbtrf_cta<R, NB, NW, MAXTR, MODEL, FWD, CKL, CKU, NFULL, true>
+                          : k_gbtrf_cta<R, NB, NW, MAXTR, MODEL, FWD, CKL, CKU, NFULL, false>;
         else return k_gbtrf_cta<R, NB, NW, MAXTR, MODEL, FWD, CKL, CKU, NFULL>;
     }();
     cudaError_t e = smem_attr((const void *) kern, smem);
