@@ -629,7 +629,8 @@ int sgb_gbtrf_batched(char prec, int nsys, int N, int KL, int KU,
 
 /** sgb_gbtrf_batched with the kernel chosen explicitly: variant 0 is the
  *  blocked kernel with panel width nb (4, 8 or 16) and nw warps per system
- *  (1, 2 or 4; KL <= 52, 56, 63 respectively; N < 65536), variant 2 its
+ *  (1, 2 or 4; KL <= 52, 56, 63 respectively; N < 65536; nw 3 for complex64
+ *  with nb 4, KL = KU = 24 or 34 and N a multiple of 4), variant 2 its
  *  lookahead form (nw 2 or 4: the next panel is factored while the other
  *  warps apply the previous panel's update), variant 1 the unblocked kernel
  *  (nb, nw ignored).  nb or nw 0 takes the shape recorded by

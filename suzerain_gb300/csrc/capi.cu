@@ -108,7 +108,8 @@ extern "C" int sgb_gbtrf_batched_ex(char prec, int nsys, int N, int KL, int KU, 
         if (nw < 0) { variant = 2; nw = -nw; }
         if (!gbtrf_blk_supported({N, KL, KU}, nb, nw))
             return fail("sgb_gbtrf_batched_ex: blocked kernel needs nb in {4,8,16}, nw in {1,2,4}, "
-                        "KL <= 52/56/64 for nw 1/2/4 and N < 65536");
+                        "KL <= 52/56/64 for nw 1/2/4 and N < 65536 (nw 3: nb 4, KL = KU = 24 or "
+                        "34, N a multiple of 4)");
     }
     GbtrfArgs a;
     a.prec = prec; a.g = {N, KL, KU}; a.nsys = nsys;
@@ -144,7 +145,8 @@ extern "C" int sgb_gbtrf_phase_cycles(char prec, int nsys, int N, int KL, int KU
 extern "C" int sgb_gbtrf_set_shape(char prec, int N, int KL, int KU, int nb, int nw)
 {
     if (prec != 'Z' && prec != 'C') return fail("sgb_gbtrf_set_shape: prec must be 'Z' or 'C'");
-    if (!geom_ok(N, KL, KU) || nw == -1 || !gbtrf_blk_supported({N, KL, KU}, nb, nw < 0 ? -nw : nw))
+    if (!geom_ok(N, KL, KU) || nw == -1 || nw == -3 || (nw == 3 && prec != 'C') ||
+        !gbtrf_blk_supported({N, KL, KU}, nb, nw < 0 ? -nw : nw))
         return fail("sgb_gbtrf_set_shape: unsupported (N, KL, KU, nb, nw)");
     gbtrf_blk_set_choice(prec, {N, KL, KU}, nb, nw);
     return 0;

@@ -231,7 +231,7 @@ cudaError_t launch_gbtrf(const GbtrfArgs &a, cudaStream_t st)
         // complex64 assembly of the model reads the float band copies
         if (a.model && a.prec == 'C' && !a.ms.mdf) return cudaErrorInvalidValue;
         int nb = a.nb, nw = a.nw;
-        gbtrf_blk_choice(a.prec, a.g, nb, nw);
+        gbtrf_blk_choice(a.prec, a.g, nb, nw, a.model);
         GbtrfArgs b = a;
         if (nw < 0) { b.variant = 2; nw = -nw; }   // the shape table's lookahead entries
         if (gbtrf_blk_supported(a.g, nb, nw)) return launch_gbtrf_blk(b, nb, nw, st);

@@ -36,6 +36,11 @@ size_t gbtrf_blk_smem_bytes(int prec_bytes, const FactorGeom &g, int S, int nb, 
 bool gbtrf_blk_supported(const FactorGeom &g, int nb, int nw)
 {
     if (nb != 4 && nb != 8 && nb != 16) return false;
+    if (nw == 3) {
+        // the three-warp shape of the specialized complex64 instances
+        const int kb = gbtrf_spec_band(g);
+        return nb == 4 && kb != 0 && spec_has_w3(kb);
+    }
     if (nw != 1 && nw != 2 && nw != 4) return false;
     const int maxkl = nw == 1 ? 52 : nw == 2 ? 56 : 64;
     if (g.KL > maxkl || g.N >= 65536) return false;
@@ -53,7 +58,7 @@ void gbtrf_blk_set_choice(char prec, const FactorGeom &g, int nb, int nw)
     g_tune[std::make_tuple(prec, g.N, g.KL, g.KU)] = {nb, nw};
 }
 
-void gbtrf_blk_choice(char prec, const FactorGeom &g, int &nb, int &nw)
+void gbtrf_blk_choice(char prec, const FactorGeom &g, int &nb, int &nw, bool model)
 {
     if (nb > 0 && nw != 0) return;          // nw < 0: the lookahead form, given
     {
@@ -69,7 +74,11 @@ void gbtrf_blk_choice(char prec, const FactorGeom &g, int &nb, int &nw)
     // narrow panels and two warps, complex128 (FP64-throughput bound) with
     // narrow panels and one warp.
     if (nb <= 0) nb = 4;
-    if (nw == 0) nw = g.KL > 56 ? 4 : (prec == 'C' || g.KL > 52) ? 2 : 1;
+    if (nw == 0) {
+        nw = g.KL > 56 ? 4 : (prec == 'C' || g.KL > 52) ? 2 : 1;
+        const int kb = prec == 'C' && nb == 4 && !model ? gbtrf_spec_band(g) : 0;
+        if (kb && spec_has_w3(kb)) nw = 3;
+    }
 }
 
 namespace {
@@ -97,18 +106,24 @@ int gbtrf_spec_band(const FactorGeom &g)
     return 0;
 }
 
-cudaError_t launch_blk_spec_any(const GbtrfArgs &a, cudaStream_t st, bool *done)
+cudaError_t launch_blk_spec_any(const GbtrfArgs &a, int nw, cudaStream_t st, bool *done)
 {
     *done = false;
-    if (a.prec != 'C') return cudaSuccess;
-    switch (gbtrf_spec_band(a.g)) {
-    case 24: *done = true; return launch_blk_spec<24>(a, st);
-    case 34: *done = true; return launch_blk_spec<34>(a, st);
-    case 48: *done = true; return launch_blk_spec<48>(a, st);
-    default: return cudaSuccess;
+    if (a.prec != 'C' || (nw != 2 && nw != 3)) return cudaSuccess;
+    const int kb = gbtrf_spec_band(a.g);
+    if (kb == 0 || (nw == 3 && !spec_has_w3(kb))) return cudaSuccess;
+    *done = true;
+    switch (kb) {
+    case 24: return launch_blk_spec<24>(a, nw, st);
+    case 34: return launch_blk_spec<34>(a, nw, st);
+    default: return launch_blk_spec<48>(a, nw, st);
     }
 }
 
+// Kind of the ragged factor instance for a plan of geometry g: the
+// specialized bandwidth instance as KB, else the generic one (-5 for
+// KL <= 40, -7 beyond); two warps (the rows are assembled from the model
+// operator, where a third warp gains nothing).
 int ragged_kind(const FactorGeom &g)
 {
     const int kb = gbtrf_spec_band(g);
@@ -121,11 +136,11 @@ cudaError_t launch_gbtrf_ragged(const RaggedDesc *descs, const int2 *items, int 
     if (nitems <= 0) return cudaSuccess;
     void (*kern)(const RaggedDesc *, const int2 *) = nullptr;
     switch (kind) {
-    case -5: kern = k_gbtrf_ragged<5>; break;
-    case -7: kern = k_gbtrf_ragged<7>; break;
-    case 24: kern = k_gbtrf_ragged<5, 24, 24, true>; break;
-    case 34: kern = k_gbtrf_ragged<5, 34, 34, true>; break;
-    case 48: kern = k_gbtrf_ragged<7, 48, 48, true>; break;
+    case -5: kern = k_gbtrf_ragged<2, 5>; break;
+    case -7: kern = k_gbtrf_ragged<2, 7>; break;
+    case 24: kern = k_gbtrf_ragged<2, spec_maxtr<24, 2>(), 24, 24, true>; break;
+    case 34: kern = k_gbtrf_ragged<2, spec_maxtr<34, 2>(), 34, 34, true>; break;
+    case 48: kern = k_gbtrf_ragged<2, spec_maxtr<48, 2>(), 48, 48, true>; break;
     default: return cudaErrorInvalidValue;
     }
     cudaError_t e = smem_attr((const void *) kern, smem);
@@ -137,15 +152,17 @@ cudaError_t launch_gbtrf_ragged(const RaggedDesc *descs, const int2 *items, int 
 cudaError_t launch_gbtrf_blk(const GbtrfArgs &a, int nb, int nw, cudaStream_t st)
 {
     if (a.prec == 'Z') {
+        if (nw == 3) nw = 2;     // three warps exist for complex64 only
         if (nb == 4) return launch_nb<double, 4>(a, nw, st);
         if (nb == 16) return launch_nb<double, 16>(a, nw, st);
         return launch_nb<double, 8>(a, nw, st);
     }
-    if (nb == 4 && nw == 2 && a.variant != 2 && !a.prof) {
+    if (nb == 4 && a.variant != 2 && !a.prof) {
         bool done = false;
-        const cudaError_t e = launch_blk_spec_any(a, st, &done);
+        const cudaError_t e = launch_blk_spec_any(a, nw, st, &done);
         if (done) return e;
     }
+    if (nw == 3) nw = 2;     // no specialized instance: the generic two-warp kernel
     if (nb == 4) return launch_nb<float, 4>(a, nw, st);
     if (nb == 16) return launch_nb<float, 16>(a, nw, st);
     return launch_nb<float, 8>(a, nw, st);

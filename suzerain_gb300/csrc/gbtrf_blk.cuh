@@ -415,7 +415,14 @@ __device__ __forceinline__ void assemble_rows(const PackedSource &src, const Mod
 // system (KL = KU = 34, NB = 4 or 8) leaves room for about 8 complex64 or 4
 // complex128 systems per SM.
 template <typename R, int NW>
-constexpr int blk_min_blocks() { return sizeof(R) == 8 ? (NW == 4 ? 3 : 4) : (NW == 4 ? 4 : 8); }
+constexpr int blk_min_blocks()
+{
+    // complex64 with three warps: registers are granted per scheduler in
+    // whole warps, so 80 registers a thread keep 8 CTAs (24 warps) resident
+    // and 81..96 only 6; asking for 7 gives 80 (a few spills), measured
+    // faster than 6 CTAs without spills
+    return sizeof(R) == 8 ? (NW == 4 ? 3 : 4) : (NW == 4 ? 4 : NW == 3 ? 7 : 8);
+}
 
 // The factor of one system s (factor, pivots and info at index fi) by the
 // CTA: the body of the phased kernel below and of the ragged kernel.
@@ -739,8 +746,8 @@ k_gbtrf_cta(FactorGeom g, int nsys, PackedSource src, ModelSource ms,
 // the plan's active count.  The plan's descriptor is read once into shared
 // memory (fewer registers than a copy in registers; no spills at MAXTR 5).
 // The shared memory is sized for the largest window of the batch.
-template <int MAXTR, int CKL = 0, int CKU = 0, bool NFULL = false>
-__global__ void __launch_bounds__(64, (blk_min_blocks<float, 2>()))
+template <int NW, int MAXTR, int CKL = 0, int CKU = 0, bool NFULL = false>
+__global__ void __launch_bounds__(32 * NW, (blk_min_blocks<float, NW>()))
 k_gbtrf_ragged(const RaggedDesc *__restrict__ descs, const int2 *__restrict__ items)
 {
     __shared__ RaggedDesc sd;
@@ -749,7 +756,7 @@ k_gbtrf_ragged(const RaggedDesc *__restrict__ descs, const int2 *__restrict__ it
     __syncthreads();
     if (w.y >= *sd.d_count) return;
     const int s = sd.sys_list[w.y];
-    gbtrf_cta_system<float, 4, 2, MAXTR, true, true, const ModelSource &, CKL, CKU, NFULL>(
+    gbtrf_cta_system<float, 4, NW, MAXTR, true, true, const ModelSource &, CKL, CKU, NFULL>(
         sd.g, s, s, PackedSource{}, sd.ms, sd.fac, sd.fac_stride, sd.ipiv, sd.info, sd.rhs,
         sd.rhs_stride, sd.y, sd.y_stride, nullptr);
 }
@@ -1109,15 +1116,23 @@ template <typename R, int NB, int FAM>
 cudaError_t launch_blk_fam(const GbtrfArgs &a, int nw, cudaStream_t st);
 
 // Bandwidths with compile-time instances of the complex64 phased kernel
-// (NB = 4, two warps; N a multiple of 4): the geometries of the B-spline
-// operators with S = 5 or 7 equations and order k = 6 or 8 (KL = KU =
-// S (k - 1) - 1 = 24, 34, 48).  Each has its own translation unit
-// (gbtrf_blk_inst.cu with SGB_BLK_SPEC set).
+// (NB = 4; N a multiple of 4): the geometries of the B-spline operators
+// with S = 5 or 7 equations and order k = 6 or 8 (KL = KU = S (k - 1) - 1 =
+// 24, 34, 48).  Each has its own translation unit (gbtrf_blk_inst.cu with
+// SGB_BLK_SPEC set).  Two warps use the generic family's row tiles (5 rows
+// per thread for KL <= 40, 7 beyond); KL <= 36 also has a three-warp shape
+// (nw 3: 12 row groups x 3 rows cover KL, 3 x 5 register tiles), the
+// default for a packed band (10 % faster at N = 960, KL = 34) and as fast
+// as two warps when the rows are assembled from the model operator, whose
+// default stays two.
 constexpr int kSpecBands[] = {24, 34, 48};
+constexpr bool spec_has_w3(int kb) { return kb <= 36; }
+template <int KB, int W> constexpr int spec_maxtr() { return W == 3 ? 3 : (KB <= 40 ? 5 : 7); }
 template <int KB>
-cudaError_t launch_blk_spec(const GbtrfArgs &a, cudaStream_t st);
-// The specialized launch for a's geometry when one exists (complex64, NB 4,
-// nw 2, KL = KU in kSpecBands, N % 4 == 0); *done false otherwise.
-cudaError_t launch_blk_spec_any(const GbtrfArgs &a, cudaStream_t st, bool *done);
+cudaError_t launch_blk_spec(const GbtrfArgs &a, int nw, cudaStream_t st);
+// The specialized launch for a's geometry and warp count when one exists
+// (complex64, NB 4, KL = KU in kSpecBands, N % 4 == 0, nw 2, or 3 where
+// the band has that shape); *done false otherwise.
+cudaError_t launch_blk_spec_any(const GbtrfArgs &a, int nw, cudaStream_t st, bool *done);
 
 }  // namespace sgb

@@ -26,20 +26,28 @@ cudaError_t launch_blk_fam(const GbtrfArgs &a, int nw, cudaStream_t st)
                         : launch_cta_r<R, NB, 4, 4, false>(a, st);
 }
 
-template <int KB>
-cudaError_t launch_blk_spec(const GbtrfArgs &a, cudaStream_t st)
+template <int KB, int W>
+cudaError_t launch_blk_spec_w(const GbtrfArgs &a, cudaStream_t st)
 {
-    constexpr int MT = KB <= 40 ? 5 : 7;          // the generic family's row tiles
+    constexpr int MT = spec_maxtr<KB, W>();
     const bool fwd = a.rhs != nullptr;
     if (a.model)
-        return fwd ? launch_cta_one<float, 4, 2, MT, false, true, true, KB, KB, true>(a, st)
-                   : launch_cta_one<float, 4, 2, MT, false, true, false, KB, KB, true>(a, st);
-    return fwd ? launch_cta_one<float, 4, 2, MT, false, false, true, KB, KB, true>(a, st)
-               : launch_cta_one<float, 4, 2, MT, false, false, false, KB, KB, true>(a, st);
+        return fwd ? launch_cta_one<float, 4, W, MT, false, true, true, KB, KB, true>(a, st)
+                   : launch_cta_one<float, 4, W, MT, false, true, false, KB, KB, true>(a, st);
+    return fwd ? launch_cta_one<float, 4, W, MT, false, false, true, KB, KB, true>(a, st)
+               : launch_cta_one<float, 4, W, MT, false, false, false, KB, KB, true>(a, st);
+}
+
+template <int KB>
+cudaError_t launch_blk_spec(const GbtrfArgs &a, int nw, cudaStream_t st)
+{
+    if constexpr (spec_has_w3(KB))
+        if (nw == 3) return launch_blk_spec_w<KB, 3>(a, st);
+    return launch_blk_spec_w<KB, 2>(a, st);
 }
 
 #if defined(SGB_BLK_SPEC)
-template cudaError_t launch_blk_spec<SGB_BLK_SPEC>(const GbtrfArgs &, cudaStream_t);
+template cudaError_t launch_blk_spec<SGB_BLK_SPEC>(const GbtrfArgs &, int, cudaStream_t);
 #endif
 
 #if defined(SGB_BLK_R) && defined(SGB_BLK_NB) && defined(SGB_BLK_FAM)

@@ -52,7 +52,7 @@ struct RaggedDesc {
 };
 // The ragged factor over descriptors and (descriptor, list position) items
 // in device memory, one CTA per item; kind (ragged_kind of every item's
-// geometry) 24, 34 or 48 for the compile-time bandwidth instances, -5 for
+// geometry) KB for the compile-time bandwidth instances (two warps), -5 for
 // the generic one with KL <= 40, -7 for KL <= 56; smem the largest window's
 // bytes.
 cudaError_t launch_gbtrf_ragged(const RaggedDesc *descs, const int2 *items, int nitems, int kind,
@@ -67,8 +67,10 @@ void gbtrf_set_specialized(int on);
 cudaError_t launch_gbtrf(const GbtrfArgs &a, cudaStream_t st);
 cudaError_t launch_gbtrf_blk(const GbtrfArgs &a, int nb, int nw, cudaStream_t st);
 bool gbtrf_blk_supported(const FactorGeom &g, int nb, int nw);
-// Fills nb / nw left at 0 from the tuned table, else the built-in default.
-void gbtrf_blk_choice(char prec, const FactorGeom &g, int &nb, int &nw);
+// Fills nb / nw left at 0 from the tuned table, else the built-in default
+// (model: rows assembled from the model operator rather than read from a
+// packed band; the default warp count of the specialized instances differs).
+void gbtrf_blk_choice(char prec, const FactorGeom &g, int &nb, int &nw, bool model = false);
 void gbtrf_blk_set_choice(char prec, const FactorGeom &g, int nb, int nw);
 size_t gbtrf_blk_smem_bytes(int prec_bytes, const FactorGeom &g, int S, int nb, int nw);
 size_t gbtrf_smem_bytes(int prec_bytes, const FactorGeom &g, int S);

@@ -1,8 +1,9 @@
 """Shape tuner of the blocked band LU, keyed (precision, N, KL, KU).
 
 The blocked factor kernels take a panel width nb (4, 8, 16), a number of
-warps per system nw (1, 2, 4) and a form (phased, or lookahead with nw < 0 in
-the shape table).  Which one is fastest depends on the geometry, the
+warps per system nw (1, 2, 4, and 3 for the complex64 bandwidth-specialized
+geometries) and a form (phased, or lookahead with nw < 0 in the shape
+table).  Which one is fastest depends on the geometry, the
 precision and the row source (a packed band in HBM, or the synthetic operator
 assembled on the fly), so the choice is measured, not guessed: every
 candidate is timed with CUDA events on the device and the fastest is recorded
@@ -21,7 +22,7 @@ import numpy as np
 
 from . import _native as nat
 
-CANDIDATES = [(4, 1), (4, 2), (4, 4), (8, 1), (8, 2), (8, 4), (16, 2), (16, 4),
+CANDIDATES = [(4, 1), (4, 2), (4, 3), (4, 4), (8, 1), (8, 2), (8, 4), (16, 2), (16, 4),
               (4, -2), (4, -4), (8, -2), (8, -4)]
 
 

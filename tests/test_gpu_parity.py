@@ -119,10 +119,11 @@ def test_blocked_factor_equals_unblocked(lib, torch_cuda, n, kl, ku, prec):
 
 def test_specialized_factor_matches_generic(lib, torch_cuda):
     """The complex64 factor's compile-time bandwidth instances (KL = KU = 24,
-    34, 48, N a multiple of 4) give the generic instance's bits: factors,
-    pivots and info of packed bands with frequent pivoting (with and without
-    the fused forward elimination), and the mixed substeps of plans whose
-    operators assemble in the kernel, per case and as one ragged batch."""
+    34, 48, N a multiple of 4; two warps, and three for KL <= 34) give the
+    generic instance's bits: factors, pivots and info of packed bands with
+    frequent pivoting, and the mixed substeps of plans whose operators
+    assemble in the kernel (fused forward elimination), per case with two
+    and three warps and as one ragged batch."""
     torch = torch_cuda
     from suzerain_gb300 import multicase, plan as P, synth
     rng = np.random.default_rng(77)
@@ -140,39 +141,52 @@ def test_specialized_factor_matches_generic(lib, torch_cuda):
             ab = dev(torch, np.stack(bands))
             fe = lib.sgb_factor_elems(n, kl, ku)
             outs = []
-            for on in (0, 1):
+            three = kl <= 34 and n % 4 == 0
+            for on, nw in ((0, 2), (1, 2)) + (((1, 3),) if three else ()):
                 assert lib.sgb_gbtrf_set_specialized(on) == 0
                 fac = torch.full((nsys * fe,), float("nan"), dtype=torch.complex64, device="cuda")
                 ipiv = torch.zeros(nsys * n, dtype=torch.int32, device="cuda")
                 info = torch.zeros(nsys, dtype=torch.int32, device="cuda")
                 assert lib.sgb_gbtrf_batched_ex(b"C", nsys, n, kl, ku, ab.data_ptr(), ld, ld * n,
                                                 fac.data_ptr(), ipiv.data_ptr(), info.data_ptr(), 0,
-                                                4, 2, 0) == 0, lib.sgb_last_error().decode()
+                                                4, nw, 0) == 0, lib.sgb_last_error().decode()
                 torch.cuda.synchronize()
                 outs.append((fac.cpu().numpy().view(np.float32), ipiv.cpu().numpy(),
                              info.cpu().numpy()))
-            for x, y in zip(outs[0], outs[1]):
-                assert np.array_equal(x, y), (n, kl)
+            assert (lib.sgb_gbtrf_batched_ex(b"C", nsys, n, kl, ku, ab.data_ptr(), ld, ld * n,
+                                             fac.data_ptr(), ipiv.data_ptr(), info.data_ptr(), 0,
+                                             4, 3, 0) == 0) == three
+            for o in outs[1:]:
+                for x, y in zip(outs[0], o):
+                    assert np.array_equal(x, y), (n, kl)
         # plans (model assembly + fused forward elimination), KL = 24, 48, 34
         cfgs = [synth.Config("a", 5, 48, 6, 8, 8, synth.FOURPI, synth.FOURPI / 3, 1e-3, seed=11),
                 synth.Config("b", 7, 64, 8, 8, 6, synth.FOURPI, synth.FOURPI / 3, 1e-3, seed=12),
                 synth.Config("c", 5, 96, 8, 16, 8, synth.FOURPI, synth.FOURPI / 3, 1e-3, seed=13)]
         spec = P.RefineSpec(aiter=5, siter=3, diter=5, tolsc=145.0)
+        from suzerain_gb300 import tune as T
         res = {}
-        for on in (0, 1):
+        for on, ragged, nw in ((0, False, 0), (1, False, 0), (1, True, 0), (1, False, 3)):
             assert lib.sgb_gbtrf_set_specialized(on) == 0
-            for ragged in (False, True):
-                mc = multicase.MultiCase(cfgs, nstreams=2, ragged=ragged)
-                mc.capture("M", spec)
-                mc.reset()
-                mc.replay()
-                torch.cuda.synchronize()
-                res[(on, ragged)] = [mc.result(i).cpu().numpy() for i in range(len(cfgs))]
-                mc.close()
+            mc = multicase.MultiCase(cfgs, nstreams=2, ragged=ragged)
+            if nw:
+                for cs in mc.cases:
+                    if cs.KL <= 34:
+                        T.set_shape("C", cs.N, cs.KL, cs.KU, 4, nw)
+            mc.capture("M", spec)
+            mc.reset()
+            mc.replay()
+            torch.cuda.synchronize()
+            res[(on, ragged, nw)] = [mc.result(i).cpu().numpy() for i in range(len(cfgs))]
+            mc.close()
+            if nw:
+                for cs in mc.cases:
+                    if cs.KL <= 34:
+                        T.set_shape("C", cs.N, cs.KL, cs.KU, 4, 2)
         assert sorted(c.KL for c in mc.cases) == [24, 34, 48]
         for key, r in res.items():
             for i in range(len(cfgs)):
-                assert np.array_equal(r[i], res[(0, False)][i]), (key, i)
+                assert np.array_equal(r[i], res[(0, False, 0)][i]), (key, i)
     finally:
         lib.sgb_gbtrf_set_specialized(1)
 

@@ -271,16 +271,22 @@ def test_factor_shape_table(native):
         return tune.get_shape(prec, N, KL, KU)
 
     N, KL, KU = 960, 34, 34
-    assert get("C", N, KL, KU) == (4, 2)          # measured defaults at this geometry
+    # measured defaults at this geometry (packed band; the complex64 instance
+    # with the bandwidths fixed at compile time has a three-warp shape)
+    assert get("C", N, KL, KU) == (4, 3)
     assert get("Z", N, KL, KU) == (4, 1)
+    assert get("C", 962, KL, KU) == (4, 2)        # N not a multiple of 4: generic
+    L = native
+    assert L.sgb_gbtrf_set_shape(b"Z", N, KL, KU, 4, 3) != 0    # nw 3: complex64 only
+    assert L.sgb_gbtrf_set_shape(b"C", 962, KL, KU, 4, 3) != 0
+    assert L.sgb_gbtrf_set_shape(b"C", N, KL, KU, 8, 3) != 0
     assert get("C", 500, 60, 60)[1] == 4          # KL > 56 needs four warps
     geo = (731, 21, 17)                           # a geometry no other test records
     for nb, nw in ((8, 4), (16, 2), (4, -2), (8, -4), (4, 1)):
         tune.set_shape("C", *geo, nb, nw)
         assert get("C", *geo) == (nb, nw)
     assert get("Z", *geo) == (4, 1)               # keyed by precision
-    L = native
-    for bad in ((3, 2), (8, 3), (4, -1), (32, 2), (4, 0)):
+    for bad in ((3, 2), (8, 3), (4, 3), (4, -1), (4, -3), (32, 2), (4, 0)):
         assert L.sgb_gbtrf_set_shape(b"C", *geo, *bad) != 0, bad
     assert L.sgb_gbtrf_set_shape(b"X", *geo, 4, 2) != 0
     assert get("C", *geo) == (4, 1)               # rejected calls change nothing
@@ -374,7 +380,7 @@ def test_c99_caller_links_and_calls_the_library(native, tmp_path):
     assert out["wn"] == "-11 12"
     assert out["spec"] == "zcgbsvx,reuse=false,aiter=5,siter=25,diter=5,tolsc=145"
     assert out["bad"] == "-1"
-    assert out["shape"] == "4 2"
+    assert out["shape"] == "4 3"            # packed-band default at this geometry
     assert out["args"] == "1 58 3"          # suzerain/bsmbsm_aPxpby_real.def:47-56, bsmbsm_pack.def:43-64
 
 
