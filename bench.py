@@ -735,6 +735,52 @@ def run_config4(args) -> int:
     return 0
 
 
+def run_profile_factor(args) -> int:
+    """Profiling run of the complex64 factor on the first --nsys systems
+    (default 4096) of configuration 2, rows assembled from the model: one
+    mixed substep with two warps per system, then one with three (the
+    shapes of the bandwidth-specialized instance), each with one factor
+    launch; prints one JSON line of the factor's CUDA-event times and
+    exits."""
+    import torch
+    rank, local, world = dist_env()
+    if world > 1 and rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    from suzerain_gb300 import build as B
+    B.build()
+    from suzerain_gb300 import _native as nat, plan as P, synth, tune as T
+    L = nat.load()
+    if L.sgb_device_ok() != 0:
+        raise RuntimeError(nat.last_error())
+    nsys = args.nsys or 4096
+    cfg = synth.CONFIGS[2]
+    cs, kx, kz, u = cfg.batch()
+    kx, kz, u = kx[:nsys], kz[:nsys], u[:nsys]
+    phi_e, phi_i = synth.smr91_phis(cfg.phi)
+    pl = P.Plan(cs, kx, kz, max_double_slots=64)
+    du = torch.from_numpy(np.ascontiguousarray(u)).cuda()
+    out = torch.empty_like(du)
+    spec = P.RefineSpec(**SPEC)
+    saved = T.get_shape("C", cs.N, cs.KL, cs.KU)
+    times = {}
+    try:
+        pl.set_timing(True)
+        for nw in (2, 3):
+            T.set_shape("C", cs.N, cs.KL, cs.KU, 4, nw)
+            pl.substep("M", phi_e, phi_i, du, out, spec)
+            torch.cuda.synchronize()
+            t, n = pl.timings()["factor_c64"]
+            times[f"nw{nw}"] = t / n
+            pl.set_timing(False)
+            pl.set_timing(True)
+    finally:
+        T.set_shape("C", cs.N, cs.KL, cs.KU, *saved)
+        pl.close()
+    print(json.dumps({"profile_factor": True, "systems": nsys, "factor_ms": times}))
+    return 0
+
+
 def run_profile_kernels(args) -> int:
     """Profiling runs of the kernels beside the headline substep, on the
     first --nsys systems (default 4096) of configuration 2: the packed-band
@@ -899,9 +945,14 @@ def main():
                     help="print this GPU's pipe-throughput microbenchmarks and exit")
     ap.add_argument("--profile-kernels", action="store_true",
                     help="run the kernels beside the headline substep once each (profiling)")
+    ap.add_argument("--profile-factor", action="store_true",
+                    help="one mixed substep per complex64 factor shape, two then three warps "
+                         "(profiling)")
     args = ap.parse_args()
     if args.peaks:
         return run_peaks(args)
+    if args.profile_factor:
+        return run_profile_factor(args)
     if args.profile_kernels:
         return run_profile_kernels(args)
     if args.impl == "reference":
