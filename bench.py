@@ -453,9 +453,12 @@ def run_ours(args):
     hun, hon = hu.numpy(), ho.numpy()
     runner.substep_host(args.method, phi_e, phi_i, hun, hon, spec, stream=sptr)
     torch.cuda.synchronize()
+    e2e_step_ms = []
     t0 = time.perf_counter()
     for _ in range(args.e2e_steps):
+        t1 = time.perf_counter()
         runner.substep_host(args.method, phi_e, phi_i, hun, hon, spec, stream=sptr)
+        e2e_step_ms.append((time.perf_counter() - t1) * 1e3)
     e2e_s = time.perf_counter() - t0
     e2e = nsys * args.e2e_steps / e2e_s
     e2e_same = bool(np.array_equal(hon, x_mixed))
@@ -561,6 +564,9 @@ def run_ours(args):
             "clocks": clocks,
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(nsys * N * 16),
                     "d2h_bytes_per_step": int(nsys * N * 16), "steps": args.e2e_steps,
+                    "step_ms_min": min(e2e_step_ms),
+                    "step_ms_median": statistics.median(e2e_step_ms),
+                    "step_ms_max": max(e2e_step_ms),
                     "entry": "sgb_batch_substep_host (pinned host buffers, per-part copies "
                              "overlapped with the other parts' substeps)",
                     "same_result_as_device_entry": e2e_same},

@@ -1090,6 +1090,7 @@ struct sgb_batch {
     std::vector<int> bounds;                 // parts + 1 row offsets
     std::vector<cudaStream_t> streams;
     std::vector<cudaEvent_t> joins;
+    std::vector<cudaEvent_t> copied_in;      // host form: part i's copy in is done
     std::vector<double2 *> stage;            // host form: per-part device staging
     cudaEvent_t fork = nullptr;
     int nsys = 0, N = 0;
@@ -1114,6 +1115,7 @@ extern "C" int sgb_batch_destroy(sgb_batch *b)
         for (double2 *s : b->stage) if (s) cudaFreeAsync(s, g_pool.st);
     }
     for (cudaEvent_t e : b->joins) cudaEventDestroy(e);
+    for (cudaEvent_t e : b->copied_in) cudaEventDestroy(e);
     if (b->fork) cudaEventDestroy(b->fork);
     for (cudaStream_t s : b->streams) cudaStreamDestroy(s);
     delete b;
@@ -1148,10 +1150,13 @@ extern "C" sgb_batch *sgb_batch_create(const sgb_case *hcase, int nsys, const do
         if (sgb_plan_prepare(p, method) != 0) { sgb_batch_destroy(b); return nullptr; }
         cudaStream_t s = nullptr;
         cudaEvent_t e = nullptr;
+        cudaEvent_t c = nullptr;
         cudaError_t err = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
         if (err == cudaSuccess) b->streams.push_back(s);
         if (err == cudaSuccess) err = cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
         if (err == cudaSuccess) b->joins.push_back(e);
+        if (err == cudaSuccess) err = cudaEventCreateWithFlags(&c, cudaEventDisableTiming);
+        if (err == cudaSuccess) b->copied_in.push_back(c);
         if (err != cudaSuccess) {
             sgb_set_error(err, "sgb_batch_create(stream)", __FILE__, __LINE__);
             sgb_batch_destroy(b);
@@ -1244,8 +1249,16 @@ extern "C" int sgb_batch_substep_host(sgb_batch *b, char method, double phi_exp,
         sgb_plan *p = b->plans[i];
         const size_t off = (size_t) b->bounds[i] * b->N;
         const size_t bytes = (size_t) (b->bounds[i + 1] - b->bounds[i]) * b->N * sizeof(double2);
-        cudaError_t e = cudaMemcpyAsync(b->stage[i], reinterpret_cast<const double2 *>(u_in_host) + off,
-                                        bytes, cudaMemcpyHostToDevice, ps);
+        // The copies in follow one another (part i's after part i-1's):
+        // issued together they would share the link and every part's data
+        // would arrive only when all of it has; in order, part 0 starts
+        // computing after a quarter of the transfer and the parts finish
+        // staggered, so the early parts' copies out overlap the later work.
+        cudaError_t e = i ? cudaStreamWaitEvent(ps, b->copied_in[i - 1], 0) : cudaSuccess;
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(b->stage[i], reinterpret_cast<const double2 *>(u_in_host) + off,
+                                bytes, cudaMemcpyHostToDevice, ps);
+        if (e == cudaSuccess) e = cudaEventRecord(b->copied_in[i], ps);
         if (e != cudaSuccess) return sgb_set_error(e, "sgb_batch_substep_host(copy in)", __FILE__, __LINE__);
         std::lock_guard<std::mutex> pk(p->mu);
         int r = plan_substep(p, m, phi_exp, phi_imp, b->stage[i], b->stage[i], spec, ps, true);
