@@ -720,10 +720,11 @@ int sgb_gbtrs_set_quad_depth(int fwd, int bwd);
  *  spread over the system's four lanes.  Results are identical. */
 int sgb_gbtrs_set_quad_bulk(int rows);
 /** Complex64 blocked factor: instances with the bandwidths fixed at compile
- *  time (KL = KU = 24, 34 or 48 with N a multiple of 4, the geometries of
- *  S = 5 or 7 equations at B-spline order 6 or 8) on (1, the default) or
- *  off (0: every geometry takes the generic instance).  Process-wide; the
- *  factors are bit-identical either way. */
+ *  time (KL = KU = 24 or 34 with N a multiple of 4, the geometries of S = 5
+ *  or 7 equations at B-spline order 6 or 8 whose window leaves room for 8
+ *  systems per SM) on (1, the default) or off (0: every geometry takes the
+ *  generic instance).  Process-wide; the factors are bit-identical either
+ *  way. */
 int sgb_gbtrf_set_specialized(int on);
 /** Kernels that wait on asynchronous copies bound every wait; one whose
  *  wait ran out records a fault (its results are invalid).  Returns the

@@ -39,7 +39,7 @@ BLK_INST = "gbtrf_blk_inst.cu"
 BLK_VARIANTS = [(p, nb, fam) for nb in (16, 8, 4) for p in ("z", "c")
                 for fam in (0, 1, 2, 4)]
 # and once per bandwidth of the compile-time complex64 instances
-BLK_SPEC_BANDS = (24, 34, 48)
+BLK_SPEC_BANDS = (24, 34)
 
 
 def jobs() -> list[tuple[str, str, list[str]]]:

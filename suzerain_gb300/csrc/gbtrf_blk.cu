@@ -75,7 +75,9 @@ void gbtrf_blk_choice(char prec, const FactorGeom &g, int &nb, int &nw, bool mod
     // narrow panels and one warp.
     if (nb <= 0) nb = 4;
     if (nw == 0) {
-        nw = g.KL > 56 ? 4 : (prec == 'C' || g.KL > 52) ? 2 : 1;
+        // complex64 beyond KL = 40: four warps (KL = 48, N = 1344: 18 %
+        // faster than two with model rows, 46 % with a packed band)
+        nw = g.KL > 56 || (prec == 'C' && g.KL > 40) ? 4 : (prec == 'C' || g.KL > 52) ? 2 : 1;
         const int kb = prec == 'C' && nb == 4 && !model ? gbtrf_spec_band(g) : 0;
         if (kb && spec_has_w3(kb)) nw = 3;
     }
@@ -113,21 +115,19 @@ cudaError_t launch_blk_spec_any(const GbtrfArgs &a, int nw, cudaStream_t st, boo
     const int kb = gbtrf_spec_band(a.g);
     if (kb == 0 || (nw == 3 && !spec_has_w3(kb))) return cudaSuccess;
     *done = true;
-    switch (kb) {
-    case 24: return launch_blk_spec<24>(a, nw, st);
-    case 34: return launch_blk_spec<34>(a, nw, st);
-    default: return launch_blk_spec<48>(a, nw, st);
-    }
+    if (kb == 24) return launch_blk_spec<24>(a, nw, st);
+    return launch_blk_spec<34>(a, nw, st);
 }
 
 // Kind of the ragged factor instance for a plan of geometry g: the
-// specialized bandwidth instance as KB, else the generic one (-5 for
-// KL <= 40, -7 beyond); two warps (the rows are assembled from the model
-// operator, where a third warp gains nothing).
+// specialized bandwidth instance as KB (two warps: the rows are assembled
+// from the model operator, where a third warp gains nothing), else the
+// generic one as -(10 warps + rows per thread): -25 for KL <= 40, -43 for
+// KL <= 48, -44 for KL <= 56 (the default shapes of the phased kernel).
 int ragged_kind(const FactorGeom &g)
 {
     const int kb = gbtrf_spec_band(g);
-    return kb ? kb : (g.KL <= 40 ? -5 : -7);
+    return kb ? kb : (g.KL <= 40 ? -25 : g.KL <= 48 ? -43 : -44);
 }
 
 cudaError_t launch_gbtrf_ragged(const RaggedDesc *descs, const int2 *items, int nitems, int kind,
@@ -135,17 +135,18 @@ cudaError_t launch_gbtrf_ragged(const RaggedDesc *descs, const int2 *items, int 
 {
     if (nitems <= 0) return cudaSuccess;
     void (*kern)(const RaggedDesc *, const int2 *) = nullptr;
+    int nw = 2;
     switch (kind) {
-    case -5: kern = k_gbtrf_ragged<2, 5>; break;
-    case -7: kern = k_gbtrf_ragged<2, 7>; break;
+    case -25: kern = k_gbtrf_ragged<2, 5>; break;
+    case -43: kern = k_gbtrf_ragged<4, 3>; nw = 4; break;
+    case -44: kern = k_gbtrf_ragged<4, 4>; nw = 4; break;
     case 24: kern = k_gbtrf_ragged<2, spec_maxtr<24, 2>(), 24, 24, true>; break;
     case 34: kern = k_gbtrf_ragged<2, spec_maxtr<34, 2>(), 34, 34, true>; break;
-    case 48: kern = k_gbtrf_ragged<2, spec_maxtr<48, 2>(), 48, 48, true>; break;
     default: return cudaErrorInvalidValue;
     }
     cudaError_t e = smem_attr((const void *) kern, smem);
     if (e != cudaSuccess) return e;
-    kern<<<nitems, 64, smem, st>>>(descs, items);
+    kern<<<nitems, 32 * nw, smem, st>>>(descs, items);
     return cudaGetLastError();
 }
 

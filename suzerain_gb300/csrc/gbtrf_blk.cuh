@@ -1117,17 +1117,20 @@ cudaError_t launch_blk_fam(const GbtrfArgs &a, int nw, cudaStream_t st);
 
 // Bandwidths with compile-time instances of the complex64 phased kernel
 // (NB = 4; N a multiple of 4): the geometries of the B-spline operators
-// with S = 5 or 7 equations and order k = 6 or 8 (KL = KU = S (k - 1) - 1 =
-// 24, 34, 48).  Each has its own translation unit (gbtrf_blk_inst.cu with
-// SGB_BLK_SPEC set).  Two warps use the generic family's row tiles (5 rows
-// per thread for KL <= 40, 7 beyond); KL <= 36 also has a three-warp shape
-// (nw 3: 12 row groups x 3 rows cover KL, 3 x 5 register tiles), the
-// default for a packed band (10 % faster at N = 960, KL = 34) and as fast
-// as two warps when the rows are assembled from the model operator, whose
-// default stays two.
-constexpr int kSpecBands[] = {24, 34, 48};
+// with S = 5 or 7 equations and order k = 6 or 8 whose window leaves room
+// for 8 CTAs per SM (KL = KU = S (k - 1) - 1 = 24, 34).  Each has its own
+// translation unit (gbtrf_blk_inst.cu with SGB_BLK_SPEC set).  Two warps
+// use 5 x 5 register tiles; the three-warp shape (nw 3: 12 row groups x 3
+// rows cover KL, 3 x 5 tiles) is the default for a packed band (10 % faster
+// at N = 960, KL = 34) and as fast as two warps when the rows are assembled
+// from the model operator, whose default stays two.  KL = 48 (S = 7, k = 8)
+// takes the generic four-warp kernel: its 48 KB window allows 4 CTAs per SM,
+// so four warps with 3 x 5 tiles fit without spills, measured 18 % (model
+// rows) to 37 % (packed band) faster than two, and fixing KL there gains
+// nothing.
+constexpr int kSpecBands[] = {24, 34};
 constexpr bool spec_has_w3(int kb) { return kb <= 36; }
-template <int KB, int W> constexpr int spec_maxtr() { return W == 3 ? 3 : (KB <= 40 ? 5 : 7); }
+template <int KB, int W> constexpr int spec_maxtr() { return W == 3 ? 3 : 5; }
 template <int KB>
 cudaError_t launch_blk_spec(const GbtrfArgs &a, int nw, cudaStream_t st);
 // The specialized launch for a's geometry and warp count when one exists

@@ -52,14 +52,14 @@ struct RaggedDesc {
 };
 // The ragged factor over descriptors and (descriptor, list position) items
 // in device memory, one CTA per item; kind (ragged_kind of every item's
-// geometry) KB for the compile-time bandwidth instances (two warps), -5 for
-// the generic one with KL <= 40, -7 for KL <= 56; smem the largest window's
-// bytes.
+// geometry) KB for the compile-time bandwidth instances (two warps), -25,
+// -43, -44 for the generic ones (two warps KL <= 40, four warps KL <= 48,
+// KL <= 56); smem the largest window's bytes.
 cudaError_t launch_gbtrf_ragged(const RaggedDesc *descs, const int2 *items, int nitems, int kind,
                                 size_t smem, cudaStream_t st);
 int ragged_kind(const FactorGeom &g);
 // The compile-time bandwidth of the complex64 phased factor's instance for
-// g (KL = KU in 24, 34, 48 and N % 4 == 0), or 0 for the generic instance;
+// g (KL = KU in 24, 34 and N % 4 == 0), or 0 for the generic instance;
 // gbtrf_set_specialized(0) makes every geometry take the generic one.
 int gbtrf_spec_band(const FactorGeom &g);
 void gbtrf_set_specialized(int on);
