@@ -140,8 +140,8 @@ cudaError_t launch_gbtrf_ragged(const RaggedDesc *descs, const int2 *items, int 
     case -25: kern = k_gbtrf_ragged<2, 5>; break;
     case -43: kern = k_gbtrf_ragged<4, 3>; nw = 4; break;
     case -44: kern = k_gbtrf_ragged<4, 4>; nw = 4; break;
-    case 24: kern = k_gbtrf_ragged<2, spec_maxtr<24, 2>(), 24, 24, true>; break;
-    case 34: kern = k_gbtrf_ragged<2, spec_maxtr<34, 2>(), 34, 34, true>; break;
+    case 24: kern = k_gbtrf_ragged<2, spec_maxtr<2>(), 24, 24, true>; break;
+    case 34: kern = k_gbtrf_ragged<2, spec_maxtr<2>(), 34, 34, true>; break;
     default: return cudaErrorInvalidValue;
     }
     cudaError_t e = smem_attr((const void *) kern, smem);

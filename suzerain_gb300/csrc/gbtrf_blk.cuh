@@ -432,7 +432,10 @@ constexpr int blk_min_blocks()
 // change the instruction stream, not the arithmetic: the factors are
 // bit-identical to the generic instance's.  PROF: the per-phase cycle
 // counters (diagnostics) are compiled in and kept when prof is set; without
-// it the counting code and its branches are absent.
+// it the counting code and its branches are absent.  MST: how the model
+// source is passed, by value (the phased kernel: a kernel parameter) or as
+// a reference to the ragged kernel's shared-memory descriptor (fewer live
+// registers).
 template <typename R, int NB, int NW, int MAXTR, bool MODEL, bool FWD, typename MST = ModelSource,
           int CKL = 0, int CKU = 0, bool NFULL = false, bool PROF = false>
 __device__ __forceinline__ void
@@ -1130,7 +1133,7 @@ cudaError_t launch_blk_fam(const GbtrfArgs &a, int nw, cudaStream_t st);
 // nothing.
 constexpr int kSpecBands[] = {24, 34};
 constexpr bool spec_has_w3(int kb) { return kb <= 36; }
-template <int KB, int W> constexpr int spec_maxtr() { return W == 3 ? 3 : 5; }
+template <int W> constexpr int spec_maxtr() { return W == 3 ? 3 : 5; }
 template <int KB>
 cudaError_t launch_blk_spec(const GbtrfArgs &a, int nw, cudaStream_t st);
 // The specialized launch for a's geometry and warp count when one exists

@@ -29,7 +29,7 @@ cudaError_t launch_blk_fam(const GbtrfArgs &a, int nw, cudaStream_t st)
 template <int KB, int W>
 cudaError_t launch_blk_spec_w(const GbtrfArgs &a, cudaStream_t st)
 {
-    constexpr int MT = spec_maxtr<KB, W>();
+    constexpr int MT = spec_maxtr<W>();
     const bool fwd = a.rhs != nullptr;
     if (a.model)
         return fwd ? launch_cta_one<float, 4, W, MT, false, true, true, KB, KB, true>(a, st)

@@ -259,6 +259,48 @@ def test_bsmbsm_permutation_layout(native):
     assert not native.suzerain_bsmbsm_permutation(0, 12)
 
 
+def test_ragged_and_stage_entries_check_arguments(native):
+    """The ragged-batch and staged-substep entries reject bad arguments
+    before touching the device (host logic, no GPU): null plans and batches,
+    empty batches, stages other than 1 and 2, methods other than 'M'."""
+    L = native
+    assert L.sgb_ragged_create(None, 0, None, None) is None
+    assert "sgb_ragged_create" in L.sgb_last_error().decode()
+    assert L.sgb_ragged_create(None, 2, None, None) is None
+    assert L.sgb_ragged_factor(None, None) != 0
+    assert "sgb_ragged_factor" in L.sgb_last_error().decode()
+    L.sgb_ragged_destroy(None)                      # no-op
+    from suzerain_gb300 import _native as nat
+    buf = np.zeros(4, dtype=np.complex128)
+    p = buf.ctypes.data
+    spec = nat.RefineSpec(5, 25, 5, 145.0)
+    for stage, method in ((1, b"M"), (3, b"M"), (1, b"Z")):
+        assert L.sgb_plan_substep_stage(None, stage, method, 0.0, 1e-3, p, p, C.byref(spec), None) != 0
+        assert "sgb_plan_substep_stage" in L.sgb_last_error().decode()
+
+
+def test_specialized_switch_and_wide_band_defaults(native):
+    """Default factor shapes follow the compile-time-bandwidth instances:
+    three warps for a packed complex64 band at KL = KU = 34 with them, two
+    without (sgb_gbtrf_set_specialized(0)), four beyond KL = 40; complex128
+    keeps one warp up to KL = 52 (host logic, no GPU)."""
+    from suzerain_gb300 import tune
+    L = native
+    try:
+        assert L.sgb_gbtrf_set_specialized(0) == 0
+        assert tune.get_shape("C", 1920, 34, 34) == (4, 2)
+        assert L.sgb_gbtrf_set_shape(b"C", 1920, 34, 34, 4, 3) != 0   # no three-warp shape off
+        assert L.sgb_gbtrf_set_specialized(1) == 0
+        assert tune.get_shape("C", 1920, 34, 34) == (4, 3)
+        assert tune.get_shape("C", 1920, 24, 24) == (4, 3)
+        assert tune.get_shape("C", 1344, 48, 48) == (4, 4)
+        assert tune.get_shape("C", 1346, 41, 41) == (4, 4)
+        assert tune.get_shape("C", 1344, 40, 40) == (4, 2)
+        assert tune.get_shape("Z", 1344, 48, 48) == (4, 1)
+    finally:
+        L.sgb_gbtrf_set_specialized(1)
+
+
 def test_factor_shape_table(native):
     """The process-wide shape table of the blocked factor (host logic, no
     GPU): built-in defaults per precision, recorded shapes per (precision,
