@@ -1129,14 +1129,16 @@ def test_multicase_graph_matches_eager(lib, torch_cuda):
 
 
 def test_ragged_factor_matches_per_case(lib, torch_cuda):
-    """One complex64 factor launch per row-tile class over every case of a
-    substep (KL = 24, 48 and 39: both classes) gives the per-case step's
-    bits, replayed from a CUDA graph and issued directly."""
+    """One complex64 factor launch per kernel kind over every case of a
+    substep (KL = 24: specialized; 39: generic two warps; 48 and 55: generic
+    four warps with three and four rows per thread) gives the per-case
+    step's bits, replayed from a CUDA graph and issued directly."""
     torch = torch_cuda
     from suzerain_gb300 import multicase, plan as P, synth
     cfgs = [synth.Config("a", 5, 48, 6, 8, 8, synth.FOURPI, synth.FOURPI / 3, 1e-3, seed=11),
             synth.Config("b", 7, 64, 8, 8, 6, synth.FOURPI, synth.FOURPI / 3, 1e-3, seed=12),
-            synth.Config("c", 5, 96, 9, 16, 8, synth.FOURPI, synth.FOURPI / 3, 1e-3, seed=13)]
+            synth.Config("c", 5, 96, 9, 16, 8, synth.FOURPI, synth.FOURPI / 3, 1e-3, seed=13),
+            synth.Config("d", 7, 40, 9, 8, 6, synth.FOURPI, synth.FOURPI / 3, 1e-3, seed=14)]
     spec = P.RefineSpec(aiter=5, siter=3, diter=5, tolsc=145.0)
     ref = multicase.MultiCase(cfgs, nstreams=2)
     ref.capture("M", spec)
@@ -1145,7 +1147,7 @@ def test_ragged_factor_matches_per_case(lib, torch_cuda):
     torch.cuda.synchronize()
     want = [ref.result(i).cpu().numpy() for i in range(len(cfgs))]
     kls = sorted(cs.KL for cs in ref.cases)
-    assert kls[0] <= 40 < kls[-1] <= 56, kls
+    assert kls == [24, 39, 48, 55], kls
     rg = multicase.MultiCase(cfgs, nstreams=2, ragged=True)
     rg.capture("M", spec)
     rg.reset()
