@@ -78,8 +78,11 @@ void gbtrf_blk_choice(char prec, const FactorGeom &g, int &nb, int &nw, bool mod
         // complex64 beyond KL = 40: four warps (KL = 48, N = 1344: 18 %
         // faster than two with model rows, 46 % with a packed band)
         nw = g.KL > 56 || (prec == 'C' && g.KL > 40) ? 4 : (prec == 'C' || g.KL > 52) ? 2 : 1;
-        const int kb = prec == 'C' && nb == 4 && !model ? gbtrf_spec_band(g) : 0;
-        if (kb && spec_has_w3(kb)) nw = 3;
+        // the three-warp shape: every specialized band with a packed
+        // source; with model rows at KL = 34 (5 % faster there, N = 960),
+        // while KL = 24 measured faster with two
+        const int kb = prec == 'C' && nb == 4 ? gbtrf_spec_band(g) : 0;
+        if (kb && spec_has_w3(kb) && (!model || kb == 34)) nw = 3;
     }
 }
 
@@ -120,10 +123,11 @@ cudaError_t launch_blk_spec_any(const GbtrfArgs &a, int nw, cudaStream_t st, boo
 }
 
 // Kind of the ragged factor instance for a plan of geometry g: the
-// specialized bandwidth instance as KB (two warps: the rows are assembled
-// from the model operator, where a third warp gains nothing), else the
-// generic one as -(10 warps + rows per thread): -25 for KL <= 40, -43 for
-// KL <= 48, -44 for KL <= 56 (the default shapes of the phased kernel).
+// specialized bandwidth instance as KB (two warps: the three-warp form of
+// the ragged kernel, whose descriptor adds live registers, still spills at
+// 80), else the generic one as -(10 warps + rows per thread): -25 for
+// KL <= 40, -43 for KL <= 48, -44 for KL <= 56 (the default shapes of the
+// phased kernel).
 int ragged_kind(const FactorGeom &g)
 {
     const int kb = gbtrf_spec_band(g);

@@ -301,15 +301,15 @@ __device__ __forceinline__ void panel_factor(cplx_t<R> *__restrict__ win, int P,
 // Rows r0 .. r0+nr-1 of A (rows outside 0..N-1 read as zero) at columns
 // cbase + cc, 0 <= cc < WC (columns outside 0..N-1 zero), handed to
 // put(k, cc, value) for every k < nr, cc < WC.  One warp, lanes over cc.  The
-// band reads of a group of rows x three column passes are all issued before
-// any value is formed, so the latency of the source (the float band copies
-// in L2 for the model, HBM for a packed band) is paid once per group instead
-// of once per entry.
+// band reads of a group of GR rows x GC column passes of 32 are all issued
+// before any value is formed, so the latency of the source (the float band
+// copies in L2 for the model, HBM for a packed band) is paid once per group
+// instead of once per entry; smaller groups hold fewer registers.
 template <typename R, bool MODEL> struct BandRaw { using type = double2; };
 template <> struct BandRaw<float, true> { using type = float4; };
 template <> struct BandRaw<double, true> { using type = double3; };
 
-template <typename R, bool MODEL, typename Put>
+template <typename R, bool MODEL, int GR = 2, int GC = 3, typename Put>
 __device__ __forceinline__ void assemble_rows(const PackedSource &src, const ModelSource &ms,
                                               const cplx_t<R> *coef, unsigned magic, int s, int N,
                                               int KL, int KU, int WC, int r0, int nr, int cbase,
@@ -317,8 +317,6 @@ __device__ __forceinline__ void assemble_rows(const PackedSource &src, const Mod
 {
     using T2 = cplx_t<R>;
     using Raw = typename BandRaw<R, MODEL>::type;
-    constexpr int GR = 2;                                    // rows per group
-    constexpr int GC = 3;                                    // column passes per group
     const int S = MODEL ? ms.cs.S : 1, SS = S * S;
     for (int k0 = 0; k0 < nr; k0 += GR) {
         for (int c0 = 0; c0 < WC; c0 += 32 * GC) {
@@ -539,9 +537,12 @@ gbtrf_cta_system(const FactorGeom g, int s, long long fi, const PackedSource src
             // the next nbk rows of A, at the next window's columns
             if (more) {
                 const int kb = nbk * (warp - 1) / (NW - 1), ke = nbk * warp / (NW - 1);
-                assemble_rows<R, MODEL>(src, ms, coef, magic, s, N, KL, KU, WC, j0 + WR + kb, ke - kb,
-                                        j0 + nbk, lane,
-                                        [&](int k, int cc, T2 v) { stg[(kb + k) * WC + cc] = v; });
+                // three staging warps: one row and two column passes per
+                // load group (fewer live registers: no spills at the
+                // 80-register bound of the three-warp instances)
+                assemble_rows<R, MODEL, (NW >= 3 ? 1 : 2), (NW >= 3 ? 2 : 3)>(
+                    src, ms, coef, magic, s, N, KL, KU, WC, j0 + WR + kb, ke - kb, j0 + nbk, lane,
+                    [&](int k, int cc, T2 v) { stg[(kb + k) * WC + cc] = v; });
                 if (FWD)
                     for (int k = tid - 32; k < nbk; k += NT - 32) {
                         const int r = j0 + WR + k;
@@ -1125,8 +1126,9 @@ cudaError_t launch_blk_fam(const GbtrfArgs &a, int nw, cudaStream_t st);
 // translation unit (gbtrf_blk_inst.cu with SGB_BLK_SPEC set).  Two warps
 // use 5 x 5 register tiles; the three-warp shape (nw 3: 12 row groups x 3
 // rows cover KL, 3 x 5 tiles) is the default for a packed band (10 % faster
-// at N = 960, KL = 34) and as fast as two warps when the rows are assembled
-// from the model operator, whose default stays two.  KL = 48 (S = 7, k = 8)
+// at N = 960, KL = 34) and, at KL = 34, for rows assembled from the model
+// operator (5 % faster once the staging's load groups shrank to fit 80
+// registers); model rows at KL = 24 keep two.  KL = 48 (S = 7, k = 8)
 // takes the generic four-warp kernel: its 48 KB window allows 4 CTAs per SM,
 // so four warps with 3 x 5 tiles fit without spills, measured 18 % (model
 // rows) to 37 % (packed band) faster than two, and fixing KL there gains
