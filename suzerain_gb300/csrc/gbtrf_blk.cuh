@@ -745,10 +745,10 @@ k_gbtrf_cta(FactorGeom g, int nsys, PackedSource src, ModelSource ms,
 // Ragged factor: one CTA per work item (plan d, list position k), the
 // items in the order given (the largest plans' systems first, which the
 // block scheduler dispatches first); each item is one system of one plan,
-// of that plan's own geometry (KL <= 8 MAXTR; KL = CKL, KU = CKU and N a
+// of that plan's own geometry (KL <= 4 NW MAXTR; KL = CKL, KU = CKU and N a
 // multiple of 4 in the specialized instances), or nothing when k is beyond
 // the plan's active count.  The plan's descriptor is read once into shared
-// memory (fewer registers than a copy in registers; no spills at MAXTR 5).
+// memory (fewer live registers than a copy in registers).
 // The shared memory is sized for the largest window of the batch.
 template <int NW, int MAXTR, int CKL = 0, int CKU = 0, bool NFULL = false>
 __global__ void __launch_bounds__(32 * NW, (blk_min_blocks<float, NW>()))
